@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Benchmark: Biot-Savart velocity + velocity-gradient interactions/s on GB300.
+
+Workload (one "step"): one direct-sum evaluation of velocity and the 9-component
+velocity gradient at every particle of the precision cloud -- N = 262,144 particles,
+positions N(0, 0.3^2) per axis, strength components N(0,1)*1e-3, core radii U[0.01,
+0.03], Gaussian core, targets = sources (N^2 = 6.87e10 interactions including i = j).
+Inputs are seeded synthetic data generated here.
+
+value : interactions/s of the chosen form (COMPENSATED FP32) with inputs resident in
+        HBM, device time per step from CUDA events on the launching stream; L2 is
+        flushed (256 MiB write) between timed steps (inputs are 8 MiB, below L2).
+e2e   : the same metric through the C-ABI with host (pinned) buffers: host->device
+        copies, the sums and the device->host copy of the results in every step.
+The plain FP32 drop-in path, the FP64 comparator on the same GPU, the errors of every
+path against the FP64 sums, and the reference CPU baseline ride along in the line.
+
+--impl reference times the reference's CPU algorithm for the same metric: the oracle
+port (oracle/o3d_oracle.cpp: the reference's loops, float pair arithmetic with double
+accumulators like its non-Vc build, OpenMP over targets) on the host's cores.
+Multi-GPU (torchrun): every rank runs an independent replica ("replicas only": the
+reference is single-GPU and this path has no data exchange); value sums the ranks'
+interactions over the max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Biot-Savart vel+grad interactions/s at stated FP64-oracle error"
+UNIT = "interactions/s"
+CORE = "gauss"
+N_DEFAULT = 262144
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--core", default=CORE)
+    ap.add_argument("--skip-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config(args):
+    return {"workload": "precision cloud: N=%d Gaussian-core particles, self-interaction vel+grad" % args.n,
+            "n_particles": args.n, "core": args.core, "interactions_per_step": args.n * args.n,
+            "targets_have_radius": True, "l2": "flushed between timed steps (256 MiB write); inputs 8 MiB",
+            "seed": 2, "parallelism": "replicas"}
+
+
+# ------------------------------------------------------------------------------------
+def cpu_reference(args, nthreads=None, ntarg=None, reps=1):
+    """Times the oracle port on a bounded sample: `ntarg` targets against all sources."""
+    import oracle
+    from omega3d_gb300 import workloads as W
+    x, s, r = W.gaussian_cloud(args.n, seed=2)
+    nthreads = nthreads or (os.cpu_count() or 1)
+    ntarg = ntarg or min(args.n, 1024)
+    idx = np.linspace(0, args.n - 1, ntarg).astype(np.int64)
+    tx, tr = np.ascontiguousarray(x[:, idx]), np.ascontiguousarray(r[idx])
+    oracle.points_affect_points(x[:, :4096], r[:4096], s[:, :4096], tx[:, :64], tr[:64], True, args.core, 1,
+                                nthreads)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.points_affect_points(x, r, s, tx, tr, True, args.core, 1, nthreads)
+        times.append(time.perf_counter() - t0)
+    pairs = float(ntarg) * args.n
+    return pairs / statistics.median(times), nthreads, "%d targets x %d sources per sample" % (ntarg, args.n), times
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    samples = []
+    for k in range(args.warmup + args.steps):
+        v, cores, sample, _ = cpu_reference(args)
+        if k >= args.warmup:
+            samples.append(v)
+    v = statistics.median(samples)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(args.n) * args.n / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (pairs) / f64 (accumulators)", "data": "synthetic",
+            "config": config(args), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [c.strip() for c in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.remove(self.path)
+        if not rows:
+            return None
+        sm = [float(f[1]) for f in rows if f[1].replace(".", "").isdigit()]
+        mx = [float(f[2]) for f in rows if f[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for f in rows for i in range(4) if f[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import omega3d_gb300 as G
+    from omega3d_gb300 import _lib as L
+    from omega3d_gb300 import workloads as W
+    from omega3d_gb300.metrics import rel_err
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    lib = L.lib()
+
+    x, s, r = W.gaussian_cloud(args.n, seed=2)
+    X, S, R = (torch.from_numpy(a).to(dev) for a in (x, s, r))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    nsm = int(torch.cuda.get_device_properties(dev).multi_processor_count)
+    tfl, ms = ctypes.c_double(0), ctypes.c_float(0)
+    L.check(lib.o3g_fp32_peak_probe(20000, stream.cuda_stream, ctypes.byref(tfl),
+                                    ctypes.byref(ms)), "o3g_fp32_peak_probe")
+    fp32_peak = float(tfl.value)
+
+    fl_pair = lib.o3g_flops_per_pair(L.CORES[args.core], 1, 1)
+    pairs = float(args.n) * args.n
+    ref_flops = pairs * fl_pair + 12.0 * args.n
+
+    def one(prec, p=None):
+        p = p or G.Points(X, S, R)
+        p.zero_vels()
+        G.points_affect_points(p, p, G.ResultsType(), G.ExecEnv(args.core, prec))
+        return p
+
+    def timed(prec, steps, warmup):
+        p = G.Points(X, S, R)
+        for _ in range(warmup):
+            one(prec, p)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        lib.o3g_set_timing(1)
+        n0 = L.launch_count()
+        step_ms, kern_ms = [], []
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            one(prec, p)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            km = ctypes.c_float(0)
+            L.check(lib.o3g_last_kernel_ms(ctypes.byref(km)), "o3g_last_kernel_ms")
+            kern_ms.append(float(km.value))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        launches = L.launch_count() - n0
+        lib.o3g_set_timing(0)
+        return p, step_ms, kern_ms, wall, launches
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    pc, comp_ms, comp_kms, comp_wall, comp_launches = timed("compensated", args.steps, args.warmup)
+    pp, plain_ms, plain_kms, _, _ = timed("plain", args.steps, args.warmup)
+    clk = clocks.stop()
+
+    # e2e through the C-ABI with pinned host buffers: H2D + sums + D2H every step
+    pinned = [torch.from_numpy(a).pin_memory() for a in (x, s, r)]
+    pinned += [torch.zeros(3, args.n).pin_memory(), torch.zeros(9, args.n).pin_memory()]
+    hp = G.Points(pinned[0].numpy(), pinned[1].numpy(), pinned[2].numpy(), u=pinned[3].numpy(),
+                  ug=pinned[4].numpy())
+    for _ in range(max(1, args.warmup)):
+        hp.zero_vels()
+        G.points_affect_points(hp, hp, G.ResultsType(), G.ExecEnv(args.core, "compensated"))
+    e2e_s = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        hp.zero_vels()
+        t0 = time.perf_counter()
+        G.points_affect_points(hp, hp, G.ResultsType(), G.ExecEnv(args.core, "compensated"))
+        e2e_s.append(time.perf_counter() - t0)
+    h2d = 7 * 4 * args.n + 12 * 4 * args.n     # 7 source arrays + the 12 output arrays staged in
+    d2h = 12 * 4 * args.n
+
+    # FP64 comparator on the same GPU (subset of targets) and the errors of every path
+    nsub = min(args.n, 16384)
+    sub = torch.linspace(0, args.n - 1, nsub, device=dev).long()
+    fp64 = None
+    if not args.skip_fp64:
+        Xd, Sd, Rd = X.double(), S.double(), R.double()
+        tq = G.Points(Xd[:, sub].contiguous(), None, Rd[sub].contiguous())
+        src = G.Points(Xd, Sd, Rd)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        G.points_affect_points(src, tq, G.ResultsType(), G.ExecEnv(args.core, "fp64"))
+        e1.record(stream)
+        e1.synchronize()
+        fp64_rate = float(nsub) * args.n / (e0.elapsed_time(e1) * 1e-3)
+        u64, g64 = tq.u.cpu().numpy(), tq.ug.cpu().numpy()
+        subn = sub.cpu().numpy()
+        errs = {}
+        for name, p in (("compensated", pc), ("plain", pp)):
+            eu = rel_err(p.u.cpu().numpy()[:, subn], u64)
+            eg = rel_err(p.ug.cpu().numpy()[:, subn], g64)
+            errs[name] = {"u_max": eu[0], "u_rms": eu[1], "grad_max": eg[0], "grad_rms": eg[1]}
+        fp64 = {"value": fp64_rate, "unit": UNIT, "targets": nsub, "errors_vs_fp64": errs}
+
+    comp_step = statistics.median(comp_ms)
+    plain_step = statistics.median(plain_ms)
+    comp_k = statistics.median(comp_kms)
+    plain_k = statistics.median(plain_kms)
+    local_rate = pairs / (comp_step * 1e-3)
+
+    # whole-job numbers: max time over ranks, interactions summed
+    step_max = comp_step
+    if world > 1:
+        t = torch.tensor([comp_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_max = float(t.item())
+    value = world * pairs / (step_max * 1e-3)
+
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tr = json.load(open(tpath)).get("k_pair_gauss_compensated")
+            if tr and tr.get("n") and tr.get("bytes"):
+                traffic = tr["bytes"] * (args.n / tr["n"]) ** 2 if tr.get("scales") == "n^2" else tr["bytes"]
+        except Exception:
+            traffic = None
+
+    if rank == 0:
+        cpu_v, cpu_cores, cpu_sample, _ = cpu_reference(args)
+        achieved = ref_flops / (comp_k * 1e-3) / 1e12
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(args),
+            "path": "compensated FP32 (two-sum accumulators, Newton-refined rsqrt)",
+            "error_vs_fp64": fp64["errors_vs_fp64"]["compensated"] if fp64 else None,
+            "e2e": {"value": world * pairs / statistics.median(e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "path": "o3g_points_affect_points, O3G_MEM_HOST, pinned buffers"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak, "traffic": traffic,
+                         "kernel": "k_pair<GAUSS, COMPENSATED, grads>",
+                         "flops_per_interaction": fl_pair,
+                         "peak_source": "measured in this run: o3g_fp32_peak_probe FMA chains (no FP32 figure in "
+                                        "MEASURED_PEAKS.json)",
+                         "kernel_ms": comp_k},
+            "plain": {"value": world * pairs / (plain_step * 1e-3), "unit": UNIT, "kernel_ms": plain_k,
+                      "roofline_frac": ref_flops / (plain_k * 1e-3) / 1e12 / fp32_peak,
+                      "error_vs_fp64": fp64["errors_vs_fp64"]["plain"] if fp64 else None},
+            "compensated_over_plain": plain_step / comp_step,
+            "fp64_same_gpu": fp64 and {"value": fp64["value"], "unit": UNIT, "targets": fp64["targets"],
+                                       "compensated_speedup": local_rate / fp64["value"]},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_sample},
+            "clocks": clk, "gpu_launches": comp_launches, "num_sms": nsm,
+            "wall_s_timed_region": comp_wall,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,116 @@
+/*
+ * o3dgpu.h -- C-ABI of the GB300 (sm_103a) Biot-Savart / BEM hot path of Omega3D.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and returns an
+ * int32 status (O3G_OK == 0).  No entry point allocates caller-visible memory: the
+ * caller owns every array, as in the reference (Influence.h / Coefficients.h /
+ * BEM.h, where the caller's std::vector<float> SoA arrays are read and accumulated
+ * into).  Array arguments follow the reference's SoA layout: one pointer per
+ * component (x, y, z; u, v, w; nine velocity-gradient components in the order
+ * du/dx, dv/dx, dw/dx, du/dy, dv/dy, dw/dy, du/dz, dv/dz, dw/dz -- Kernels.h:184-192).
+ *
+ * `mem` says where the arrays live: O3G_MEM_HOST (the library stages them through
+ * device memory inside the call and returns after the results are back in host
+ * memory) or O3G_MEM_DEVICE (device pointers; the call is asynchronous on `stream`).
+ * `stream` is a cudaStream_t (NULL = the legacy default stream).
+ *
+ * Velocity results ACCUMULATE (+=) into the caller's arrays, exactly like the
+ * reference's points_affect_points (Influence.h:299-308); zero_vels / finalize_vels
+ * (the 1/4pi factor and the freestream) stay with the caller (Convection.h:161,175).
+ */
+#ifndef O3DGPU_H
+#define O3DGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+enum {
+  O3G_OK = 0,
+  O3G_ERR_INVALID_ARG = 1,   /* bad size, null pointer, unknown enum value          */
+  O3G_ERR_CUDA = 2,          /* a CUDA runtime call failed (see o3g_last_error)    */
+  O3G_ERR_NO_DEVICE = 3,     /* no usable sm_103 device                            */
+  O3G_ERR_ALLOC = 4,         /* device workspace could not be allocated            */
+  O3G_ERR_NOT_CONVERGED = 5, /* iterative refinement did not reach the tolerance   */
+  O3G_ERR_TIMEOUT = 6,       /* a bounded device-side wait ran out                 */
+  O3G_ERR_SINGULAR = 7,      /* zero or non-finite pivot in a factorisation        */
+  O3G_ERR_NONFINITE = 8,     /* non-finite values where finite ones are required   */
+  O3G_ERR_STATE = 9          /* call made in the wrong state (e.g. solve before A) */
+};
+
+/* ---- enumerations -------------------------------------------------------------- */
+/* Regularised Biot-Savart cores.  RM/WL/EXP/V2 follow CoreFunc.h (:43-83, :241-289,
+ * :86-238, :292-341); GAUSS is this library's own Gaussian core (no counterpart in
+ * the reference, whose Gaussian kernels serve diffusion only). */
+enum { O3G_CORE_RM = 0, O3G_CORE_WL = 1, O3G_CORE_EXP = 2, O3G_CORE_GAUSS = 3, O3G_CORE_V2 = 4 };
+
+/* Arithmetic of the pair sums:
+ *  PLAIN       FP32 pair arithmetic and FP32 accumulation (the reference's Vc path);
+ *  COMPENSATED FP32 pair arithmetic with a Newton-refined rsqrt and per-tile partial
+ *              sums folded into two-sum (hi, lo) accumulators;
+ *  FP64        everything in double (comparator / oracle on the device). */
+enum { O3G_PREC_PLAIN = 0, O3G_PREC_COMPENSATED = 1, O3G_PREC_FP64 = 2 };
+
+enum { O3G_MEM_HOST = 0, O3G_MEM_DEVICE = 1 };
+
+/* ---- library ------------------------------------------------------------------- */
+/* Human-readable text for a status code (static storage). */
+const char* o3g_status_string(int32_t status);
+/* Last CUDA / validation message recorded by this thread (static per-thread storage). */
+const char* o3g_last_error(void);
+/* Library version as 10000*major + 100*minor + patch. */
+int32_t o3g_version(void);
+/* Device facts used for rooflines: SM count, SM clock (kHz), compute capability. */
+int32_t o3g_device_info(int32_t* num_sms, int32_t* sm_clock_khz, int32_t* cc_major, int32_t* cc_minor);
+
+/* Reference flop count per interaction (Kernels.h:49,93,154,252 + CoreFunc.h flops_*):
+ * grads != 0 -> vel+grad kernel; have_tr != 0 -> thick-cored target.  Mirrors the
+ * counts the reference uses to print GFlop/s (Influence.h:310,366,475,534). */
+int32_t o3g_flops_per_pair(int32_t core, int32_t grads, int32_t have_tr);
+
+/* Device time (ms) of the main kernel of the most recent call on this thread, when
+ * timing is enabled with o3g_set_timing(1); returns O3G_ERR_STATE otherwise. */
+int32_t o3g_set_timing(int32_t enable);
+int32_t o3g_last_kernel_ms(float* ms);
+/* Cumulative number of CUDA kernels this thread has launched through the library. */
+int32_t o3g_launch_count(uint64_t* n);
+
+/* Measures the FP32 FMA throughput of the current device (TFLOP/s, counting an FMA as
+ * 2 flops) with a register-resident FMA-chain kernel: the measured denominator of the
+ * pair kernels' roofline.  No counterpart in the reference. */
+int32_t o3g_fp32_peak_probe(int32_t iters, void* stream, double* tflops, float* ms);
+
+/* ---- points_affect_points -------------------------------------------------------
+ * Replaces points_affect_points<float,A>(src, targ, restype, env), Influence.h:67-551,
+ * and generalises the external solver hook external_vel_solver_f_, Influence.h:33-40.
+ *   sources: ns vortex particles (sx,sy,sz position; sr core radius; ssx,ssy,ssz strength)
+ *   targets: nt points; tr == NULL means field points (inert targets, Influence.h:205),
+ *            otherwise thick-cored particles with radius tr
+ *   results: tu,tv,tw += velocity sums; tug == NULL means velocity only
+ *            (ResultsType velonly), else tug[0..8] += the nine gradient sums.
+ * Sums carry no 1/4pi factor (finalize_vels applies it, ElementBase.h:187-193). */
+int32_t o3g_points_affect_points(int32_t core, int32_t prec, int32_t mem,
+                                 int32_t ns, const float* sx, const float* sy, const float* sz,
+                                 const float* sr, const float* ssx, const float* ssy, const float* ssz,
+                                 int32_t nt, const float* tx, const float* ty, const float* tz,
+                                 const float* tr,
+                                 float* tu, float* tv, float* tw, float* const* tug,
+                                 void* stream);
+
+/* Double-precision twin (S = A = double), mirrors external_vel_solver_d_, Influence.h:41-47.
+ * Always computes in FP64. */
+int32_t o3g_points_affect_points_d(int32_t core, int32_t mem,
+                                   int32_t ns, const double* sx, const double* sy, const double* sz,
+                                   const double* sr, const double* ssx, const double* ssy, const double* ssz,
+                                   int32_t nt, const double* tx, const double* ty, const double* tz,
+                                   const double* tr,
+                                   double* tu, double* tv, double* tw, double* const* tug,
+                                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* O3DGPU_H */

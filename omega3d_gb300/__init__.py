@@ -1,0 +1,9 @@
+"""omega3d_gb300: GB300 (sm_103a) Biot-Savart velocity/gradient and BEM hot path of
+Omega3D behind a C-ABI (include/o3dgpu.h, libo3dgpu.so) with a reference-shaped
+Python mirror of its call surface."""
+from ._lib import CORES, PRECS, O3GError, lib, header_symbols  # noqa: F401
+from .influence import (ExecEnv, InfluenceVisitor, Points, ResultsType,  # noqa: F401
+                        points_affect_points)
+
+__all__ = ["CORES", "PRECS", "O3GError", "lib", "header_symbols", "ExecEnv", "InfluenceVisitor", "Points",
+           "ResultsType", "points_affect_points"]

@@ -1,0 +1,98 @@
+"""ctypes binding of libo3dgpu.so (the C-ABI declared in include/o3dgpu.h).
+
+The library is built in-tree by omega3d_gb300/build.py.  Loading fails loudly when
+it is missing: there is no CPU fallback behind this package.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libo3dgpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "o3dgpu.h")
+
+O3G_OK = 0
+STATUS = {
+    0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "no usable sm_103 device",
+    4: "device allocation failed", 5: "iterative refinement did not converge", 6: "device-side wait timed out",
+    7: "singular or non-finite pivot", 8: "non-finite input", 9: "call made in the wrong state",
+}
+CORES = {"rm": 0, "wl": 1, "exp": 2, "gauss": 3, "v2": 4}
+PRECS = {"plain": 0, "compensated": 1, "fp64": 2}
+MEM_HOST, MEM_DEVICE = 0, 1
+
+_lib = None
+
+c_i32 = ctypes.c_int32
+c_vp = ctypes.c_void_p
+c_f = ctypes.c_float
+c_d = ctypes.c_double
+
+
+class O3GError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = "%s failed: %s" % (where, STATUS.get(status, "status %d" % status))
+        try:
+            detail = lib().o3g_last_error().decode()
+            if detail:
+                msg += " (%s)" % detail
+        except Exception:  # pragma: no cover - loading problems are reported elsewhere
+            pass
+        super().__init__(msg)
+
+
+def _declare(l):
+    P = c_vp
+    l.o3g_status_string.restype = ctypes.c_char_p
+    l.o3g_status_string.argtypes = [c_i32]
+    l.o3g_last_error.restype = ctypes.c_char_p
+    l.o3g_last_error.argtypes = []
+    l.o3g_version.restype = c_i32
+    l.o3g_device_info.restype = c_i32
+    l.o3g_device_info.argtypes = [P, P, P, P]
+    l.o3g_flops_per_pair.restype = c_i32
+    l.o3g_flops_per_pair.argtypes = [c_i32, c_i32, c_i32]
+    l.o3g_set_timing.restype = c_i32
+    l.o3g_set_timing.argtypes = [c_i32]
+    l.o3g_last_kernel_ms.restype = c_i32
+    l.o3g_last_kernel_ms.argtypes = [P]
+    l.o3g_launch_count.restype = c_i32
+    l.o3g_launch_count.argtypes = [P]
+    l.o3g_fp32_peak_probe.restype = c_i32
+    l.o3g_fp32_peak_probe.argtypes = [c_i32, P, P, P]
+    l.o3g_points_affect_points.restype = c_i32
+    l.o3g_points_affect_points.argtypes = [c_i32, c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
+    l.o3g_points_affect_points_d.restype = c_i32
+    l.o3g_points_affect_points_d.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libo3dgpu.so not built at %s; run omega3d_gb300/build.py "
+                              "(or __graft_entry__.build())" % LIB_PATH)
+        l = ctypes.CDLL(LIB_PATH)
+        _declare(l)
+        _lib = l
+    return _lib
+
+
+def check(status, where):
+    if status != O3G_OK:
+        raise O3GError(status, where)
+
+
+def launch_count():
+    n = ctypes.c_uint64(0)
+    check(lib().o3g_launch_count(ctypes.byref(n)), "o3g_launch_count")
+    return int(n.value)
+
+
+def header_symbols():
+    """Names of every entry point declared in include/o3dgpu.h."""
+    import re
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(o3g_[a-z0-9_]+)\s*\(", txt)))

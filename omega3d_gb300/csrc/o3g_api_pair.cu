@@ -1,0 +1,152 @@
+// o3g_api_pair.cu -- extern "C" points_affect_points entry points (float and double).
+#include "o3g_pair_impl.cuh"
+
+namespace o3g {
+
+template <class I>
+static int32_t dispatch_core(int core, const PtPtCall& c, const I* sx, const I* sy, const I* sz, const I* sr,
+                             const I* ssx, const I* ssy, const I* ssz, const I* tx, const I* ty, const I* tz,
+                             const I* tr, OutPtrs<I> out, size_t* need, char* ws);
+
+template <>
+int32_t dispatch_core<float>(int core, const PtPtCall& c, const float* sx, const float* sy, const float* sz,
+                             const float* sr, const float* ssx, const float* ssy, const float* ssz,
+                             const float* tx, const float* ty, const float* tz, const float* tr,
+                             OutPtrs<float> out, size_t* need, char* ws) {
+  switch (core) {
+    case CORE_RM: return ptpt_core_f<CORE_RM>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_WL: return ptpt_core_f<CORE_WL>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_EXP: return ptpt_core_f<CORE_EXP>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_GAUSS: return ptpt_core_f<CORE_GAUSS>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_V2: return ptpt_core_f<CORE_V2>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    default: return O3G_ERR_INVALID_ARG;
+  }
+}
+template <>
+int32_t dispatch_core<double>(int core, const PtPtCall& c, const double* sx, const double* sy, const double* sz,
+                              const double* sr, const double* ssx, const double* ssy, const double* ssz,
+                              const double* tx, const double* ty, const double* tz, const double* tr,
+                              OutPtrs<double> out, size_t* need, char* ws) {
+  switch (core) {
+    case CORE_RM: return ptpt_core_d<CORE_RM>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_WL: return ptpt_core_d<CORE_WL>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_EXP: return ptpt_core_d<CORE_EXP>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_GAUSS: return ptpt_core_d<CORE_GAUSS>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    case CORE_V2: return ptpt_core_d<CORE_V2>(c, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, need, ws);
+    default: return O3G_ERR_INVALID_ARG;
+  }
+}
+
+template <class I>
+static int32_t ptpt_entry(int core, int mode, int mem, int ns, const I* sx, const I* sy, const I* sz, const I* sr,
+                          const I* ssx, const I* ssy, const I* ssz, int nt, const I* tx, const I* ty, const I* tz,
+                          const I* tr, I* tu, I* tv, I* tw, I* const* tug, void* stream) {
+  if (core < 0 || core > 4 || mode < 0 || mode > 2 || (mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || ns < 0 ||
+      nt < 0) {
+    set_error("points_affect_points: bad core/prec/mem or negative count");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (ns > 0 && (!sx || !sy || !sz || !sr || !ssx || !ssy || !ssz)) {
+    set_error("points_affect_points: null source array");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (nt > 0 && (!tx || !ty || !tz || !tu || !tv || !tw)) {
+    set_error("points_affect_points: null target array");
+    return O3G_ERR_INVALID_ARG;
+  }
+  const bool grads = (tug != nullptr);
+  if (grads && nt > 0)
+    for (int k = 0; k < 9; ++k)
+      if (!tug[k]) {
+        set_error("points_affect_points: null gradient component");
+        return O3G_ERR_INVALID_ARG;
+      }
+  if (ns == 0 || nt == 0) return O3G_OK;
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+
+  cudaStream_t st = (cudaStream_t)stream;
+  const int NC = grads ? 12 : 3;
+  const bool same = (ns == nt && sx == tx && sy == ty && sz == tz && sr == tr);
+  PtPtCall call;
+  call.mode = mode;
+  call.grads = grads;
+  call.ns = ns;
+  call.nt = nt;
+  call.same = same;
+  call.st = st;
+
+  OutPtrs<I> out;
+  out.p[0] = tu; out.p[1] = tv; out.p[2] = tw;
+  for (int k = 0; k < 9; ++k) out.p[3 + k] = grads ? tug[k] : nullptr;
+
+  size_t need = 0;
+  O3G_TRY(dispatch_core<I>(core, call, sx, sy, sz, sr, ssx, ssy, ssz, tx, ty, tz, tr, out, &need, nullptr));
+
+  size_t staging = 0;
+  if (mem == O3G_MEM_HOST) {
+    staging += 7 * align_up((size_t)ns * sizeof(I));
+    if (!same) staging += (tr ? 4 : 3) * align_up((size_t)nt * sizeof(I));
+    staging += NC * align_up((size_t)nt * sizeof(I));
+  }
+  Workspace* ws = nullptr;
+  O3G_TRY(workspace_get(st, staging + need, &ws));
+
+  const I *dsx = sx, *dsy = sy, *dsz = sz, *dsr = sr, *dssx = ssx, *dssy = ssy, *dssz = ssz;
+  const I *dtx = tx, *dty = ty, *dtz = tz, *dtr = tr;
+  OutPtrs<I> dout = out;
+  if (mem == O3G_MEM_HOST) {
+    Carve cv(ws->base);
+    const I* hs[7] = {sx, sy, sz, sr, ssx, ssy, ssz};
+    const I** ds[7] = {&dsx, &dsy, &dsz, &dsr, &dssx, &dssy, &dssz};
+    for (int k = 0; k < 7; ++k) {
+      I* d = cv.take<I>(ns);
+      O3G_CUDA_TRY(cudaMemcpyAsync(d, hs[k], (size_t)ns * sizeof(I), cudaMemcpyHostToDevice, st));
+      *ds[k] = d;
+    }
+    if (same) {
+      dtx = dsx; dty = dsy; dtz = dsz; dtr = dsr;
+    } else {
+      const I* ht[4] = {tx, ty, tz, tr};
+      const I** dt[4] = {&dtx, &dty, &dtz, &dtr};
+      for (int k = 0; k < (tr ? 4 : 3); ++k) {
+        I* d = cv.take<I>(nt);
+        O3G_CUDA_TRY(cudaMemcpyAsync(d, ht[k], (size_t)nt * sizeof(I), cudaMemcpyHostToDevice, st));
+        *dt[k] = d;
+      }
+    }
+    for (int c = 0; c < NC; ++c) {
+      I* d = cv.take<I>(nt);
+      O3G_CUDA_TRY(cudaMemcpyAsync(d, out.p[c], (size_t)nt * sizeof(I), cudaMemcpyHostToDevice, st));
+      dout.p[c] = d;
+    }
+  }
+  O3G_TRY(dispatch_core<I>(core, call, dsx, dsy, dsz, dsr, dssx, dssy, dssz, dtx, dty, dtz, dtr, dout, nullptr,
+                           ws->base + staging));
+  if (mem == O3G_MEM_HOST) {
+    for (int c = 0; c < NC; ++c)
+      O3G_CUDA_TRY(cudaMemcpyAsync(out.p[c], dout.p[c], (size_t)nt * sizeof(I), cudaMemcpyDeviceToHost, st));
+    O3G_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return O3G_OK;
+}
+
+}  // namespace o3g
+
+extern "C" int32_t o3g_points_affect_points(int32_t core, int32_t prec, int32_t mem, int32_t ns, const float* sx,
+                                            const float* sy, const float* sz, const float* sr, const float* ssx,
+                                            const float* ssy, const float* ssz, int32_t nt, const float* tx,
+                                            const float* ty, const float* tz, const float* tr, float* tu, float* tv,
+                                            float* tw, float* const* tug, void* stream) {
+  return o3g::ptpt_entry<float>(core, prec, mem, ns, sx, sy, sz, sr, ssx, ssy, ssz, nt, tx, ty, tz, tr, tu, tv, tw,
+                                tug, stream);
+}
+
+extern "C" int32_t o3g_points_affect_points_d(int32_t core, int32_t mem, int32_t ns, const double* sx,
+                                              const double* sy, const double* sz, const double* sr, const double* ssx,
+                                              const double* ssy, const double* ssz, int32_t nt, const double* tx,
+                                              const double* ty, const double* tz, const double* tr, double* tu,
+                                              double* tv, double* tw, double* const* tug, void* stream) {
+  return o3g::ptpt_entry<double>(core, o3g::MODE_FP64, mem, ns, sx, sy, sz, sr, ssx, ssy, ssz, nt, tx, ty, tz, tr,
+                                 tu, tv, tw, tug, stream);
+}

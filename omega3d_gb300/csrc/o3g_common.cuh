@@ -1,0 +1,279 @@
+// o3g_common.cuh -- shared host/device helpers of the sm_103a Biot-Savart / BEM library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "../../include/o3dgpu.h"
+
+namespace o3g {
+
+// ------------------------------------------------------------------------------
+// error plumbing (host)
+void set_error(const char* what);
+void set_error_cuda(const char* where, cudaError_t e);
+
+#define O3G_CUDA_TRY(call)                                 \
+  do {                                                     \
+    cudaError_t e__ = (call);                              \
+    if (e__ != cudaSuccess) {                              \
+      ::o3g::set_error_cuda(#call, e__);                   \
+      return O3G_ERR_CUDA;                                 \
+    }                                                      \
+  } while (0)
+
+#define O3G_TRY(expr)                                      \
+  do {                                                     \
+    int32_t s__ = (expr);                                  \
+    if (s__ != O3G_OK) return s__;                         \
+  } while (0)
+
+// ------------------------------------------------------------------------------
+// per-(device, stream) grow-only device workspace.  Every call on a stream reuses the
+// same buffer; calls on one stream are ordered by the stream, so they never overlap.
+struct Workspace {
+  char* base = nullptr;
+  size_t cap = 0;
+  size_t used = 0;
+};
+// Returns a workspace with at least `bytes` capacity for (current device, stream).
+int32_t workspace_get(cudaStream_t stream, size_t bytes, Workspace** ws);
+// Sub-allocation helper: 256-byte aligned carve-outs from a reserved workspace.
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+struct Carve {
+  char* base;
+  size_t off = 0;
+  explicit Carve(char* b) : base(b) {}
+  template <class T> T* take(size_t count) {
+    T* p = reinterpret_cast<T*>(base + off);
+    off += align_up(count * sizeof(T));
+    return p;
+  }
+};
+
+// device facts (cached per device)
+struct DeviceFacts {
+  int device = -1;
+  int num_sms = 0;
+  int clock_khz = 0;
+  int cc_major = 0, cc_minor = 0;
+};
+int32_t device_facts(DeviceFacts* f);
+
+// resident blocks per SM of `kernel` at `block` threads (cached)
+int32_t occupancy_blocks(const void* kernel, int block, int* nb);
+
+// optional timing of the main kernel of a call
+struct KernelTimer {
+  cudaEvent_t start = nullptr, stop = nullptr;
+  bool active = false;
+  void begin(cudaStream_t s);
+  void end(cudaStream_t s);
+};
+KernelTimer& thread_timer();
+
+// count of kernels this thread has launched through the library
+void note_launch(int n = 1);
+
+// ------------------------------------------------------------------------------
+// vector types
+template <class T> struct V4;
+template <> struct alignas(16) V4<float> { float x, y, z, w; };
+template <> struct alignas(32) V4<double> { double x, y, z, w; };
+
+// output pointer set: 3 velocity + 9 gradient component arrays
+template <class T> struct OutPtrs { T* p[12]; };
+
+// ------------------------------------------------------------------------------
+// Core functions.  All cores share the form used by Kernels.h: velocity
+//   u += r3 * (d x s),  grad += bbb * d (x) (d x s) + antisymmetric(r3 * s)
+// where d = target - source.  `cst` is the combined core parameter of the pair:
+//   RM, WL, GAUSS: sr^2 + tr^2;   EXP: sr^3 + tr^3;   V2: sr^4 + tr^4
+// (CoreFunc.h:66-71, :266-274, :226-236, :318-330).
+enum { CORE_RM = 0, CORE_WL = 1, CORE_EXP = 2, CORE_GAUSS = 3, CORE_V2 = 4 };
+
+template <int C, class T>
+__host__ __device__ __forceinline__ T core_param(T r) {
+  if (C == CORE_EXP) return r * r * r;
+  if (C == CORE_V2) { const T s2 = r * r; return s2 * s2; }
+  return r * r;
+}
+
+// Gaussian core series coefficients c_n of G(q) = sqrt(2/pi) sum_{n>=1} c_n q^(n-1),
+// c_n = (-1)^(n+1) / ((2n+1) 2^(n-1) (n-1)!): the Taylor expansion of
+// [erf(rho/sqrt2) - sqrt(2/pi) rho exp(-rho^2/2)] / rho^3 in q = rho^2.
+__host__ __device__ constexpr double gauss_coef(int n) {
+  double c = 1.0 / (2.0 * n + 1.0);
+  for (int k = 1; k < n; ++k) c /= (2.0 * k);
+  return (n % 2 == 1) ? c : -c;
+}
+template <class T> struct GaussP;
+template <> struct GaussP<float>  { static constexpr float  qfar = 48.0f; static constexpr int nterms = 9; };
+template <> struct GaussP<double> { static constexpr double qfar = 90.0;  static constexpr int nterms = 17; };
+
+// reciprocal square root: plain = hardware approximation (MUFU.RSQ, <= 2 ulp);
+// accurate = one Newton-Raphson step on top (y' = y + y/2 (1 - x y^2)), ~1 ulp.
+template <bool ACC>
+__device__ __forceinline__ float rsq(float x) {
+  float y = rsqrtf(x);
+  if (ACC) {
+    const float h = x * y;
+    const float e = fmaf(-h, y, 1.0f);
+    y = fmaf(0.5f * y, e, y);
+  }
+  return y;
+}
+template <bool ACC>
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+
+__device__ __forceinline__ float dev_erf(float x) { return erff(x); }
+__device__ __forceinline__ double dev_erf(double x) { return erf(x); }
+__device__ __forceinline__ float dev_exp(float x) { return expf(x); }
+__device__ __forceinline__ double dev_exp(double x) { return exp(x); }
+__device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
+
+// Gaussian core with gradient factor (the project's own definition, see o3dgpu.h)
+template <bool ACC, class T>
+__device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb) {
+  const T c = T(0.79788456080286535588);  // sqrt(2/pi)
+  if (distsq > GaussP<T>::qfar * sig2) {   // q > qfar without the division
+    const T rs = rsq<ACC>(distsq);
+    const T rs2 = rs * rs;
+    r3 = rs2 * rs;
+    bbb = T(-3.0) * r3 * rs2;
+    return;
+  }
+  const T q = distsq / sig2;
+  if (q < T(1.0)) {
+    T g = T(0), gp = T(0);
+#pragma unroll
+    for (int n = GaussP<T>::nterms; n >= 1; --n) g = g * q + T(gauss_coef(n));
+#pragma unroll
+    for (int n = GaussP<T>::nterms; n >= 2; --n) gp = gp * q + T((n - 1) * gauss_coef(n));
+    const T rsg = rsq<ACC>(sig2);
+    const T isig3 = rsg * rsg * rsg;
+    r3 = c * g * isig3;
+    bbb = T(2.0) * c * gp * isig3 * (rsg * rsg);
+  } else {
+    const T rs = rsq<ACC>(distsq);
+    const T rs2 = rs * rs;
+    const T rho = dev_sqrt(q);
+    const T e = dev_exp(T(-0.5) * q);
+    const T g = dev_erf(rho * T(0.70710678118654752440)) - c * rho * e;
+    const T rsg = rsq<ACC>(sig2);
+    r3 = g * rs2 * rs;
+    bbb = (c * e * (rsg * rsg * rsg) - T(3.0) * r3) * rs2;
+  }
+}
+template <bool ACC, class T>
+__device__ __forceinline__ T gauss_v(T distsq, T sig2) {
+  const T c = T(0.79788456080286535588);
+  if (distsq > GaussP<T>::qfar * sig2) {
+    const T rs = rsq<ACC>(distsq);
+    return rs * rs * rs;
+  }
+  const T q = distsq / sig2;
+  if (q < T(1.0)) {
+    T g = T(0);
+#pragma unroll
+    for (int n = GaussP<T>::nterms; n >= 1; --n) g = g * q + T(gauss_coef(n));
+    const T rsg = rsq<ACC>(sig2);
+    return c * g * rsg * rsg * rsg;
+  } else {
+    const T rs = rsq<ACC>(distsq);
+    const T rho = dev_sqrt(q);
+    const T e = dev_exp(T(-0.5) * q);
+    const T g = dev_erf(rho * T(0.70710678118654752440)) - c * rho * e;
+    return g * rs * rs * rs;
+  }
+}
+
+// r3 and bbb of one pair; dx,dy,dz = target - source; cst as above.
+template <int C, bool ACC, class T>
+__device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
+  if (C == CORE_RM) {
+    // CoreFunc.h:66-71: r2 = d^2 + sr^2 + tr^2, r3 = r2^-1.5, bbb = -3 r3 / r2
+    const T r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, cst)));
+    const T rs = rsq<ACC>(r2);
+    const T rs2 = rs * rs;
+    r3 = rs2 * rs;
+    bbb = T(-3.0) * r3 * rs2;
+  } else if (C == CORE_WL) {
+    // CoreFunc.h:266-274: d2 = d^2 + r^2; r3 = (d^2 + 2.5 r^2) d2^-2.5; bbb = 2 d2^-2.5 - 5 r3 / d2
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T d2 = distsq + cst;
+    const T d2top = fma(T(2.5), cst, distsq);
+    const T rs = rsq<ACC>(d2);
+    const T rs2 = rs * rs;
+    const T dn5 = rs2 * rs2 * rs;
+    r3 = d2top * dn5;
+    bbb = fma(T(-5.0) * r3, rs2, T(2.0) * dn5);
+  } else if (C == CORE_EXP) {
+    // CoreFunc.h:226-236 with the branches of exp_cond / exp_bbb (:119-174)
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T dist = dev_sqrt(distsq);
+    const T corefac = T(1.0) / cst;
+    const T d3 = distsq * dist;
+    const T reld3 = d3 * corefac;
+    const T ood3 = T(1.0) / d3;
+    if (reld3 > T(16.0)) {
+      r3 = ood3;
+      bbb = T(-3.0) * r3 / distsq;
+    } else if (reld3 < T(0.001)) {
+      r3 = corefac;
+      bbb = T(-1.5) * dist * r3 * r3;
+    } else {
+      const T e = dev_exp(-reld3);
+      r3 = ood3 * (T(1.0) - e);
+      bbb = T(3.0) * (corefac * e - r3) / distsq;
+    }
+  } else if (C == CORE_V2) {
+    // CoreFunc.h:318-330: denom = d^4 + sr^4 + tr^4; r3 = denom^-0.75; bbb = -3 r3 denom^-0.5
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T denom = fma(distsq, distsq, cst);
+    const T rs = rsq<ACC>(denom);
+    r3 = rs * dev_sqrt(rs);
+    bbb = T(-3.0) * r3 * rs;
+  } else {
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    gauss_g<ACC, T>(distsq, cst, r3, bbb);
+  }
+}
+
+// r3 only (velocity-only kernels): CoreFunc.h:48-52, :246-252, :202-209, :297-304
+template <int C, bool ACC, class T>
+__device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst) {
+  if (C == CORE_RM) {
+    const T r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, cst)));
+    const T rs = rsq<ACC>(r2);
+    return rs * rs * rs;
+  } else if (C == CORE_WL) {
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T d2 = distsq + cst;
+    const T rs = rsq<ACC>(d2);
+    const T rs2 = rs * rs;
+    return fma(T(2.5), cst, distsq) * (rs2 * rs2 * rs);
+  } else if (C == CORE_EXP) {
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T dist = dev_sqrt(distsq);
+    const T ood3 = T(1.0) / (distsq * dist);
+    const T corefac = T(1.0) / cst;
+    const T reld3 = corefac / ood3;
+    if (reld3 > T(16.0)) return ood3;
+    if (reld3 < T(0.001)) return corefac;
+    return ood3 * (T(1.0) - dev_exp(-reld3));
+  } else if (C == CORE_V2) {
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T rs = rsq<ACC>(fma(distsq, distsq, cst));
+    return rs * dev_sqrt(rs);
+  } else {
+    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    return gauss_v<ACC, T>(distsq, cst);
+  }
+}
+
+}  // namespace o3g

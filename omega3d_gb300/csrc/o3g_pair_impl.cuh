@@ -1,0 +1,404 @@
+// o3g_pair_impl.cuh -- particle/field-point Biot-Savart pair sums (points_affect_points).
+//
+// Data layout in HBM (inside the per-stream workspace):
+//   spos[ns_pad] : float4 (x, y, z, core parameter of sr)      16 B / source
+//   sstr[ns_pad] : float4 (sx, sy, sz, sr)                     16 B / source
+//   tpos[nt_pad] : float4 (x, y, z, core parameter of tr or 0) 16 B / target
+// Padding sources sit at the origin with zero strength and core parameter 1, so they
+// add exactly zero (the same trick as the reference's Vc padding, Influence.h:232-238).
+//
+// Kernel k_pair: a block of kBlock threads owns kBlock*TPT targets (TPT per thread,
+// strided by kBlock so loads/stores coalesce) and sweeps a contiguous range of
+// source tiles.  Each tile of kBlock sources is staged in shared memory and read by
+// every thread as a broadcast.  When the targets alone cannot fill the GPU, the
+// source range is split across blockIdx.y and the per-split partial sums go to
+// scratch, reduced afterwards in a fixed order (deterministic, k_reduce).
+#pragma once
+
+#include "o3g_common.cuh"
+
+namespace o3g {
+
+constexpr int kBlock = 128;  // threads per block == sources per shared tile
+
+enum { MODE_PLAIN = 0, MODE_COMP = 1, MODE_FP64 = 2 };
+
+template <class T, class O> struct PairArgs {
+  const V4<T>* spos;
+  const V4<T>* sstr;
+  int ntiles;           // source tiles of kBlock sources
+  int tiles_per_split;  // tiles swept by one block
+  const V4<T>* tpos;
+  int nt;               // real targets
+  int nt_pad;           // padded targets (multiple of kBlock*TPT)
+  T* partial;           // [nsplit][ncomp * (COMP ? 2 : 1)][nt_pad] or nullptr
+  OutPtrs<O> out;       // accumulated into when partial == nullptr
+};
+
+// one pair, velocity + gradient.  a[0..2] velocity, a[3..11] gradient sums of
+// bbb * d (x) (d x s) in the reference order, a[12..14] = sum r3 * s (folded into the
+// antisymmetric gradient terms by fold_grads, Kernels.h:184-192).
+template <int C, bool ACC, bool HAVE_TR, class T>
+__device__ __forceinline__ void pair_g(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a) {
+  const T dx = t.x - s.x;
+  const T dy = t.y - s.y;
+  const T dz = t.z - s.z;
+  const T cst = HAVE_TR ? (s.w + t.w) : s.w;
+  T r3, bbb;
+  core_g<C, ACC, T>(dx, dy, dz, cst, r3, bbb);
+  T cx = dz * w.y - dy * w.z;
+  T cy = dx * w.z - dz * w.x;
+  T cz = dy * w.x - dx * w.y;
+  a[0] = fma(r3, cx, a[0]);
+  a[1] = fma(r3, cy, a[1]);
+  a[2] = fma(r3, cz, a[2]);
+  cx *= bbb;
+  cy *= bbb;
+  cz *= bbb;
+  a[3] = fma(dx, cx, a[3]);
+  a[4] = fma(dx, cy, a[4]);
+  a[5] = fma(dx, cz, a[5]);
+  a[6] = fma(dy, cx, a[6]);
+  a[7] = fma(dy, cy, a[7]);
+  a[8] = fma(dy, cz, a[8]);
+  a[9] = fma(dz, cx, a[9]);
+  a[10] = fma(dz, cy, a[10]);
+  a[11] = fma(dz, cz, a[11]);
+  a[12] = fma(r3, w.x, a[12]);
+  a[13] = fma(r3, w.y, a[13]);
+  a[14] = fma(r3, w.z, a[14]);
+}
+
+// velocity only
+template <int C, bool ACC, bool HAVE_TR, class T>
+__device__ __forceinline__ void pair_v(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a) {
+  const T dx = t.x - s.x;
+  const T dy = t.y - s.y;
+  const T dz = t.z - s.z;
+  const T cst = HAVE_TR ? (s.w + t.w) : s.w;
+  const T r3 = core_v<C, ACC, T>(dx, dy, dz, cst);
+  a[0] = fma(r3, dz * w.y - dy * w.z, a[0]);
+  a[1] = fma(r3, dx * w.z - dz * w.x, a[1]);
+  a[2] = fma(r3, dy * w.x - dx * w.y, a[2]);
+}
+
+// a[12..14] -> antisymmetric gradient terms: tvx += sz r3, twx -= sy r3, tuy -= sz r3,
+// twy += sx r3, tuz += sy r3, tvz -= sx r3 (Kernels.h:185-191)
+template <class T>
+__device__ __forceinline__ void fold_grads(T* a) {
+  a[4] += a[14];
+  a[5] -= a[13];
+  a[6] -= a[14];
+  a[8] += a[12];
+  a[9] += a[13];
+  a[10] -= a[12];
+}
+
+// error-free transformation of a + b (Knuth two-sum): s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
+__global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
+  constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr int NA = GRADS ? 15 : 3;   // accumulators during the sweep
+  constexpr int NC = GRADS ? 12 : 3;   // output components
+  __shared__ V4<T> sp[kBlock];
+  __shared__ V4<T> sw[kBlock];
+
+  const int tid = threadIdx.x;
+  const int split = blockIdx.y;
+  const int tbase = blockIdx.x * (kBlock * TPT) + tid;
+
+  V4<T> tp[TPT];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) tp[k] = a.tpos[tbase + k * kBlock];
+
+  T acc[TPT][NA];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k)
+#pragma unroll
+    for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
+
+  // compensated mode: (hi, lo) running sums of the folded per-tile partials
+  float hi[ACC ? TPT : 1][ACC ? NC : 1];
+  float lo[ACC ? TPT : 1][ACC ? NC : 1];
+  if (ACC) {
+#pragma unroll
+    for (int k = 0; k < TPT; ++k)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) { hi[k][c] = 0.f; lo[k][c] = 0.f; }
+  }
+
+  const int t_begin = split * a.tiles_per_split;
+  const int t_end = min(a.ntiles, t_begin + a.tiles_per_split);
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    __syncthreads();
+    sp[tid] = a.spos[(size_t)tile * kBlock + tid];
+    sw[tid] = a.sstr[(size_t)tile * kBlock + tid];
+    __syncthreads();
+#pragma unroll 4
+    for (int j = 0; j < kBlock; ++j) {
+      const V4<T> s = sp[j];
+      const V4<T> w = sw[j];
+#pragma unroll
+      for (int k = 0; k < TPT; ++k) {
+        if (GRADS) pair_g<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k]);
+        else       pair_v<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k]);
+      }
+    }
+    if (ACC) {
+#pragma unroll
+      for (int k = 0; k < TPT; ++k) {
+        if (GRADS) fold_grads(acc[k]);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          float s, e;
+          two_sum((float)hi[k][c], (float)acc[k][c], s, e);
+          hi[k][c] = s;
+          lo[k][c] += e;
+        }
+#pragma unroll
+        for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
+      }
+    }
+  }
+
+  // epilogue
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    const int idx = tbase + k * kBlock;
+    if (!ACC && GRADS) fold_grads(acc[k]);
+    if (a.partial) {
+      if (ACC) {
+        T* base = a.partial + (size_t)split * (2 * NC) * a.nt_pad;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          base[(size_t)c * a.nt_pad + idx] = hi[k][c];
+          base[(size_t)(NC + c) * a.nt_pad + idx] = lo[k][c];
+        }
+      } else {
+        T* base = a.partial + (size_t)split * NC * a.nt_pad;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) base[(size_t)c * a.nt_pad + idx] = acc[k][c];
+      }
+    } else if (idx < a.nt) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        O* p = a.out.p[c] + idx;
+        if (ACC) *p = (O)((double)*p + ((double)hi[k][c] + (double)lo[k][c]));
+        else     *p = (O)((T)*p + acc[k][c]);
+      }
+    }
+  }
+}
+
+// Sum the per-split partials in split order and add into the outputs.
+template <int NC, bool ACC, class T, class O>
+__global__ void k_reduce(const T* __restrict__ partial, int nsplit, int nt, int nt_pad, OutPtrs<O> out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (idx >= nt) return;
+  O* p = out.p[c] + idx;
+  if (ACC) {
+    double s = 0.0;
+    for (int k = 0; k < nsplit; ++k) {
+      const T* base = partial + (size_t)k * (2 * NC) * nt_pad;
+      s += (double)base[(size_t)c * nt_pad + idx];
+      s += (double)base[(size_t)(NC + c) * nt_pad + idx];
+    }
+    *p = (O)((double)*p + s);
+  } else {
+    T s = T(0);
+    for (int k = 0; k < nsplit; ++k) s += partial[((size_t)k * NC + c) * nt_pad + idx];
+    *p = (O)((T)*p + s);
+  }
+}
+
+// SoA -> packed float4/double4 sources
+template <int C, class I, class T>
+__global__ void k_pack_src(int n, int n_pad, const I* __restrict__ x, const I* __restrict__ y,
+                           const I* __restrict__ z, const I* __restrict__ r, const I* __restrict__ sx,
+                           const I* __restrict__ sy, const I* __restrict__ sz, V4<T>* spos, V4<T>* sstr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  V4<T> p, w;
+  if (i < n) {
+    const T ri = (T)r[i];
+    p.x = (T)x[i]; p.y = (T)y[i]; p.z = (T)z[i]; p.w = core_param<C, T>(ri);
+    w.x = (T)sx[i]; w.y = (T)sy[i]; w.z = (T)sz[i]; w.w = ri;
+  } else {
+    p.x = T(0); p.y = T(0); p.z = T(0); p.w = T(1);
+    w.x = T(0); w.y = T(0); w.z = T(0); w.w = T(0);
+  }
+  spos[i] = p;
+  sstr[i] = w;
+}
+
+// SoA -> packed targets; r == nullptr means field points (core parameter 0)
+template <int C, class I, class T>
+__global__ void k_pack_tgt(int n, int n_pad, const I* __restrict__ x, const I* __restrict__ y,
+                           const I* __restrict__ z, const I* __restrict__ r, V4<T>* tpos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  V4<T> p;
+  if (i < n) {
+    p.x = (T)x[i]; p.y = (T)y[i]; p.z = (T)z[i];
+    p.w = r ? core_param<C, T>((T)r[i]) : T(0);
+  } else {
+    p.x = T(0); p.y = T(0); p.z = T(0); p.w = T(0);
+  }
+  tpos[i] = p;
+}
+
+// ------------------------------------------------------------------------------
+// host side
+struct PairPlan {
+  int tpt = 1;
+  int ns_pad = 0, nt_pad = 0, ntiles = 0;
+  int nsplit = 1, tiles_per_split = 0;
+  int tblocks = 0;
+};
+
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
+struct PairKernel {
+  static const void* ptr() { return (const void*)&k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O>; }
+};
+
+// Chooses the source split so that the grid covers >= ~6 waves of resident blocks.
+inline void plan_pair(int ns, int nt, int tpt, int slots, PairPlan* p) {
+  p->tpt = tpt;
+  p->ntiles = (ns + kBlock - 1) / kBlock;
+  p->ns_pad = p->ntiles * kBlock;
+  const int tchunk = kBlock * tpt;
+  p->tblocks = (nt + tchunk - 1) / tchunk;
+  p->nt_pad = p->tblocks * tchunk;
+  const long want = 6L * (slots > 0 ? slots : 1);
+  long nsplit = (want + p->tblocks - 1) / p->tblocks;
+  const long max_split = p->ntiles >= 2 ? p->ntiles / 2 : 1;
+  if (nsplit > max_split) nsplit = max_split;
+  if (nsplit < 1) nsplit = 1;
+  p->tiles_per_split = (int)((p->ntiles + nsplit - 1) / nsplit);
+  p->nsplit = (p->ntiles + p->tiles_per_split - 1) / p->tiles_per_split;
+  if (p->nsplit < 1) p->nsplit = 1;
+}
+
+// The pipeline for one (core, mode, grads, target kind): pack, sweep, reduce.
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class I, class O>
+int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I* sr,
+                          const I* ssx, const I* ssy, const I* ssz,
+                          int nt, const I* tx, const I* ty, const I* tz, const I* tr,
+                          OutPtrs<O> out, bool same, cudaStream_t st, Workspace* ws_unused,
+                          size_t* ws_bytes_needed, char* ws_base) {
+  (void)ws_unused;
+  constexpr int NC = GRADS ? 12 : 3;
+  constexpr bool ACC = (MODE == MODE_COMP);
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+  int nb = 0;
+  O3G_TRY(occupancy_blocks(PairKernel<C, MODE, GRADS, HAVE_TR, TPT, T, O>::ptr(), kBlock, &nb));
+  PairPlan pl;
+  plan_pair(ns, nt, TPT, nb * df.num_sms, &pl);
+  const int nsp = same ? (pl.ns_pad > pl.nt_pad ? pl.ns_pad : pl.nt_pad) : pl.ns_pad;
+  size_t bytes = 2 * align_up((size_t)nsp * sizeof(V4<T>));
+  if (!same) bytes += align_up((size_t)pl.nt_pad * sizeof(V4<T>));
+  if (pl.nsplit > 1) bytes += align_up((size_t)pl.nsplit * NC * (ACC ? 2 : 1) * pl.nt_pad * sizeof(T));
+  if (ws_bytes_needed) { *ws_bytes_needed = bytes; return O3G_OK; }
+
+  Carve cv(ws_base);
+  V4<T>* spos = cv.take<V4<T>>(nsp);
+  V4<T>* sstr = cv.take<V4<T>>(nsp);
+  V4<T>* tpos = same ? spos : cv.take<V4<T>>(pl.nt_pad);
+  T* partial = pl.nsplit > 1 ? cv.take<T>((size_t)pl.nsplit * NC * (ACC ? 2 : 1) * pl.nt_pad) : nullptr;
+
+  k_pack_src<C, I, T><<<(nsp + 255) / 256, 256, 0, st>>>(ns, nsp, sx, sy, sz, sr, ssx, ssy, ssz, spos, sstr);
+  note_launch();
+  if (!same) {
+    k_pack_tgt<C, I, T><<<(pl.nt_pad + 255) / 256, 256, 0, st>>>(nt, pl.nt_pad, tx, ty, tz, tr, tpos);
+    note_launch();
+  }
+
+  PairArgs<T, O> a;
+  a.spos = spos; a.sstr = sstr; a.ntiles = pl.ntiles; a.tiles_per_split = pl.tiles_per_split;
+  a.tpos = tpos; a.nt = nt; a.nt_pad = pl.nt_pad; a.partial = partial; a.out = out;
+  dim3 grid(pl.tblocks, pl.nsplit);
+  KernelTimer& tm = thread_timer();
+  tm.begin(st);
+  k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O><<<grid, kBlock, 0, st>>>(a);
+  note_launch();
+  tm.end(st);
+  if (pl.nsplit > 1) {
+    dim3 rg((nt + 255) / 256, NC);
+    k_reduce<NC, ACC, T, O><<<rg, 256, 0, st>>>(partial, pl.nsplit, nt, pl.nt_pad, out);
+    note_launch();
+  }
+  O3G_CUDA_TRY(cudaGetLastError());
+  return O3G_OK;
+}
+
+// Dispatch on (mode, grads, target kind) for one core; declared here, defined per core
+// in o3g_pair_<core>.cu so the instantiations compile in parallel.
+struct PtPtCall {
+  int mode;      // MODE_*
+  bool grads;
+  int ns, nt;
+  bool same;     // sources and targets are the same packed set
+  cudaStream_t st;
+};
+template <int C>
+int32_t ptpt_core_f(const PtPtCall& c, const float* sx, const float* sy, const float* sz, const float* sr,
+                    const float* ssx, const float* ssy, const float* ssz, const float* tx, const float* ty,
+                    const float* tz, const float* tr, OutPtrs<float> out, size_t* need, char* ws);
+template <int C>
+int32_t ptpt_core_d(const PtPtCall& c, const double* sx, const double* sy, const double* sz, const double* sr,
+                    const double* ssx, const double* ssy, const double* ssz, const double* tx, const double* ty,
+                    const double* tz, const double* tr, OutPtrs<double> out, size_t* need, char* ws);
+
+#define O3G_DEFINE_PTPT_CORE(CORE)                                                                          \
+  template <>                                                                                               \
+  int32_t ptpt_core_f<CORE>(const PtPtCall& c, const float* sx, const float* sy, const float* sz,           \
+                            const float* sr, const float* ssx, const float* ssy, const float* ssz,          \
+                            const float* tx, const float* ty, const float* tz, const float* tr,             \
+                            OutPtrs<float> out, size_t* need, char* ws) {                                   \
+    const bool htr = (tr != nullptr);                                                                       \
+    if (c.mode == MODE_PLAIN) {                                                                             \
+      if (c.grads) {                                                                                        \
+        if (htr) return run_points_points<CORE, MODE_PLAIN, true, true, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+        return run_points_points<CORE, MODE_PLAIN, true, false, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+      }                                                                                                     \
+      if (htr) return run_points_points<CORE, MODE_PLAIN, false, true, 4, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+      return run_points_points<CORE, MODE_PLAIN, false, false, 4, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+    }                                                                                                       \
+    if (c.mode == MODE_COMP) {                                                                              \
+      if (c.grads) {                                                                                        \
+        if (htr) return run_points_points<CORE, MODE_COMP, true, true, 1, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+        return run_points_points<CORE, MODE_COMP, true, false, 1, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+      }                                                                                                     \
+      if (htr) return run_points_points<CORE, MODE_COMP, false, true, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+      return run_points_points<CORE, MODE_COMP, false, false, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+    }                                                                                                       \
+    if (c.grads) {                                                                                          \
+      if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+      return run_points_points<CORE, MODE_FP64, true, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+    }                                                                                                       \
+    if (htr) return run_points_points<CORE, MODE_FP64, false, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+    return run_points_points<CORE, MODE_FP64, false, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+  }                                                                                                         \
+  template <>                                                                                               \
+  int32_t ptpt_core_d<CORE>(const PtPtCall& c, const double* sx, const double* sy, const double* sz,        \
+                            const double* sr, const double* ssx, const double* ssy, const double* ssz,      \
+                            const double* tx, const double* ty, const double* tz, const double* tr,         \
+                            OutPtrs<double> out, size_t* need, char* ws) {                                  \
+    const bool htr = (tr != nullptr);                                                                       \
+    if (c.grads) {                                                                                          \
+      if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+      return run_points_points<CORE, MODE_FP64, true, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+    }                                                                                                       \
+    if (htr) return run_points_points<CORE, MODE_FP64, false, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+    return run_points_points<CORE, MODE_FP64, false, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+  }
+
+}  // namespace o3g

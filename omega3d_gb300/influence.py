@@ -1,0 +1,171 @@
+"""Reference-shaped call surface over the C-ABI: Points / ResultsType / ExecEnv /
+points_affect_points, mirroring Omega3D's Influence.h:67 (points_affect_points),
+Points.h (the SoA particle container) and ExecEnv.h / ResultsType.h.
+
+Arrays are either numpy arrays (host memory: the C-ABI stages them through the GPU
+inside the call) or torch CUDA tensors (device memory: the call is asynchronous on
+the given stream).  Positions/strengths/velocities are [3, n], gradients [9, n] in
+the reference order (Kernels.h:184-192), radii/elongations [n]; all float32 (or all
+float64 for the double entry point).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+try:  # torch is only needed for device-resident arrays
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+class ResultsType:
+    """ResultsType.h: which results a target wants."""
+    velonly = "velonly"
+    velandgrad = "velandgrad"
+
+    def __init__(self, kind="velandgrad"):
+        if kind not in (self.velonly, self.velandgrad):
+            raise ValueError("ResultsType must be 'velonly' or 'velandgrad'")
+        self.kind = kind
+
+    def compute_grad(self):
+        return self.kind == self.velandgrad
+
+
+class ExecEnv:
+    """ExecEnv.h counterpart: core function, pair-sum precision and CUDA stream."""
+
+    def __init__(self, core="rm", precision="plain", stream=None):
+        if core not in L.CORES:
+            raise ValueError("unknown core %r" % (core,))
+        if precision not in L.PRECS:
+            raise ValueError("unknown precision %r" % (precision,))
+        self.core = core
+        self.precision = precision
+        self.stream = stream
+
+    def stream_handle(self, on_device):
+        if self.stream is None:
+            if on_device and torch is not None:
+                return torch.cuda.current_stream().cuda_stream
+            return 0
+        if torch is not None and isinstance(self.stream, torch.cuda.Stream):
+            return self.stream.cuda_stream
+        return int(self.stream)
+
+
+def _is_dev(a):
+    return torch is not None and isinstance(a, torch.Tensor) and a.is_cuda
+
+
+def _dtype_ok(a, dt):
+    if _is_dev(a):
+        return a.dtype == (torch.float32 if dt == np.float32 else torch.float64) and a.is_contiguous()
+    return isinstance(a, np.ndarray) and a.dtype == dt and a.flags["C_CONTIGUOUS"]
+
+
+def _base(a):
+    return a.data_ptr() if _is_dev(a) else a.ctypes.data
+
+
+def _rows(a, k):
+    """Pointers to the k component rows of a C-contiguous [k, n] array."""
+    n = a.shape[1]
+    item = a.element_size() if _is_dev(a) else a.itemsize
+    b = _base(a)
+    return [b + i * n * item for i in range(k)]
+
+
+class Points:
+    """Points<S> (Points.h:50-140): positions x[3,n], strengths s[3,n], core radii r[n],
+    velocities u[3,n] and optional gradients ug[9,n].  `inert` marks field points
+    (elem_t inert, Omega3D.h:33): they have no radius and no strength."""
+
+    def __init__(self, x, s=None, r=None, inert=False, grads=True, u=None, ug=None):
+        self.x = x
+        self.s = s
+        self.r = r
+        self.inert = inert
+        n = x.shape[1]
+        dev = _is_dev(x)
+        dt = x.dtype
+        if u is None:
+            u = torch.zeros((3, n), dtype=dt, device=x.device) if dev else np.zeros((3, n), dt)
+        if ug is None and grads:
+            ug = torch.zeros((9, n), dtype=dt, device=x.device) if dev else np.zeros((9, n), dt)
+        self.u = u
+        self.ug = ug
+
+    @property
+    def n(self):
+        return self.x.shape[1]
+
+    def zero_vels(self):
+        """ElementBase.h:174-184 / Points.h:255-262."""
+        for a in (self.u, self.ug):
+            if a is not None:
+                a[...] = 0
+
+    def finalize_vels(self, fs=(0.0, 0.0, 0.0)):
+        """u = fs + u/(4 pi); ug *= 1/(4 pi)  (ElementBase.h:187-193, Points.h:265-277)."""
+        fac = 0.25 / np.pi
+        for d in range(3):
+            self.u[d] = fs[d] + self.u[d] * fac
+        if self.ug is not None:
+            self.ug *= np.float32(fac) if self.ug.dtype in (np.float32,) else fac
+
+
+def points_affect_points(src, targ, restype=None, env=None):
+    """Influence.h:67: accumulate (+=) the velocity (and gradients) induced by the vortex
+    particles `src` at the points `targ`.  No 1/4pi factor (see Points.finalize_vels)."""
+    restype = restype or ResultsType()
+    env = env or ExecEnv()
+    if src.inert:
+        raise ValueError("inert points cannot be sources")
+    grads = restype.compute_grad()
+    if grads and targ.ug is None:
+        raise ValueError("targets have no velocity-gradient arrays")
+    dt = np.float64 if (src.x.dtype in (np.float64,) or (_is_dev(src.x) and src.x.dtype == torch.float64)) \
+        else np.float32
+    arrays = [src.x, src.s, src.r, targ.x, targ.u] + ([targ.ug] if grads else []) + \
+             ([targ.r] if not targ.inert else [])
+    on_dev = _is_dev(src.x)
+    for a in arrays:
+        if _is_dev(a) != on_dev:
+            raise ValueError("all arrays must live in the same memory (numpy host or torch CUDA)")
+        if not _dtype_ok(a, dt):
+            raise ValueError("arrays must be C-contiguous %s" % np.dtype(dt).name)
+    sxp = _rows(src.x, 3)
+    ssp = _rows(src.s, 3)
+    txp = _rows(targ.x, 3)
+    tup = _rows(targ.u, 3)
+    tug = None
+    if grads:
+        tug = (ctypes.c_void_p * 9)(*_rows(targ.ug, 9))
+    tr = None if targ.inert else _base(targ.r)
+    mem = L.MEM_DEVICE if on_dev else L.MEM_HOST
+    stream = env.stream_handle(on_dev)
+    lib = L.lib()
+    if dt == np.float64:
+        st = lib.o3g_points_affect_points_d(L.CORES[env.core], mem, src.n, *sxp, _base(src.r), *ssp,
+                                            targ.n, *txp, tr, *tup, tug, stream)
+        L.check(st, "o3g_points_affect_points_d")
+    else:
+        st = lib.o3g_points_affect_points(L.CORES[env.core], L.PRECS[env.precision], mem, src.n, *sxp,
+                                          _base(src.r), *ssp, targ.n, *txp, tr, *tup, tug, stream)
+        L.check(st, "o3g_points_affect_points")
+
+
+class InfluenceVisitor:
+    """Influence.h:1251-1261: dispatch on (source kind, target kind)."""
+
+    def __init__(self, restype=None, env=None):
+        self.restype = restype or ResultsType()
+        self.env = env or ExecEnv()
+
+    def __call__(self, src, targ):
+        if isinstance(src, Points) and isinstance(targ, Points):
+            return points_affect_points(src, targ, self.restype, self.env)
+        raise NotImplementedError("pairing %s -> %s" % (type(src).__name__, type(targ).__name__))

@@ -1,0 +1,43 @@
+#!/bin/sh
+# TEST INFRASTRUCTURE ONLY.
+#
+# Builds oracle/_ref/libo3dref_<core>.so from the reference's own pair/panel kernels,
+# compiled where they lie (no copy of the reference is written anywhere):
+#   src/MathHelper.h  (included through -I)
+#   src/CoreFunc.h    (streamed; for RM/EXP/V2 the hard-wired `#define USE_WL_KERNEL`
+#                      at CoreFunc.h:37 is switched to the chosen core in the stream,
+#                      the switch the reference documents at CoreFunc.h:35-39)
+#   src/Kernels.h     (streamed; its `#include "CoreFunc.h"` is dropped because the
+#                      switched CoreFunc.h precedes it in the same stream)
+#   oracle/ref_driver.cpp (this project's restatement of the loops around them)
+#
+# The reference location defaults to /root/reference/src; set O3D_REFERENCE_SRC to
+# override.  When the sources are absent (e.g. on a machine without the reference) the
+# script prints a note and exits 0: the ref libraries are a checker, not the product.
+set -e
+REF="${O3D_REFERENCE_SRC:-/root/reference/src}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+if [ ! -f "$REF/Kernels.h" ] || [ ! -f "$REF/CoreFunc.h" ] || [ ! -f "$REF/MathHelper.h" ]; then
+  echo "build_ref: reference sources not found under $REF; oracle/_ref not built"
+  exit 0
+fi
+CXX="${CXX:-g++}"
+mkdir -p "$OUT"
+for core in RM WL EXP V2; do
+  lc=$(echo "$core" | tr 'A-Z' 'a-z')
+  macro="$core"
+  [ "$core" = EXP ] && macro=EXPONENTIAL
+  {
+    if [ "$core" = WL ]; then
+      cat "$REF/CoreFunc.h"
+    else
+      sed -e 's|^#define USE_WL_KERNEL|/* WL switched off for this build */|' \
+          -e "s|^//#define USE_${macro}_KERNEL|#define USE_${macro}_KERNEL|" "$REF/CoreFunc.h"
+    fi
+    sed -e 's|^#include "CoreFunc.h"|/* CoreFunc.h streamed above */|' "$REF/Kernels.h"
+    cat "$HERE/ref_driver.cpp"
+  } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w -I"$REF" -x c++ - \
+        -o "$OUT/libo3dref_$lc.so"
+  echo "build_ref: built $OUT/libo3dref_$lc.so"
+done

@@ -1,0 +1,259 @@
+"""TEST INFRASTRUCTURE ONLY.
+
+numpy front end of the C++ oracle (oracle/o3d_oracle.cpp) and of the reference-kernel
+libraries built by oracle/build_ref.sh into oracle/_ref/.  Arrays are component-major
+SoA exactly like the reference's std::array<Vector<S>,3> (x[3, n]); gradients are
+[9, n] in the reference order (Kernels.h:184-192).
+
+prec 0: S=A=float (reference Vc build), 1: S=float, A=double (non-Vc build),
+prec 2: S=A=double (FP64 oracle).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libo3d_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+CORES = {"rm": 0, "wl": 1, "exp": 2, "gauss": 3, "v2": 4}
+REF_CORES = ("rm", "wl", "exp", "v2")   # cores the reference itself implements
+
+_lib = None
+_ref = {}
+
+
+def build_oracle(force=False):
+    """Compile oracle/o3d_oracle.cpp into oracle/libo3d_oracle.so."""
+    src = os.path.join(HERE, "o3d_oracle.cpp")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+        return LIB_PATH
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+           src, "-o", LIB_PATH]
+    subprocess.run(cmd, check=True)
+    return LIB_PATH
+
+
+def build_ref():
+    """Compile the reference's own kernels into oracle/_ref (no-op without the sources)."""
+    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle()
+        _lib = ctypes.CDLL(LIB_PATH)
+    return _lib
+
+
+def ref_available(core="rm"):
+    return os.path.exists(os.path.join(REF_DIR, "libo3dref_%s.so" % core))
+
+
+def ref_lib(core):
+    if core not in _ref:
+        path = os.path.join(REF_DIR, "libo3dref_%s.so" % core)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        _ref[core] = ctypes.CDLL(path)
+    return _ref[core]
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _dtypes(prec):
+    return np.float64 if prec == 2 else np.float32
+
+
+def _as(a, dt):
+    if a is None:
+        return None
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def _nthreads(nthreads):
+    return int(nthreads) if nthreads else (os.cpu_count() or 1)
+
+
+def points_affect_points(src_x, src_r, src_s, targ_x, targ_r=None, grads=True, core="rm", prec=0,
+                         nthreads=0, use_ref=False):
+    """Returns (u[3,nt], ug[9,nt] or None) accumulated from zero."""
+    dt = _dtypes(prec)
+    sx, sr, ss = _as(src_x, dt), _as(src_r, dt), _as(src_s, dt)
+    tx, tr = _as(targ_x, dt), _as(targ_r, dt)
+    ns, nt = sr.shape[0], tx.shape[1]
+    tu = np.zeros((3, nt), dt)
+    tug = np.zeros((9, nt), dt) if grads else None
+    if use_ref:
+        rc = ref_lib(core).ref_points_affect_points(
+            ctypes.c_int(prec), ctypes.c_int(ns), _p(sx), _p(sr), _p(ss), ctypes.c_int(nt), _p(tx), _p(tr),
+            _p(tu), _p(tug))
+    else:
+        rc = lib().o3o_points_affect_points(
+            ctypes.c_int(prec), ctypes.c_int(CORES[core]), ctypes.c_int(ns), _p(sx), _p(sr), _p(ss),
+            ctypes.c_int(nt), _p(tx), _p(tr), _p(tu), _p(tug), ctypes.c_int(_nthreads(nthreads)))
+    if rc != 0:
+        raise RuntimeError("oracle points_affect_points failed")
+    return tu, tug
+
+
+def panels_affect_points(nodes, idx, area, ts, targ_x, sss=None, grads=True, core="rm", prec=0, maxlev=3,
+                         nthreads=0, use_ref=False):
+    dt = _dtypes(prec)
+    nx, ar, t, tx, s3 = _as(nodes, dt), _as(area, dt), _as(ts, dt), _as(targ_x, dt), _as(sss, dt)
+    idx = np.ascontiguousarray(idx, dtype=np.uint32)
+    nn, np_, nt = nx.shape[1], ar.shape[0], tx.shape[1]
+    tu = np.zeros((3, nt), dt)
+    tug = np.zeros((9, nt), dt) if grads else None
+    if use_ref:
+        rc = ref_lib(core).ref_panels_affect_points(
+            ctypes.c_int(prec), ctypes.c_int(maxlev), ctypes.c_int(nn), _p(nx), ctypes.c_int(np_), _p(idx),
+            _p(ar), _p(t), _p(s3), ctypes.c_int(nt), _p(tx), _p(tu), _p(tug))
+    else:
+        rc = lib().o3o_panels_affect_points(
+            ctypes.c_int(prec), ctypes.c_int(CORES[core]), ctypes.c_int(maxlev), ctypes.c_int(nn), _p(nx),
+            ctypes.c_int(np_), _p(idx), _p(ar), _p(t), _p(s3), ctypes.c_int(nt), _p(tx), _p(tu), _p(tug),
+            ctypes.c_int(_nthreads(nthreads)))
+    if rc != 0:
+        raise RuntimeError("oracle panels_affect_points failed")
+    return tu, tug
+
+
+def points_affect_panels(src_x, src_s, nodes, idx, area, core="rm", prec=0, maxlev=3, nthreads=0, use_ref=False):
+    """Returns the (negated, reference convention) panel velocities pu[3, np] from zero."""
+    dt = _dtypes(prec)
+    sx, ss, nx, ar = _as(src_x, dt), _as(src_s, dt), _as(nodes, dt), _as(area, dt)
+    idx = np.ascontiguousarray(idx, dtype=np.uint32)
+    ns, nn, np_ = sx.shape[1], nx.shape[1], ar.shape[0]
+    pu = np.zeros((3, np_), dt)
+    if use_ref:
+        rc = ref_lib(core).ref_points_affect_panels(
+            ctypes.c_int(prec), ctypes.c_int(maxlev), ctypes.c_int(ns), _p(sx), _p(ss), ctypes.c_int(nn), _p(nx),
+            ctypes.c_int(np_), _p(idx), _p(ar), _p(pu))
+    else:
+        rc = lib().o3o_points_affect_panels(
+            ctypes.c_int(prec), ctypes.c_int(CORES[core]), ctypes.c_int(maxlev), ctypes.c_int(ns), _p(sx), _p(ss),
+            ctypes.c_int(nn), _p(nx), ctypes.c_int(np_), _p(idx), _p(ar), _p(pu), ctypes.c_int(_nthreads(nthreads)))
+    if rc != 0:
+        raise RuntimeError("oracle points_affect_panels failed")
+    return pu
+
+
+def panels_on_panels_coeff(src, targ, nunk=2, is_self=True, core="rm", prec=0, maxlev=3, nthreads=0,
+                           use_ref=False):
+    """src/targ: dicts with nodes[3,nn], idx[np*3], area[np], x1[3,np], x2[3,np], norm[3,np].
+    Returns the column-major block as a (ncols, nrows) array (row index fastest)."""
+    dt = _dtypes(prec)
+    S = {k: (_as(v, dt) if k != "idx" else np.ascontiguousarray(v, np.uint32)) for k, v in src.items()}
+    T = {k: (_as(v, dt) if k != "idx" else np.ascontiguousarray(v, np.uint32)) for k, v in targ.items()}
+    snp, tnp = S["area"].shape[0], T["area"].shape[0]
+    out = np.zeros((snp * nunk, tnp * nunk), dt)
+    args = [ctypes.c_int(maxlev), ctypes.c_int(nunk), ctypes.c_int(1 if is_self else 0),
+            ctypes.c_int(S["nodes"].shape[1]), _p(S["nodes"]), ctypes.c_int(snp), _p(S["idx"]), _p(S["area"]),
+            _p(S["x1"]), _p(S["x2"]),
+            ctypes.c_int(T["nodes"].shape[1]), _p(T["nodes"]), ctypes.c_int(tnp), _p(T["idx"]), _p(T["area"]),
+            _p(T["x1"]), _p(T["x2"]), _p(T["norm"]), _p(out)]
+    if use_ref:
+        rc = ref_lib(core).ref_panels_on_panels_coeff(ctypes.c_int(prec), *args)
+    else:
+        rc = lib().o3o_panels_on_panels_coeff(ctypes.c_int(prec), ctypes.c_int(CORES[core]), *args,
+                                              ctypes.c_int(_nthreads(nthreads)))
+    if rc != 0:
+        raise RuntimeError("oracle panels_on_panels_coeff failed")
+    return out
+
+
+def compute_bases(nodes, idx):
+    nx = _as(nodes, np.float32)
+    idx = np.ascontiguousarray(idx, np.uint32)
+    np_ = idx.shape[0] // 3
+    x1, x2, nm = (np.zeros((3, np_), np.float32) for _ in range(3))
+    area = np.zeros(np_, np.float32)
+    rc = lib().o3o_compute_bases(ctypes.c_int(nx.shape[1]), _p(nx), ctypes.c_int(np_), _p(idx),
+                                 _p(x1), _p(x2), _p(nm), _p(area))
+    if rc != 0:
+        raise RuntimeError("oracle compute_bases failed")
+    return x1, x2, nm, area
+
+
+def sheet_to_panel_strength(ps0, ps1, x1, x2, area):
+    np_ = area.shape[0]
+    ts = np.zeros((3, np_), np.float32)
+    args = [_as(ps0, np.float32), _as(ps1, np.float32), _as(x1, np.float32), _as(x2, np.float32),
+            _as(area, np.float32)]
+    rc = lib().o3o_sheet_to_panel_strength(ctypes.c_int(np_), *[_p(a) for a in args], _p(ts))
+    if rc != 0:
+        raise RuntimeError("oracle sheet_to_panel_strength failed")
+    return ts
+
+
+def vels_to_rhs_panels(pu, x1, x2, norm, nunk=2):
+    np_ = pu.shape[1]
+    rhs = np.zeros(np_ * nunk, np.float32)
+    args = [_as(pu, np.float32), _as(x1, np.float32), _as(x2, np.float32), _as(norm, np.float32)]
+    rc = lib().o3o_vels_to_rhs_panels(ctypes.c_int(np_), ctypes.c_int(nunk), *[_p(a) for a in args], _p(rhs))
+    if rc != 0:
+        raise RuntimeError("oracle vels_to_rhs_panels failed")
+    return rhs
+
+
+def finalize_vels(u, ug, fs=(0.0, 0.0, 0.0)):
+    """In place: u = fs + u/(4 pi) (double arithmetic), ug *= float(1/(4 pi))."""
+    fsa = np.ascontiguousarray(fs, np.float64)
+    rc = lib().o3o_finalize_vels(ctypes.c_int(u.shape[1]), _p(fsa), _p(u), _p(ug))
+    if rc != 0:
+        raise RuntimeError("oracle finalize_vels failed")
+
+
+def points_move_euler(x, s, elong, u, ug, dt, wt1=1.0):
+    rc = lib().o3o_points_move_euler(ctypes.c_int(x.shape[1]), ctypes.c_double(dt), ctypes.c_double(wt1),
+                                     _p(x), _p(s), _p(elong), _p(u), _p(ug))
+    if rc != 0:
+        raise RuntimeError("oracle points_move_euler failed")
+
+
+def points_move_rk2(x, s, elong, u1, ug1, u2, ug2, dt, wt1=0.25, wt2=0.75):
+    rc = lib().o3o_points_move_rk2(ctypes.c_int(x.shape[1]), ctypes.c_double(dt), ctypes.c_double(wt1),
+                                   _p(u1), _p(ug1), ctypes.c_double(wt2), _p(u2), _p(ug2), _p(x), _p(s),
+                                   _p(elong))
+    if rc != 0:
+        raise RuntimeError("oracle points_move_rk2 failed")
+
+
+def generate_ovoid(levels, rx=1.0, ry=1.0, rz=1.0):
+    nn, np_ = 10 * 4 ** levels + 2, 20 * 4 ** levels
+    x = np.zeros((3, nn), np.float32)
+    idx = np.zeros(3 * np_, np.uint32)
+    rc = lib().o3o_generate_ovoid(ctypes.c_int(levels), ctypes.c_float(rx), ctypes.c_float(ry),
+                                  ctypes.c_float(rz), _p(x), _p(idx))
+    if rc != 0:
+        raise RuntimeError("oracle generate_ovoid failed")
+    return x, idx
+
+
+def flops_per_pair(core="rm", grads=True, have_tr=True):
+    return int(lib().o3o_flops_per_pair(ctypes.c_int(CORES[core]), ctypes.c_int(int(grads)),
+                                        ctypes.c_int(int(have_tr))))
+
+
+def ralston_step(x, s, r, elong, dt, core="rm", prec=1, fs=(0.0, 0.0, 0.0), nthreads=0):
+    """One inviscid, boundary-free Ralston RK2 step of a particle set (Convection.h:349-425):
+    returns new (x, s, elong) plus the stage-1 (u, ug) evaluated at the starting state."""
+    x0, s0, e0 = x.copy(), s.copy(), elong.copy()
+    u1, ug1 = points_affect_points(x0, r, s0, x0, r, True, core, prec, nthreads)
+    u1, ug1 = u1.astype(np.float32), ug1.astype(np.float32)
+    finalize_vels(u1, ug1, fs)
+    xi, si, ei = x0.copy(), s0.copy(), e0.copy()
+    points_move_euler(xi, si, ei, u1, ug1, 2.0 / 3.0 * dt, 1.0)
+    u2, ug2 = points_affect_points(xi, r, si, xi, r, True, core, prec, nthreads)
+    u2, ug2 = u2.astype(np.float32), ug2.astype(np.float32)
+    finalize_vels(u2, ug2, fs)
+    uc = u1.copy()
+    points_move_rk2(x0, s0, e0, uc, ug1, u2, ug2, dt, 0.25, 0.75)
+    return x0, s0, e0, u1, ug1

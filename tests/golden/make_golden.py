@@ -1,0 +1,111 @@
+"""Generates the golden vectors in tests/golden/ from the REFERENCE's own kernels.
+
+Run in a checkout that has the reference sources (oracle/build_ref.sh compiles
+src/Kernels.h, src/CoreFunc.h and src/MathHelper.h of the reference into
+oracle/_ref/libo3dref_<core>.so; the loops around them are oracle/ref_driver.cpp):
+
+    sh oracle/build_ref.sh && python tests/golden/make_golden.py
+
+Every fixture holds its seeded inputs and the outputs of the reference build for the
+precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
+The Gaussian core has no reference implementation; its fixture comes from the oracle
+restatement and is marked "pinned": False.  The sphere fixture comes from the oracle's
+restatement of generate_ovoid + igl::upsample (the reference's version needs Eigen and
+cannot be built here) and is also marked unpinned.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from omega3d_gb300 import workloads as W  # noqa: E402
+
+
+def _save(name, meta, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+def pair_inputs():
+    x, s, r = W.gaussian_cloud(192, seed=11, pos_std=0.2, rmin=0.02, rmax=0.06)
+    tx2, _, tr2 = W.gaussian_cloud(96, seed=12, pos_std=0.25, rmin=0.02, rmax=0.06)
+    # the first 64 targets coincide with sources (self pairs, d = 0)
+    tx = np.concatenate([x[:, :64], tx2], axis=1)
+    tr = np.concatenate([r[:64], tr2])
+    return x, s, r, tx, tr
+
+
+def sphere_inputs(levels=1, scale=2.0, seed=13):
+    nodes, idx = O.generate_ovoid(levels, scale, scale, scale)
+    x1, x2, nm, area = O.compute_bases(nodes, idx)
+    rng = np.random.default_rng(seed)
+    np_ = area.shape[0]
+    ps0 = rng.normal(size=np_).astype(np.float32)
+    ps1 = rng.normal(size=np_).astype(np.float32)
+    sss = rng.normal(size=np_).astype(np.float32)
+    ts = O.sheet_to_panel_strength(ps0, ps1, x1, x2, area)
+    return dict(nodes=nodes, idx=idx, x1=x1, x2=x2, norm=nm, area=area, ps0=ps0, ps1=ps1, sss=sss, ts=ts)
+
+
+def main():
+    for core in O.REF_CORES:
+        if not O.ref_available(core):
+            raise SystemExit("oracle/_ref/libo3dref_%s.so missing: run sh oracle/build_ref.sh" % core)
+    x, s, r, tx, tr = pair_inputs()
+    for core in ("rm", "wl", "exp", "v2", "gauss"):
+        use_ref = core != "gauss"
+        out = {}
+        for prec in (0, 2):
+            u, g = O.points_affect_points(x, r, s, tx, tr, True, core, prec, use_ref=use_ref)
+            out["pg_u_p%d" % prec], out["pg_g_p%d" % prec] = u, g
+            u, g = O.points_affect_points(x, r, s, tx, None, True, core, prec, use_ref=use_ref)
+            out["fg_u_p%d" % prec], out["fg_g_p%d" % prec] = u, g
+            u, _ = O.points_affect_points(x, r, s, tx, tr, False, core, prec, use_ref=use_ref)
+            out["pv_u_p%d" % prec] = u
+        _save("ptpt_%s.npz" % core, {"core": core, "pinned": use_ref, "source": "reference kernels" if use_ref
+                                     else "oracle restatement"}, sx=x, ss=s, sr=r, tx=tx, tr=tr, **out)
+
+    sph = sphere_inputs()
+    ptx, pts, ptr = W.shell_particles(64, seed=14, rin=1.02, rout=1.5)
+    ptx[:, :8] *= np.float32(1.0 / 1.1)   # a few targets close to the surface (subdivision active)
+    for core in ("rm", "wl", "exp"):
+        out = {}
+        for prec in (0, 2):
+            u, g = O.panels_affect_points(sph["nodes"], sph["idx"], sph["area"], sph["ts"], ptx, sph["sss"], True,
+                                          core, prec, use_ref=True)
+            out["pg_u_p%d" % prec], out["pg_g_p%d" % prec] = u, g
+            u, _ = O.panels_affect_points(sph["nodes"], sph["idx"], sph["area"], sph["ts"], ptx, None, False, core,
+                                          prec, use_ref=True)
+            out["pv_u_p%d" % prec] = u
+            out["pan_u_p%d" % prec] = O.points_affect_panels(ptx, pts, sph["nodes"], sph["idx"], sph["area"], core,
+                                                             prec, use_ref=True)
+        _save("panel_%s.npz" % core, {"core": core, "pinned": True, "maxlev": 3, "source": "reference kernels"},
+              tx=ptx, ps=pts, **sph, **out)
+
+    geo = {k: sph[k] for k in ("nodes", "idx", "area", "x1", "x2", "norm")}
+    for core in ("rm", "wl"):
+        out = {}
+        for nunk in (2, 3):
+            out["c%d_p0" % nunk] = O.panels_on_panels_coeff(geo, geo, nunk, True, core, 0, use_ref=True)
+        if core == "rm":
+            out["c2_p2"] = O.panels_on_panels_coeff(geo, geo, 2, True, core, 2, use_ref=True)
+        _save("coeff_%s.npz" % core, {"core": core, "pinned": True, "maxlev": 3, "is_self": True,
+                                      "source": "reference kernels"}, **geo, **out)
+
+    arrays = {}
+    for lev in range(4):
+        n, i = O.generate_ovoid(lev, 2.0, 2.0, 2.0)
+        arrays["nodes_L%d" % lev], arrays["idx_L%d" % lev] = n, i
+    _save("sphere.npz", {"pinned": False, "scale": 2.0, "source": "oracle restatement of generate_ovoid"},
+          **arrays)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,207 @@
+"""CPU tests of the oracle: pinned against the reference's own kernels (oracle/_ref,
+when the reference sources were available to build it) and against the committed
+golden vectors made from them; plus known answers of the physics."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from omega3d_gb300 import workloads as W
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _gold(name):
+    d = np.load(os.path.join(GOLD, name))
+    return d, json.loads(str(d["meta"]))
+
+
+def _exact(a, b):
+    return a.shape == b.shape and np.array_equal(a, b)
+
+
+# ---- golden vectors (always run) --------------------------------------------------
+@pytest.mark.parametrize("core", ["rm", "wl", "exp", "v2", "gauss"])
+def test_oracle_matches_golden_pairs(core):
+    d, meta = _gold("ptpt_%s.npz" % core)
+    assert meta["core"] == core
+    for prec in (0, 2):
+        u, g = O.points_affect_points(d["sx"], d["sr"], d["ss"], d["tx"], d["tr"], True, core, prec)
+        assert _exact(u, d["pg_u_p%d" % prec]) and _exact(g, d["pg_g_p%d" % prec])
+        u, g = O.points_affect_points(d["sx"], d["sr"], d["ss"], d["tx"], None, True, core, prec)
+        assert _exact(u, d["fg_u_p%d" % prec]) and _exact(g, d["fg_g_p%d" % prec])
+        u, _ = O.points_affect_points(d["sx"], d["sr"], d["ss"], d["tx"], d["tr"], False, core, prec)
+        assert _exact(u, d["pv_u_p%d" % prec])
+
+
+@pytest.mark.parametrize("core", ["rm", "wl", "exp"])
+def test_oracle_matches_golden_panels(core):
+    d, meta = _gold("panel_%s.npz" % core)
+    for prec in (0, 2):
+        u, g = O.panels_affect_points(d["nodes"], d["idx"], d["area"], d["ts"], d["tx"], d["sss"], True, core, prec)
+        assert _exact(u, d["pg_u_p%d" % prec]) and _exact(g, d["pg_g_p%d" % prec])
+        u, _ = O.panels_affect_points(d["nodes"], d["idx"], d["area"], d["ts"], d["tx"], None, False, core, prec)
+        assert _exact(u, d["pv_u_p%d" % prec])
+        pu = O.points_affect_panels(d["tx"], d["ps"], d["nodes"], d["idx"], d["area"], core, prec)
+        assert _exact(pu, d["pan_u_p%d" % prec])
+
+
+@pytest.mark.parametrize("core", ["rm", "wl"])
+def test_oracle_matches_golden_coefficients(core):
+    d, meta = _gold("coeff_%s.npz" % core)
+    geo = {k: d[k] for k in ("nodes", "idx", "area", "x1", "x2", "norm")}
+    for nunk in (2, 3):
+        c = O.panels_on_panels_coeff(geo, geo, nunk, True, core, 0)
+        assert _exact(c, d["c%d_p0" % nunk])
+    if "c2_p2" in d:
+        assert _exact(O.panels_on_panels_coeff(geo, geo, 2, True, core, 2), d["c2_p2"])
+
+
+def test_sphere_fixture_and_topology():
+    d, meta = _gold("sphere.npz")
+    for lev in range(4):
+        n, i = O.generate_ovoid(lev, 2.0, 2.0, 2.0)
+        assert n.shape == (3, 10 * 4 ** lev + 2) and i.shape == (3 * 20 * 4 ** lev,)
+        assert _exact(n, d["nodes_L%d" % lev]) and _exact(i, d["idx_L%d" % lev])
+        # every edge shared by exactly two faces, in opposite orientation (closed 2-manifold)
+        f = i.reshape(-1, 3)
+        e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+        assert len({tuple(x) for x in e}) == len(e)
+        assert {tuple(x) for x in e} == {tuple(x) for x in e[:, ::-1]}
+        # the first 12 nodes are the icosahedron and old nodes keep their numbers
+        if lev > 0:
+            prev = d["nodes_L%d" % (lev - 1)]
+            assert np.allclose(np.linalg.norm(n, axis=0), 1.0, atol=1e-6)
+            assert np.allclose(n[:, :prev.shape[1]], prev, atol=1e-6)
+
+
+# ---- pinned against the reference's own kernels (needs oracle/_ref) --------------
+def _need_ref(core):
+    if not O.ref_available(core):
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+
+
+@pytest.mark.parametrize("core", list(O.REF_CORES))
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_oracle_bit_exact_vs_reference_pairs(core, prec):
+    _need_ref(core)
+    x, s, r = W.gaussian_cloud(257, seed=21, pos_std=0.2)
+    tx, _, tr = W.gaussian_cloud(131, seed=22, pos_std=0.2)
+    for trr in (tr, None):
+        for grads in (True, False):
+            a = O.points_affect_points(x, r, s, tx, trr, grads, core, prec)
+            b = O.points_affect_points(x, r, s, tx, trr, grads, core, prec, use_ref=True)
+            assert _exact(a[0], b[0])
+            if grads:
+                assert _exact(a[1], b[1])
+
+
+@pytest.mark.parametrize("core", list(O.REF_CORES))
+def test_oracle_bit_exact_vs_reference_panels(core):
+    _need_ref(core)
+    nodes, idx = O.generate_ovoid(1, 2.0, 2.0, 2.0)
+    x1, x2, nm, area = O.compute_bases(nodes, idx)
+    rng = np.random.default_rng(5)
+    ts = O.sheet_to_panel_strength(rng.normal(size=80).astype(np.float32), rng.normal(size=80).astype(np.float32),
+                                   x1, x2, area)
+    sss = rng.normal(size=80).astype(np.float32)
+    tx, ps, _ = W.shell_particles(50, seed=23, rin=1.01, rout=1.3)
+    for prec in (0, 1, 2):
+        a = O.panels_affect_points(nodes, idx, area, ts, tx, sss, True, core, prec)
+        b = O.panels_affect_points(nodes, idx, area, ts, tx, sss, True, core, prec, use_ref=True)
+        assert _exact(a[0], b[0]) and _exact(a[1], b[1])
+        a = O.points_affect_panels(tx, ps, nodes, idx, area, core, prec)
+        b = O.points_affect_panels(tx, ps, nodes, idx, area, core, prec, use_ref=True)
+        assert _exact(a, b)
+    geo = dict(nodes=nodes, idx=idx, area=area, x1=x1, x2=x2, norm=nm)
+    for prec in (0, 2):
+        for nunk in (2, 3):
+            a = O.panels_on_panels_coeff(geo, geo, nunk, True, core, prec)
+            b = O.panels_on_panels_coeff(geo, geo, nunk, True, core, prec, use_ref=True)
+            assert _exact(a, b)
+
+
+# ---- known answers ----------------------------------------------------------------
+@pytest.mark.parametrize("core", ["rm", "wl", "exp", "gauss", "v2"])
+def test_far_field_is_singular_biot_savart(core):
+    # a particle far from its core sees the singular kernel u = (s x d)/|d|^3, d = target - source
+    sx = np.zeros((3, 1), np.float64)
+    ss = np.array([[0.0], [0.0], [1.0]])
+    sr = np.array([1e-6])
+    tx = np.array([[3.0], [0.5], [-0.2]])
+    u, g = O.points_affect_points(sx, sr, ss, tx, None, True, core, 2)
+    d = tx[:, 0]
+    uref = np.cross(ss[:, 0], d) / np.linalg.norm(d) ** 3
+    assert np.allclose(u[:, 0], uref, rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("core", ["rm", "wl", "exp", "gauss", "v2"])
+def test_self_pair_has_zero_velocity_and_antisymmetric_gradient(core):
+    sx = np.array([[0.3], [0.1], [-0.2]])
+    ss = np.array([[0.2], [-0.5], [0.7]])
+    sr = np.array([0.05])
+    u, g = O.points_affect_points(sx, sr, ss, sx, sr, True, core, 2)
+    assert np.all(u == 0.0)
+    G = g[:, 0].reshape(3, 3)        # G[j][i] = d u_i / d x_j
+    assert np.abs(G).max() > 0
+    assert np.allclose(G, -G.T, rtol=0, atol=1e-12 * np.abs(G).max())
+
+
+@pytest.mark.parametrize("core", ["rm", "wl", "gauss"])
+def test_gradient_is_derivative_of_velocity(core):
+    x, s, r = W.gaussian_cloud(64, seed=31, pos_std=0.2, rmin=0.05, rmax=0.08)
+    x, s, r = x.astype(np.float64), s.astype(np.float64), r.astype(np.float64)
+    t = np.array([[0.05], [-0.02], [0.03]])
+    _, g = O.points_affect_points(x, r, s, t, None, True, core, 2)
+    h = 1e-5
+    for j in range(3):
+        tp, tm = t.copy(), t.copy()
+        tp[j] += h
+        tm[j] -= h
+        up, _ = O.points_affect_points(x, r, s, tp, None, False, core, 2)
+        um, _ = O.points_affect_points(x, r, s, tm, None, False, core, 2)
+        fd = (up[:, 0] - um[:, 0]) / (2 * h)
+        assert np.allclose(g[3 * j:3 * j + 3, 0], fd, rtol=1e-5, atol=1e-7 * np.abs(g).max())
+
+
+def test_gaussian_core_matches_closed_form_on_every_branch():
+    # the oracle's Gaussian core (series for q < 1, closed form, singular beyond q_far)
+    # against an independent float64 evaluation of K = [erf(rho/sqrt2) - sqrt(2/pi) rho e^(-q/2)] / r^3
+    from scipy.special import erf
+    sig = 0.1
+    sx = np.zeros((3, 1))
+    ss = np.array([[0.1], [0.4], [0.9]])
+    sr = np.array([sig])
+    for q in (0.01, 0.5, 0.999, 1.001, 5.0, 47.9, 48.1, 89.9, 90.1, 200.0):
+        rad = np.sqrt(q) * sig
+        d = np.array([rad, 0.0, 0.0])
+        rho = np.sqrt(q)
+        K = (erf(rho / np.sqrt(2)) - np.sqrt(2 / np.pi) * rho * np.exp(-0.5 * q)) / rad ** 3
+        uref = K * np.cross(ss[:, 0], d)
+        for prec, tol in ((2, 1e-10), (0, 3e-6)):
+            dt = np.float64 if prec == 2 else np.float32
+            u, _ = O.points_affect_points(sx.astype(dt), sr.astype(dt), ss.astype(dt), d[:, None].astype(dt), None,
+                                          True, "gauss", prec)
+            err = np.abs(np.asarray(u, np.float64)[:, 0] - uref).max() / np.abs(uref).max()
+            assert err < tol, (q, prec, err)
+
+
+def test_divergence_free_gradient_trace():
+    x, s, r = W.gaussian_cloud(128, seed=41, pos_std=0.3)
+    t, _, _ = W.gaussian_cloud(64, seed=42, pos_std=0.3)
+    for core in ("rm", "wl", "gauss"):
+        _, g = O.points_affect_points(x.astype(np.float64), r.astype(np.float64), s.astype(np.float64),
+                                      t.astype(np.float64), None, True, core, 2)
+        # trace of the singular part vanishes; regularised cores keep it small relative to |grad|
+        tr = g[0] + g[4] + g[8]
+        assert np.all(np.isfinite(tr))
+
+
+def test_flop_counts_match_reference_accounting():
+    assert O.flops_per_pair("rm", True, True) == 63
+    assert O.flops_per_pair("rm", True, False) == 61
+    assert O.flops_per_pair("wl", True, True) == 70
+    assert O.flops_per_pair("exp", True, True) == 68
+    assert O.flops_per_pair("rm", False, True) == 30

@@ -1,0 +1,167 @@
+"""GPU parity tests of points_affect_points through the C-ABI (libo3dgpu.so).
+
+Tolerances (per-target relative error, metrics.rel_err, floor 1e-6 of the max):
+  * PLAIN vs the reference's FP32 pair arithmetic with double accumulators (the
+    reference's non-Vc build, Simulation.h:44-46; oracle prec 1): max <= 1e-5, the
+    FP32-summation-reordering tolerance of the drop-in path.
+  * PLAIN vs the golden vectors of the reference's Vc-semantics build (prec 0): max <= 1e-5.
+  * COMPENSATED vs the FP64 oracle: max <= 2e-6.
+  * FP64 vs the FP64 oracle / golden: max <= 1e-11.
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from omega3d_gb300 import ExecEnv, Points, ResultsType, points_affect_points
+from omega3d_gb300 import _lib as L
+from omega3d_gb300 import workloads as W
+from omega3d_gb300.metrics import rel_err
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CORES = ["rm", "wl", "exp", "gauss", "v2"]
+
+
+def _dev(a, dtype=None):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(a if dtype is None else a.astype(dtype)))
+    return t.cuda()
+
+
+def gpu_eval(sx, ss, sr, tx, tr, grads=True, core="rm", prec="plain", on_device=True, dtype=np.float32,
+             u0=None, g0=None):
+    import torch
+    cv = (lambda a: _dev(a, dtype)) if on_device else (lambda a: np.ascontiguousarray(a.astype(dtype)))
+    src = Points(cv(sx), cv(ss), cv(sr))
+    targ = Points(cv(tx), None, None if tr is None else cv(tr), inert=tr is None, grads=grads,
+                  u=None if u0 is None else cv(u0), ug=None if g0 is None else cv(g0))
+    points_affect_points(src, targ, ResultsType("velandgrad" if grads else "velonly"), ExecEnv(core, prec))
+    if on_device:
+        torch.cuda.synchronize()
+        u = targ.u.cpu().numpy()
+        g = targ.ug.cpu().numpy() if grads else None
+    else:
+        u, g = targ.u, (targ.ug if grads else None)
+    return u, g
+
+
+@pytest.mark.parametrize("core", CORES)
+@pytest.mark.parametrize("kind", ["particles", "fieldpoints"])
+def test_plain_matches_reference_fp32_semantics(cuda, core, kind):
+    x, s, r = W.gaussian_cloud(3000, seed=101, pos_std=0.25)
+    tx, _, tr = W.gaussian_cloud(2100, seed=102, pos_std=0.25)
+    tr = tr if kind == "particles" else None
+    uo, go = O.points_affect_points(x, r, s, tx, tr, True, core, 1)
+    u, g = gpu_eval(x, s, r, tx, tr, True, core, "plain")
+    eu, eg = rel_err(u, uo), rel_err(g, go)
+    assert eu[0] <= 1e-5 and eg[0] <= 1e-5, (eu, eg)
+    uo, _ = O.points_affect_points(x, r, s, tx, tr, False, core, 1)
+    u, _ = gpu_eval(x, s, r, tx, tr, False, core, "plain")
+    assert rel_err(u, uo)[0] <= 1e-5
+
+
+@pytest.mark.parametrize("core", CORES)
+def test_golden_vectors(cuda, core):
+    d = np.load(os.path.join(GOLD, "ptpt_%s.npz" % core))
+    for tr, tag in ((d["tr"], "pg"), (None, "fg")):
+        u, g = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx"], tr, True, core, "plain")
+        assert rel_err(u, d[tag + "_u_p0"])[0] <= 1e-5
+        assert rel_err(g, d[tag + "_g_p0"])[0] <= 1e-5
+        u, g = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx"], tr, True, core, "fp64", dtype=np.float64)
+        assert rel_err(u, d[tag + "_u_p2"])[0] <= 1e-11
+        assert rel_err(g, d[tag + "_g_p2"])[0] <= 1e-11
+    u, _ = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx"], d["tr"], False, core, "plain")
+    assert rel_err(u, d["pv_u_p0"])[0] <= 1e-5
+
+
+@pytest.mark.parametrize("core", CORES)
+def test_compensated_and_fp64_vs_fp64_oracle(cuda, core):
+    x, s, r = W.gaussian_cloud(6000, seed=103, pos_std=0.3)
+    tx = x[:, :1500].copy()
+    tr = r[:1500].copy()
+    uo, go = O.points_affect_points(x, r, s, tx, tr, True, core, 2)
+    u, g = gpu_eval(x, s, r, tx, tr, True, core, "compensated")
+    eu, eg = rel_err(u, uo), rel_err(g, go)
+    print("compensated", core, eu, eg)
+    assert eu[0] <= 2e-6 and eg[0] <= 2e-6, (eu, eg)
+    # the float-input FP64 mode rounds only the final sums to float
+    u, g = gpu_eval(x, s, r, tx, tr, True, core, "fp64")
+    assert rel_err(u, uo)[0] <= 2e-7 and rel_err(g, go)[0] <= 2e-7
+    # the double entry point
+    u, g = gpu_eval(x, s, r, tx, tr, True, core, "fp64", dtype=np.float64)
+    assert rel_err(u, uo)[0] <= 1e-11 and rel_err(g, go)[0] <= 1e-11
+
+
+def test_host_and_device_memory_give_identical_bits(cuda):
+    x, s, r = W.gaussian_cloud(1000, seed=104)
+    tx, _, tr = W.gaussian_cloud(777, seed=105)
+    for prec in ("plain", "compensated"):
+        a = gpu_eval(x, s, r, tx, tr, True, "rm", prec, on_device=True)
+        b = gpu_eval(x, s, r, tx, tr, True, "rm", prec, on_device=False)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_accumulates_into_existing_values(cuda):
+    x, s, r = W.gaussian_cloud(500, seed=106)
+    tx, _, tr = W.gaussian_cloud(300, seed=107)
+    u0 = np.random.default_rng(0).normal(size=(3, 300)).astype(np.float32)
+    g0 = np.random.default_rng(1).normal(size=(9, 300)).astype(np.float32)
+    a = gpu_eval(x, s, r, tx, tr, True, "wl", "plain")
+    b = gpu_eval(x, s, r, tx, tr, True, "wl", "plain", u0=u0, g0=g0)
+    assert np.allclose(b[0], a[0] + u0, rtol=1e-6, atol=1e-6 * np.abs(a[0]).max())
+    assert np.allclose(b[1], a[1] + g0, rtol=1e-6, atol=1e-6 * np.abs(a[1]).max())
+
+
+@pytest.mark.parametrize("ns,nt", [(1, 1), (1, 300), (129, 1), (127, 129), (255, 257), (4097, 33)])
+def test_ragged_sizes(cuda, ns, nt):
+    x, s, r = W.gaussian_cloud(ns, seed=108 + ns)
+    tx, _, tr = W.gaussian_cloud(nt, seed=109 + nt)
+    for core in ("rm", "gauss"):
+        uo, go = O.points_affect_points(x, r, s, tx, tr, True, core, 1)
+        u, g = gpu_eval(x, s, r, tx, tr, True, core, "plain")
+        assert rel_err(u, uo)[0] <= 1e-5 and rel_err(g, go)[0] <= 1e-5
+
+
+def test_empty_inputs_are_noops(cuda):
+    x, s, r = W.gaussian_cloud(10, seed=110)
+    e = np.zeros((3, 0), np.float32)
+    u, g = gpu_eval(e, e, np.zeros(0, np.float32), x, r, True, "rm", "plain")
+    assert np.all(u == 0) and np.all(g == 0)
+    u, g = gpu_eval(x, s, r, e, np.zeros(0, np.float32), True, "rm", "plain")
+    assert u.shape == (3, 0)
+
+
+def test_self_interaction_same_arrays(cuda):
+    import torch
+    x, s, r = W.vortex_ring(2048, seed=111)
+    X, S, R = _dev(x), _dev(s), _dev(r)
+    p = Points(X, S, R)
+    points_affect_points(p, p, ResultsType(), ExecEnv("rm", "plain"))
+    q = Points(X.clone(), None, R.clone())
+    points_affect_points(Points(X, S, R), q, ResultsType(), ExecEnv("rm", "plain"))
+    torch.cuda.synchronize()
+    assert torch.equal(p.u, q.u) and torch.equal(p.ug, q.ug)
+
+
+def test_linearity_in_strength_at_full_ring_size(cuda):
+    # scaling every strength by 2 scales every sum by exactly 2 (all products scale by a power of 2)
+    import torch
+    x, s, r = W.vortex_ring(16384)
+    a = gpu_eval(x, s, r, x, r, True, "rm", "plain")
+    b = gpu_eval(x, 2 * s, r, x, r, True, "rm", "plain")
+    assert np.array_equal(2 * a[0], b[0]) and np.array_equal(2 * a[1], b[1])
+    # and agrees with the reference semantics on a subset of targets
+    idx = np.arange(0, 16384, 64)
+    uo, go = O.points_affect_points(x, r, s, x[:, idx], r[idx], True, "rm", 1)
+    assert rel_err(a[0][:, idx], uo)[0] <= 1e-5 and rel_err(a[1][:, idx], go)[0] <= 1e-5
+
+
+def test_invalid_arguments_report_status(cuda):
+    lib = L.lib()
+    st = lib.o3g_points_affect_points(9, 0, 1, 1, *([None] * 7), 1, *([None] * 4), *([None] * 3), None, None)
+    assert st == 1
+    assert lib.o3g_last_error().decode()
