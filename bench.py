@@ -163,7 +163,7 @@ def run_ours(args):
     import omega3d_gb300 as G
     from omega3d_gb300 import _lib as L
     from omega3d_gb300 import workloads as W
-    from omega3d_gb300.metrics import rel_err
+    from omega3d_gb300.metrics import linf_err, rel_err
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -187,16 +187,16 @@ def run_ours(args):
     pairs = float(args.n) * args.n
     ref_flops = pairs * fl_pair + 12.0 * args.n
 
-    def one(prec, p=None):
+    def one(prec, p=None, core=None):
         p = p or G.Points(X, S, R)
         p.zero_vels()
-        G.points_affect_points(p, p, G.ResultsType(), G.ExecEnv(args.core, prec))
+        G.points_affect_points(p, p, G.ResultsType(), G.ExecEnv(core or args.core, prec))
         return p
 
-    def timed(prec, steps, warmup):
+    def timed(prec, steps, warmup, core=None):
         p = G.Points(X, S, R)
         for _ in range(warmup):
-            one(prec, p)
+            one(prec, p, core)
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
@@ -208,7 +208,7 @@ def run_ours(args):
             flush.fill_(1)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            one(prec, p)
+            one(prec, p, core)
             e1.record(stream)
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
@@ -225,6 +225,14 @@ def run_ours(args):
     clocks.start()
     pc, comp_ms, comp_kms, comp_wall, comp_launches = timed("compensated", args.steps, args.warmup)
     pp, plain_ms, plain_kms, _, _ = timed("plain", args.steps, args.warmup)
+    # the Rosenhead-Moore core (no distance branches) on the same cloud, for the FP32 roofline
+    rm = {}
+    for prec in ("plain", "compensated"):
+        _, rms, rkms, _, _ = timed(prec, args.steps, args.warmup, core="rm")
+        fl_rm = lib.o3g_flops_per_pair(L.CORES["rm"], 1, 1)
+        kms = statistics.median(rkms)
+        rm[prec] = {"value": pairs / (statistics.median(rms) * 1e-3), "unit": UNIT, "kernel_ms": kms,
+                    "roofline_frac": (pairs * fl_rm + 12.0 * args.n) / (kms * 1e-3) / 1e12 / fp32_peak}
     clk = clocks.stop()
 
     # e2e through the C-ABI with pinned host buffers: H2D + sums + D2H every step
@@ -267,7 +275,9 @@ def run_ours(args):
         for name, p in (("compensated", pc), ("plain", pp)):
             eu = rel_err(p.u.cpu().numpy()[:, subn], u64)
             eg = rel_err(p.ug.cpu().numpy()[:, subn], g64)
-            errs[name] = {"u_max": eu[0], "u_rms": eu[1], "grad_max": eg[0], "grad_rms": eg[1]}
+            errs[name] = {"u_max": eu[0], "u_rms": eu[1], "grad_max": eg[0], "grad_rms": eg[1],
+                          "u_linf": linf_err(p.u.cpu().numpy()[:, subn], u64),
+                          "grad_linf": linf_err(p.ug.cpu().numpy()[:, subn], g64)}
         fp64 = {"value": fp64_rate, "unit": UNIT, "targets": nsub, "errors_vs_fp64": errs}
 
     comp_step = statistics.median(comp_ms)
@@ -316,6 +326,7 @@ def run_ours(args):
                       "roofline_frac": ref_flops / (plain_k * 1e-3) / 1e12 / fp32_peak,
                       "error_vs_fp64": fp64["errors_vs_fp64"]["plain"] if fp64 else None},
             "compensated_over_plain": plain_step / comp_step,
+            "rm_core_same_cloud": rm,
             "fp64_same_gpu": fp64 and {"value": fp64["value"], "unit": UNIT, "targets": fp64["targets"],
                                        "compensated_speedup": local_rate / fp64["value"]},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_sample},

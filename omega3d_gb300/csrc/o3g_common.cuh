@@ -133,6 +133,8 @@ __device__ __forceinline__ float dev_erf(float x) { return erff(x); }
 __device__ __forceinline__ double dev_erf(double x) { return erf(x); }
 __device__ __forceinline__ float dev_exp(float x) { return expf(x); }
 __device__ __forceinline__ double dev_exp(double x) { return exp(x); }
+__device__ __forceinline__ float dev_expm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double dev_expm1(double x) { return expm1(x); }
 __device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 
@@ -227,9 +229,10 @@ __device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
       r3 = corefac;
       bbb = T(-1.5) * dist * r3 * r3;
     } else {
-      const T e = dev_exp(-reld3);
-      r3 = ood3 * (T(1.0) - e);
-      bbb = T(3.0) * (corefac * e - r3) / distsq;
+      // 1 - exp(-x) through expm1: the reference's float 1.0f - exp(-x) loses ~eps/x here
+      const T em1 = dev_expm1(-reld3);
+      r3 = ood3 * (-em1);
+      bbb = T(3.0) * (corefac * (em1 + T(1.0)) - r3) / distsq;
     }
   } else if (C == CORE_V2) {
     // CoreFunc.h:318-330: denom = d^4 + sr^4 + tr^4; r3 = denom^-0.75; bbb = -3 r3 denom^-0.5
@@ -265,7 +268,7 @@ __device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst) {
     const T reld3 = corefac / ood3;
     if (reld3 > T(16.0)) return ood3;
     if (reld3 < T(0.001)) return corefac;
-    return ood3 * (T(1.0) - dev_exp(-reld3));
+    return ood3 * (-dev_expm1(-reld3));
   } else if (C == CORE_V2) {
     const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
     const T rs = rsq<ACC>(fma(distsq, distsq, cst));

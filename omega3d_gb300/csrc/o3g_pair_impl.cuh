@@ -4,48 +4,68 @@
 //   spos[ns_pad] : float4 (x, y, z, core parameter of sr)      16 B / source
 //   sstr[ns_pad] : float4 (sx, sy, sz, sr)                     16 B / source
 //   tpos[nt_pad] : float4 (x, y, z, core parameter of tr or 0) 16 B / target
-// Padding sources sit at the origin with zero strength and core parameter 1, so they
-// add exactly zero (the same trick as the reference's Vc padding, Influence.h:232-238).
+//   (double4 for the FP64 mode).  Padding sources sit at the origin with zero strength
+//   and core parameter 1, so they add exactly zero (as the reference's Vc padding,
+//   Influence.h:232-238).
 //
 // Kernel k_pair: a block of kBlock threads owns kBlock*TPT targets (TPT per thread,
-// strided by kBlock so loads/stores coalesce) and sweeps a contiguous range of
+// strided by kBlock so loads and stores coalesce) and sweeps a contiguous range of
 // source tiles.  Each tile of kBlock sources is staged in shared memory and read by
-// every thread as a broadcast.  When the targets alone cannot fill the GPU, the
-// source range is split across blockIdx.y and the per-split partial sums go to
-// scratch, reduced afterwards in a fixed order (deterministic, k_reduce).
+// every thread as a broadcast.  When the targets alone cannot fill the GPU, the source
+// range is split across blockIdx.y and the per-split partial sums go to scratch,
+// reduced afterwards in a fixed order (deterministic, k_reduce).
+//
+// Cores with distance branches (Gaussian, compact exponential) sweep Morton-ordered
+// sources and targets.  For every (target block, source tile) the bounding boxes decide
+// whether all of the tile's pairs lie beyond the core's far-field threshold; such tiles
+// run the branch-free singular loop (r3 = 1/d^3, bbb = -3/d^5), the others the full core.
+// The decision is uniform over the block, so warps never diverge on it.
 #pragma once
 
 #include "o3g_common.cuh"
+#include "o3g_sort.cuh"
 
 namespace o3g {
 
 constexpr int kBlock = 128;  // threads per block == sources per shared tile
 
 enum { MODE_PLAIN = 0, MODE_COMP = 1, MODE_FP64 = 2 };
+enum { CORE_SING = 5 };      // internal: singular far-field kernel (cst ignored)
 
 template <class T, class O> struct PairArgs {
   const V4<T>* spos;
   const V4<T>* sstr;
-  int ntiles;           // source tiles of kBlock sources
-  int tiles_per_split;  // tiles swept by one block
+  int ntiles;                // source tiles of kBlock sources
+  int tiles_per_split;       // tiles swept by one block
   const V4<T>* tpos;
-  int nt;               // real targets
-  int nt_pad;           // padded targets (multiple of kBlock*TPT)
-  T* partial;           // [nsplit][ncomp * (COMP ? 2 : 1)][nt_pad] or nullptr
-  OutPtrs<O> out;       // accumulated into when partial == nullptr
+  int nt;                    // real targets
+  int nt_pad;                // padded targets (multiple of kBlock*TPT)
+  T* partial;                // [nsplit][ncomp * (COMP ? 2 : 1)][nt_pad] or nullptr
+  OutPtrs<O> out;            // accumulated into when partial == nullptr
+  const uint32_t* tperm;     // sorted target k -> caller's index, or nullptr
+  const float4* tile_lo;     // per source tile: (min x, min y, min z, max core param)
+  const float4* tile_hi;     // per source tile: (max x, max y, max z, -)
 };
 
 // one pair, velocity + gradient.  a[0..2] velocity, a[3..11] gradient sums of
-// bbb * d (x) (d x s) in the reference order, a[12..14] = sum r3 * s (folded into the
+// bbb * d (x) (s x d) in the reference order, a[12..14] = sum r3 * s (folded into the
 // antisymmetric gradient terms by fold_grads, Kernels.h:184-192).
 template <int C, bool ACC, bool HAVE_TR, class T>
 __device__ __forceinline__ void pair_g(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a) {
   const T dx = t.x - s.x;
   const T dy = t.y - s.y;
   const T dz = t.z - s.z;
-  const T cst = HAVE_TR ? (s.w + t.w) : s.w;
   T r3, bbb;
-  core_g<C, ACC, T>(dx, dy, dz, cst, r3, bbb);
+  if (C == CORE_SING) {
+    const T r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    const T rs = rsq<ACC>(r2);
+    const T rs2 = rs * rs;
+    r3 = rs2 * rs;
+    bbb = T(-3.0) * r3 * rs2;
+  } else {
+    const T cst = HAVE_TR ? (s.w + t.w) : s.w;
+    core_g<C, ACC, T>(dx, dy, dz, cst, r3, bbb);
+  }
   T cx = dz * w.y - dy * w.z;
   T cy = dx * w.z - dz * w.x;
   T cz = dy * w.x - dx * w.y;
@@ -75,8 +95,14 @@ __device__ __forceinline__ void pair_v(const V4<T>& t, const V4<T>& s, const V4<
   const T dx = t.x - s.x;
   const T dy = t.y - s.y;
   const T dz = t.z - s.z;
-  const T cst = HAVE_TR ? (s.w + t.w) : s.w;
-  const T r3 = core_v<C, ACC, T>(dx, dy, dz, cst);
+  T r3;
+  if (C == CORE_SING) {
+    const T rs = rsq<ACC>(fma(dx, dx, fma(dy, dy, dz * dz)));
+    r3 = rs * rs * rs;
+  } else {
+    const T cst = HAVE_TR ? (s.w + t.w) : s.w;
+    r3 = core_v<C, ACC, T>(dx, dy, dz, cst);
+  }
   a[0] = fma(r3, dz * w.y - dy * w.z, a[0]);
   a[1] = fma(r3, dx * w.z - dz * w.x, a[1]);
   a[2] = fma(r3, dy * w.x - dx * w.y, a[2]);
@@ -94,54 +120,24 @@ __device__ __forceinline__ void fold_grads(T* a) {
   a[10] -= a[12];
 }
 
-// error-free transformation of a + b (Knuth two-sum): s + e == a + b exactly
+// error-free transformation of a + b (Knuth's two-sum): s + e == a + b exactly
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
 
-template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
-__global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
+// Sweep the staged tile (kBlock sources in shared memory) for TPT targets.  In the
+// compensated mode the plain partial of every FOLD sources is folded into (hi, lo).
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, int NA, int NC, int NH>
+__device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, const V4<T>* tp, T (*acc)[NA],
+                                           float (*hi)[NH], float (*lo)[NH]) {
   constexpr bool ACC = (MODE == MODE_COMP);
-  constexpr int NA = GRADS ? 15 : 3;   // accumulators during the sweep
-  constexpr int NC = GRADS ? 12 : 3;   // output components
-  __shared__ V4<T> sp[kBlock];
-  __shared__ V4<T> sw[kBlock];
-
-  const int tid = threadIdx.x;
-  const int split = blockIdx.y;
-  const int tbase = blockIdx.x * (kBlock * TPT) + tid;
-
-  V4<T> tp[TPT];
-#pragma unroll
-  for (int k = 0; k < TPT; ++k) tp[k] = a.tpos[tbase + k * kBlock];
-
-  T acc[TPT][NA];
-#pragma unroll
-  for (int k = 0; k < TPT; ++k)
-#pragma unroll
-    for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
-
-  // compensated mode: (hi, lo) running sums of the folded per-tile partials
-  float hi[ACC ? TPT : 1][ACC ? NC : 1];
-  float lo[ACC ? TPT : 1][ACC ? NC : 1];
-  if (ACC) {
-#pragma unroll
-    for (int k = 0; k < TPT; ++k)
-#pragma unroll
-      for (int c = 0; c < NC; ++c) { hi[k][c] = 0.f; lo[k][c] = 0.f; }
-  }
-
-  const int t_begin = split * a.tiles_per_split;
-  const int t_end = min(a.ntiles, t_begin + a.tiles_per_split);
-  for (int tile = t_begin; tile < t_end; ++tile) {
-    __syncthreads();
-    sp[tid] = a.spos[(size_t)tile * kBlock + tid];
-    sw[tid] = a.sstr[(size_t)tile * kBlock + tid];
-    __syncthreads();
+  constexpr int FOLD = ACC ? 16 : kBlock;
+#pragma unroll 1
+  for (int j0 = 0; j0 < kBlock; j0 += FOLD) {
 #pragma unroll 4
-    for (int j = 0; j < kBlock; ++j) {
+    for (int j = j0; j < j0 + FOLD; ++j) {
       const V4<T> s = sp[j];
       const V4<T> w = sw[j];
 #pragma unroll
@@ -157,7 +153,7 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           float s, e;
-          two_sum((float)hi[k][c], (float)acc[k][c], s, e);
+          two_sum(hi[k][c], (float)acc[k][c], s, e);
           hi[k][c] = s;
           lo[k][c] += e;
         }
@@ -165,6 +161,115 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
         for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
       }
     }
+  }
+}
+
+// far-field threshold on the squared distance, as a multiple of the pair's core parameter
+template <int C> struct FarRule {
+  __device__ static bool far(float, float) { return false; }
+};
+template <> struct FarRule<CORE_GAUSS> {
+  // q = d^2 / (sr^2 + tr^2) > qfar: the Gaussian core equals the singular kernel
+  __device__ static bool far(float d2min, float maxcst) { return d2min > GaussP<float>::qfar * maxcst; }
+};
+template <> struct FarRule<CORE_EXP> {
+  // reld3 = d^3 / (sr^3 + tr^3) > 16 (CoreFunc.h:121): exp_cond returns 1/d^3; the box
+  // test asks for 20 to stay clear of the boundary
+  __device__ static bool far(float d2min, float maxcst) { return d2min * sqrtf(d2min) > 20.0f * maxcst; }
+};
+
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
+__global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
+  constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr bool CLASSIFY = (C == CORE_GAUSS || C == CORE_EXP);
+  constexpr int NA = GRADS ? 15 : 3;   // accumulators during the sweep
+  constexpr int NC = GRADS ? 12 : 3;   // output components
+  constexpr int NH = ACC ? NC : 1;
+  __shared__ V4<T> sp[kBlock];
+  __shared__ V4<T> sw[kBlock];
+  __shared__ float sbox[kBlock / 32][7];
+
+  const int tid = threadIdx.x;
+  const int split = blockIdx.y;
+  const int tbase = blockIdx.x * (kBlock * TPT) + tid;
+
+  V4<T> tp[TPT];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) tp[k] = a.tpos[tbase + k * kBlock];
+
+  // bounding box and largest core parameter of this block's real targets
+  float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
+  if (CLASSIFY) {
+    float lo3[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi3[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mw = 0.f;
+#pragma unroll
+    for (int k = 0; k < TPT; ++k) {
+      if (tbase + k * kBlock < a.nt) {
+        const float v[3] = {(float)tp[k].x, (float)tp[k].y, (float)tp[k].z};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { lo3[d] = fminf(lo3[d], v[d]); hi3[d] = fmaxf(hi3[d], v[d]); }
+        mw = fmaxf(mw, (float)tp[k].w);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        lo3[d] = fminf(lo3[d], __shfl_xor_sync(0xffffffffu, lo3[d], o));
+        hi3[d] = fmaxf(hi3[d], __shfl_xor_sync(0xffffffffu, hi3[d], o));
+      }
+      mw = fmaxf(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+    }
+    if ((tid & 31) == 0) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) { sbox[tid >> 5][d] = lo3[d]; sbox[tid >> 5][3 + d] = hi3[d]; }
+      sbox[tid >> 5][6] = mw;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { blo[d] = 3.0e38f; bhi[d] = -3.0e38f; }
+#pragma unroll
+    for (int wq = 0; wq < kBlock / 32; ++wq) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) { blo[d] = fminf(blo[d], sbox[wq][d]); bhi[d] = fmaxf(bhi[d], sbox[wq][3 + d]); }
+      bw = fmaxf(bw, sbox[wq][6]);
+    }
+    // widen by a relative 1e-6 so rounding of the (float) box never makes it too small
+    const float pad = 1e-6f * (fabsf(blo[0]) + fabsf(blo[1]) + fabsf(blo[2]) + fabsf(bhi[0]) + fabsf(bhi[1]) +
+                               fabsf(bhi[2]));
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { blo[d] -= pad; bhi[d] += pad; }
+    bw *= 1.000001f;
+  }
+
+  T acc[TPT][NA];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k)
+#pragma unroll
+    for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
+  float hi[TPT][NH], lo[TPT][NH];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k)
+#pragma unroll
+    for (int c = 0; c < NH; ++c) { hi[k][c] = 0.f; lo[k][c] = 0.f; }
+
+  const int t_begin = split * a.tiles_per_split;
+  const int t_end = min(a.ntiles, t_begin + a.tiles_per_split);
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    __syncthreads();
+    sp[tid] = a.spos[(size_t)tile * kBlock + tid];
+    sw[tid] = a.sstr[(size_t)tile * kBlock + tid];
+    __syncthreads();
+    bool far = false;
+    if (CLASSIFY) {
+      const float4 slo = a.tile_lo[tile], shi = a.tile_hi[tile];
+      const float gx = fmaxf(0.f, fmaxf(slo.x - bhi[0], blo[0] - shi.x));
+      const float gy = fmaxf(0.f, fmaxf(slo.y - bhi[1], blo[1] - shi.y));
+      const float gz = fmaxf(0.f, fmaxf(slo.z - bhi[2], blo[2] - shi.z));
+      const float d2min = gx * gx + gy * gy + gz * gz;
+      far = FarRule<C>::far(d2min, HAVE_TR ? slo.w + bw : slo.w);
+    }
+    if (far) sweep_tile<CORE_SING, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
+    else     sweep_tile<C, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
   }
 
   // epilogue
@@ -186,9 +291,10 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
         for (int c = 0; c < NC; ++c) base[(size_t)c * a.nt_pad + idx] = acc[k][c];
       }
     } else if (idx < a.nt) {
+      const int o = a.tperm ? (int)a.tperm[idx] : idx;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        O* p = a.out.p[c] + idx;
+        O* p = a.out.p[c] + o;
         if (ACC) *p = (O)((double)*p + ((double)hi[k][c] + (double)lo[k][c]));
         else     *p = (O)((T)*p + acc[k][c]);
       }
@@ -198,11 +304,12 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
 
 // Sum the per-split partials in split order and add into the outputs.
 template <int NC, bool ACC, class T, class O>
-__global__ void k_reduce(const T* __restrict__ partial, int nsplit, int nt, int nt_pad, OutPtrs<O> out) {
+__global__ void k_reduce(const T* __restrict__ partial, int nsplit, int nt, int nt_pad, OutPtrs<O> out,
+                         const uint32_t* __restrict__ tperm) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (idx >= nt) return;
-  O* p = out.p[c] + idx;
+  O* p = out.p[c] + (tperm ? (int)tperm[idx] : idx);
   if (ACC) {
     double s = 0.0;
     for (int k = 0; k < nsplit; ++k) {
@@ -218,18 +325,20 @@ __global__ void k_reduce(const T* __restrict__ partial, int nsplit, int nt, int 
   }
 }
 
-// SoA -> packed float4/double4 sources
+// SoA -> packed float4/double4 sources, optionally gathered through perm
 template <int C, class I, class T>
 __global__ void k_pack_src(int n, int n_pad, const I* __restrict__ x, const I* __restrict__ y,
                            const I* __restrict__ z, const I* __restrict__ r, const I* __restrict__ sx,
-                           const I* __restrict__ sy, const I* __restrict__ sz, V4<T>* spos, V4<T>* sstr) {
+                           const I* __restrict__ sy, const I* __restrict__ sz, const uint32_t* __restrict__ perm,
+                           V4<T>* spos, V4<T>* sstr) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_pad) return;
   V4<T> p, w;
   if (i < n) {
-    const T ri = (T)r[i];
-    p.x = (T)x[i]; p.y = (T)y[i]; p.z = (T)z[i]; p.w = core_param<C, T>(ri);
-    w.x = (T)sx[i]; w.y = (T)sy[i]; w.z = (T)sz[i]; w.w = ri;
+    const int j = perm ? (int)perm[i] : i;
+    const T ri = (T)r[j];
+    p.x = (T)x[j]; p.y = (T)y[j]; p.z = (T)z[j]; p.w = core_param<C, T>(ri);
+    w.x = (T)sx[j]; w.y = (T)sy[j]; w.z = (T)sz[j]; w.w = ri;
   } else {
     p.x = T(0); p.y = T(0); p.z = T(0); p.w = T(1);
     w.x = T(0); w.y = T(0); w.z = T(0); w.w = T(0);
@@ -241,17 +350,57 @@ __global__ void k_pack_src(int n, int n_pad, const I* __restrict__ x, const I* _
 // SoA -> packed targets; r == nullptr means field points (core parameter 0)
 template <int C, class I, class T>
 __global__ void k_pack_tgt(int n, int n_pad, const I* __restrict__ x, const I* __restrict__ y,
-                           const I* __restrict__ z, const I* __restrict__ r, V4<T>* tpos) {
+                           const I* __restrict__ z, const I* __restrict__ r, const uint32_t* __restrict__ perm,
+                           V4<T>* tpos) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_pad) return;
   V4<T> p;
   if (i < n) {
-    p.x = (T)x[i]; p.y = (T)y[i]; p.z = (T)z[i];
-    p.w = r ? core_param<C, T>((T)r[i]) : T(0);
+    const int j = perm ? (int)perm[i] : i;
+    p.x = (T)x[j]; p.y = (T)y[j]; p.z = (T)z[j];
+    p.w = r ? core_param<C, T>((T)r[j]) : T(0);
   } else {
     p.x = T(0); p.y = T(0); p.z = T(0); p.w = T(0);
   }
   tpos[i] = p;
+}
+
+// per source tile: bounding box of its real sources and their largest core parameter,
+// widened by a relative 1e-6 so float rounding never shrinks it
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_tile_bounds(const V4<T>* __restrict__ spos, int ns, float4* tlo,
+                                                        float4* thi) {
+  __shared__ float red[kBlock / 32][7];
+  const int tile = blockIdx.x;
+  const int i = tile * kBlock + threadIdx.x;
+  float v[7];
+  if (i < ns) {
+    const V4<T> p = spos[i];
+    v[0] = (float)p.x; v[1] = (float)p.y; v[2] = (float)p.z;
+    v[3] = -(float)p.x; v[4] = -(float)p.y; v[5] = -(float)p.z;   // max via -min(-x)
+    v[6] = -(float)p.w;
+  } else {
+#pragma unroll
+    for (int d = 0; d < 7; ++d) v[d] = 3.0e38f;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int d = 0; d < 7; ++d) v[d] = fminf(v[d], __shfl_xor_sync(0xffffffffu, v[d], o));
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int d = 0; d < 7; ++d) red[threadIdx.x >> 5][d] = v[d];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m[7];
+    for (int d = 0; d < 7; ++d) {
+      m[d] = red[0][d];
+      for (int wq = 1; wq < kBlock / 32; ++wq) m[d] = fminf(m[d], red[wq][d]);
+    }
+    const float pad = 1e-6f * (fabsf(m[0]) + fabsf(m[1]) + fabsf(m[2]) + fabsf(m[3]) + fabsf(m[4]) + fabsf(m[5]));
+    tlo[tile] = make_float4(m[0] - pad, m[1] - pad, m[2] - pad, -m[6] * 1.000001f);
+    thi[tile] = make_float4(-m[3] + pad, -m[4] + pad, -m[5] + pad, 0.f);
+  }
 }
 
 // ------------------------------------------------------------------------------
@@ -286,16 +435,15 @@ inline void plan_pair(int ns, int nt, int tpt, int slots, PairPlan* p) {
   if (p->nsplit < 1) p->nsplit = 1;
 }
 
-// The pipeline for one (core, mode, grads, target kind): pack, sweep, reduce.
+// The pipeline for one (core, mode, grads, target kind): [sort], pack, sweep, reduce.
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class I, class O>
 int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I* sr,
                           const I* ssx, const I* ssy, const I* ssz,
                           int nt, const I* tx, const I* ty, const I* tz, const I* tr,
-                          OutPtrs<O> out, bool same, cudaStream_t st, Workspace* ws_unused,
-                          size_t* ws_bytes_needed, char* ws_base) {
-  (void)ws_unused;
+                          OutPtrs<O> out, bool same, cudaStream_t st, size_t* ws_bytes_needed, char* ws_base) {
   constexpr int NC = GRADS ? 12 : 3;
   constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr bool SORT = (C == CORE_GAUSS || C == CORE_EXP);
   DeviceFacts df;
   O3G_TRY(device_facts(&df));
   int nb = 0;
@@ -306,6 +454,13 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   size_t bytes = 2 * align_up((size_t)nsp * sizeof(V4<T>));
   if (!same) bytes += align_up((size_t)pl.nt_pad * sizeof(V4<T>));
   if (pl.nsplit > 1) bytes += align_up((size_t)pl.nsplit * NC * (ACC ? 2 : 1) * pl.nt_pad * sizeof(T));
+  size_t sort_bytes = 0;
+  if (SORT) {
+    bytes += align_up((size_t)ns * sizeof(uint32_t)) + 2 * align_up((size_t)pl.ntiles * sizeof(float4));
+    if (!same) bytes += align_up((size_t)nt * sizeof(uint32_t));
+    sort_bytes = morton_sort_bytes(ns > nt ? ns : nt);
+    bytes += sort_bytes;
+  }
   if (ws_bytes_needed) { *ws_bytes_needed = bytes; return O3G_OK; }
 
   Carve cv(ws_base);
@@ -313,17 +468,35 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   V4<T>* sstr = cv.take<V4<T>>(nsp);
   V4<T>* tpos = same ? spos : cv.take<V4<T>>(pl.nt_pad);
   T* partial = pl.nsplit > 1 ? cv.take<T>((size_t)pl.nsplit * NC * (ACC ? 2 : 1) * pl.nt_pad) : nullptr;
+  uint32_t* sperm = nullptr;
+  uint32_t* tperm = nullptr;
+  float4* tile_lo = nullptr;
+  float4* tile_hi = nullptr;
+  if (SORT) {
+    sperm = cv.take<uint32_t>(ns);
+    tperm = same ? sperm : cv.take<uint32_t>(nt);
+    tile_lo = cv.take<float4>(pl.ntiles);
+    tile_hi = cv.take<float4>(pl.ntiles);
+    char* sort_ws = cv.take<char>(sort_bytes);
+    O3G_TRY(morton_sort<I>(sx, sy, sz, ns, sperm, sort_ws, st));
+    if (!same) O3G_TRY(morton_sort<I>(tx, ty, tz, nt, tperm, sort_ws, st));
+  }
 
-  k_pack_src<C, I, T><<<(nsp + 255) / 256, 256, 0, st>>>(ns, nsp, sx, sy, sz, sr, ssx, ssy, ssz, spos, sstr);
+  k_pack_src<C, I, T><<<(nsp + 255) / 256, 256, 0, st>>>(ns, nsp, sx, sy, sz, sr, ssx, ssy, ssz, sperm, spos, sstr);
   note_launch();
   if (!same) {
-    k_pack_tgt<C, I, T><<<(pl.nt_pad + 255) / 256, 256, 0, st>>>(nt, pl.nt_pad, tx, ty, tz, tr, tpos);
+    k_pack_tgt<C, I, T><<<(pl.nt_pad + 255) / 256, 256, 0, st>>>(nt, pl.nt_pad, tx, ty, tz, tr, tperm, tpos);
+    note_launch();
+  }
+  if (SORT) {
+    k_tile_bounds<T><<<pl.ntiles, kBlock, 0, st>>>(spos, ns, tile_lo, tile_hi);
     note_launch();
   }
 
   PairArgs<T, O> a;
   a.spos = spos; a.sstr = sstr; a.ntiles = pl.ntiles; a.tiles_per_split = pl.tiles_per_split;
   a.tpos = tpos; a.nt = nt; a.nt_pad = pl.nt_pad; a.partial = partial; a.out = out;
+  a.tperm = tperm; a.tile_lo = tile_lo; a.tile_hi = tile_hi;
   dim3 grid(pl.tblocks, pl.nsplit);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
@@ -332,7 +505,7 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   tm.end(st);
   if (pl.nsplit > 1) {
     dim3 rg((nt + 255) / 256, NC);
-    k_reduce<NC, ACC, T, O><<<rg, 256, 0, st>>>(partial, pl.nsplit, nt, pl.nt_pad, out);
+    k_reduce<NC, ACC, T, O><<<rg, 256, 0, st>>>(partial, pl.nsplit, nt, pl.nt_pad, out, tperm);
     note_launch();
   }
   O3G_CUDA_TRY(cudaGetLastError());
@@ -357,48 +530,49 @@ int32_t ptpt_core_d(const PtPtCall& c, const double* sx, const double* sy, const
                     const double* ssx, const double* ssy, const double* ssz, const double* tx, const double* ty,
                     const double* tz, const double* tr, OutPtrs<double> out, size_t* need, char* ws);
 
-#define O3G_DEFINE_PTPT_CORE(CORE)                                                                          \
-  template <>                                                                                               \
-  int32_t ptpt_core_f<CORE>(const PtPtCall& c, const float* sx, const float* sy, const float* sz,           \
-                            const float* sr, const float* ssx, const float* ssy, const float* ssz,          \
-                            const float* tx, const float* ty, const float* tz, const float* tr,             \
-                            OutPtrs<float> out, size_t* need, char* ws) {                                   \
-    const bool htr = (tr != nullptr);                                                                       \
-    if (c.mode == MODE_PLAIN) {                                                                             \
-      if (c.grads) {                                                                                        \
-        if (htr) return run_points_points<CORE, MODE_PLAIN, true, true, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-        return run_points_points<CORE, MODE_PLAIN, true, false, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-      }                                                                                                     \
-      if (htr) return run_points_points<CORE, MODE_PLAIN, false, true, 4, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-      return run_points_points<CORE, MODE_PLAIN, false, false, 4, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-    }                                                                                                       \
-    if (c.mode == MODE_COMP) {                                                                              \
-      if (c.grads) {                                                                                        \
-        if (htr) return run_points_points<CORE, MODE_COMP, true, true, 1, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-        return run_points_points<CORE, MODE_COMP, true, false, 1, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-      }                                                                                                     \
-      if (htr) return run_points_points<CORE, MODE_COMP, false, true, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-      return run_points_points<CORE, MODE_COMP, false, false, 2, float>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-    }                                                                                                       \
-    if (c.grads) {                                                                                          \
-      if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-      return run_points_points<CORE, MODE_FP64, true, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-    }                                                                                                       \
-    if (htr) return run_points_points<CORE, MODE_FP64, false, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-    return run_points_points<CORE, MODE_FP64, false, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-  }                                                                                                         \
-  template <>                                                                                               \
-  int32_t ptpt_core_d<CORE>(const PtPtCall& c, const double* sx, const double* sy, const double* sz,        \
-                            const double* sr, const double* ssx, const double* ssy, const double* ssz,      \
-                            const double* tx, const double* ty, const double* tz, const double* tr,         \
-                            OutPtrs<double> out, size_t* need, char* ws) {                                  \
-    const bool htr = (tr != nullptr);                                                                       \
-    if (c.grads) {                                                                                          \
-      if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-      return run_points_points<CORE, MODE_FP64, true, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-    }                                                                                                       \
-    if (htr) return run_points_points<CORE, MODE_FP64, false, true, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
-    return run_points_points<CORE, MODE_FP64, false, false, 1, double>(c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, nullptr, need, ws); \
+#define O3G_PTPT_ARGS c.ns, sx, sy, sz, sr, ssx, ssy, ssz, c.nt, tx, ty, tz, tr, out, c.same, c.st, need, ws
+#define O3G_DEFINE_PTPT_CORE(CORE)                                                                           \
+  template <>                                                                                                \
+  int32_t ptpt_core_f<CORE>(const PtPtCall& c, const float* sx, const float* sy, const float* sz,            \
+                            const float* sr, const float* ssx, const float* ssy, const float* ssz,           \
+                            const float* tx, const float* ty, const float* tz, const float* tr,              \
+                            OutPtrs<float> out, size_t* need, char* ws) {                                    \
+    const bool htr = (tr != nullptr);                                                                        \
+    if (c.mode == MODE_PLAIN) {                                                                              \
+      if (c.grads) {                                                                                         \
+        if (htr) return run_points_points<CORE, MODE_PLAIN, true, true, 2, float>(O3G_PTPT_ARGS);            \
+        return run_points_points<CORE, MODE_PLAIN, true, false, 2, float>(O3G_PTPT_ARGS);                    \
+      }                                                                                                      \
+      if (htr) return run_points_points<CORE, MODE_PLAIN, false, true, 4, float>(O3G_PTPT_ARGS);             \
+      return run_points_points<CORE, MODE_PLAIN, false, false, 4, float>(O3G_PTPT_ARGS);                     \
+    }                                                                                                        \
+    if (c.mode == MODE_COMP) {                                                                               \
+      if (c.grads) {                                                                                         \
+        if (htr) return run_points_points<CORE, MODE_COMP, true, true, 1, float>(O3G_PTPT_ARGS);             \
+        return run_points_points<CORE, MODE_COMP, true, false, 1, float>(O3G_PTPT_ARGS);                     \
+      }                                                                                                      \
+      if (htr) return run_points_points<CORE, MODE_COMP, false, true, 2, float>(O3G_PTPT_ARGS);              \
+      return run_points_points<CORE, MODE_COMP, false, false, 2, float>(O3G_PTPT_ARGS);                      \
+    }                                                                                                        \
+    if (c.grads) {                                                                                           \
+      if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(O3G_PTPT_ARGS);              \
+      return run_points_points<CORE, MODE_FP64, true, false, 1, double>(O3G_PTPT_ARGS);                      \
+    }                                                                                                        \
+    if (htr) return run_points_points<CORE, MODE_FP64, false, true, 1, double>(O3G_PTPT_ARGS);               \
+    return run_points_points<CORE, MODE_FP64, false, false, 1, double>(O3G_PTPT_ARGS);                       \
+  }                                                                                                          \
+  template <>                                                                                                \
+  int32_t ptpt_core_d<CORE>(const PtPtCall& c, const double* sx, const double* sy, const double* sz,         \
+                            const double* sr, const double* ssx, const double* ssy, const double* ssz,       \
+                            const double* tx, const double* ty, const double* tz, const double* tr,          \
+                            OutPtrs<double> out, size_t* need, char* ws) {                                   \
+    const bool htr = (tr != nullptr);                                                                        \
+    if (c.grads) {                                                                                           \
+      if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(O3G_PTPT_ARGS);              \
+      return run_points_points<CORE, MODE_FP64, true, false, 1, double>(O3G_PTPT_ARGS);                      \
+    }                                                                                                        \
+    if (htr) return run_points_points<CORE, MODE_FP64, false, true, 1, double>(O3G_PTPT_ARGS);               \
+    return run_points_points<CORE, MODE_FP64, false, false, 1, double>(O3G_PTPT_ARGS);                       \
   }
 
 }  // namespace o3g

@@ -5,7 +5,11 @@ Tolerances (per-target relative error, metrics.rel_err, floor 1e-6 of the max):
     reference's non-Vc build, Simulation.h:44-46; oracle prec 1): max <= 1e-5, the
     FP32-summation-reordering tolerance of the drop-in path.
   * PLAIN vs the golden vectors of the reference's Vc-semantics build (prec 0): max <= 1e-5.
-  * COMPENSATED vs the FP64 oracle: max <= 2e-6.
+  * EXP core: the reference evaluates 1 - exp(-x) in float (CoreFunc.h:130), which
+    loses ~eps/x near the core; the GPU uses expm1, so its PLAIN result is compared
+    with the FP64 oracle at 1e-5 and with the reference semantics at 5e-5.
+  * COMPENSATED vs the FP64 oracle: L-infinity (metrics.linf_err) <= 1e-6 and
+    per-target max <= 1e-5 (FP32 rounding of single pair terms bounds the latter).
   * FP64 vs the FP64 oracle / golden: max <= 1e-11.
 """
 import ctypes
@@ -19,7 +23,7 @@ import oracle as O
 from omega3d_gb300 import ExecEnv, Points, ResultsType, points_affect_points
 from omega3d_gb300 import _lib as L
 from omega3d_gb300 import workloads as W
-from omega3d_gb300.metrics import rel_err
+from omega3d_gb300.metrics import linf_err, rel_err
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -55,27 +59,32 @@ def test_plain_matches_reference_fp32_semantics(cuda, core, kind):
     x, s, r = W.gaussian_cloud(3000, seed=101, pos_std=0.25)
     tx, _, tr = W.gaussian_cloud(2100, seed=102, pos_std=0.25)
     tr = tr if kind == "particles" else None
+    tol = 5e-5 if core == "exp" else 1e-5
     uo, go = O.points_affect_points(x, r, s, tx, tr, True, core, 1)
     u, g = gpu_eval(x, s, r, tx, tr, True, core, "plain")
     eu, eg = rel_err(u, uo), rel_err(g, go)
-    assert eu[0] <= 1e-5 and eg[0] <= 1e-5, (eu, eg)
+    assert eu[0] <= tol and eg[0] <= tol, (eu, eg)
+    if core == "exp":
+        u64, g64 = O.points_affect_points(x, r, s, tx, tr, True, core, 2)
+        assert rel_err(u, u64)[0] <= 1e-5 and rel_err(g, g64)[0] <= 1e-5
     uo, _ = O.points_affect_points(x, r, s, tx, tr, False, core, 1)
     u, _ = gpu_eval(x, s, r, tx, tr, False, core, "plain")
-    assert rel_err(u, uo)[0] <= 1e-5
+    assert rel_err(u, uo)[0] <= tol
 
 
 @pytest.mark.parametrize("core", CORES)
 def test_golden_vectors(cuda, core):
     d = np.load(os.path.join(GOLD, "ptpt_%s.npz" % core))
     for tr, tag in ((d["tr"], "pg"), (None, "fg")):
+        tol = 5e-5 if core == "exp" else 1e-5
         u, g = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx"], tr, True, core, "plain")
-        assert rel_err(u, d[tag + "_u_p0"])[0] <= 1e-5
-        assert rel_err(g, d[tag + "_g_p0"])[0] <= 1e-5
+        assert rel_err(u, d[tag + "_u_p0"])[0] <= tol
+        assert rel_err(g, d[tag + "_g_p0"])[0] <= tol
         u, g = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx"], tr, True, core, "fp64", dtype=np.float64)
         assert rel_err(u, d[tag + "_u_p2"])[0] <= 1e-11
         assert rel_err(g, d[tag + "_g_p2"])[0] <= 1e-11
     u, _ = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx"], d["tr"], False, core, "plain")
-    assert rel_err(u, d["pv_u_p0"])[0] <= 1e-5
+    assert rel_err(u, d["pv_u_p0"])[0] <= (5e-5 if core == "exp" else 1e-5)
 
 
 @pytest.mark.parametrize("core", CORES)
@@ -86,8 +95,10 @@ def test_compensated_and_fp64_vs_fp64_oracle(cuda, core):
     uo, go = O.points_affect_points(x, r, s, tx, tr, True, core, 2)
     u, g = gpu_eval(x, s, r, tx, tr, True, core, "compensated")
     eu, eg = rel_err(u, uo), rel_err(g, go)
-    print("compensated", core, eu, eg)
-    assert eu[0] <= 2e-6 and eg[0] <= 2e-6, (eu, eg)
+    lu, lg = linf_err(u, uo), linf_err(g, go)
+    print("compensated", core, eu, eg, lu, lg)
+    assert lu <= 1e-6 and lg <= 1e-6, (lu, lg)
+    assert eu[0] <= 1e-5 and eg[0] <= 1e-5, (eu, eg)
     # the float-input FP64 mode rounds only the final sums to float
     u, g = gpu_eval(x, s, r, tx, tr, True, core, "fp64")
     assert rel_err(u, uo)[0] <= 2e-7 and rel_err(g, go)[0] <= 2e-7
