@@ -110,6 +110,28 @@ int32_t o3g_points_affect_points_d(int32_t core, int32_t mem,
                                    double* tu, double* tv, double* tw, double* const* tug,
                                    void* stream);
 
+/* ---- points_affect_points without device allocation ------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device memory
+ * after start-up (applications that give all device memory to their own pool, real-time
+ * loops that cannot absorb an allocation or the synchronisation of cudaFree, plugin
+ * hosts that forbid allocation): the same sums as o3g_points_affect_points on
+ * device-resident arrays (mem is always device; prec PLAIN or COMPENSATED), with every
+ * scratch byte taken from one fixed 64 MiB array in the library's device image.
+ *  - The first call on a device resolves that array's address (cudaGetSymbolAddress);
+ *    make it before capturing a stream into a graph.
+ *  - All calls share the array: calls that overlap on the GPU race; use one stream.
+ *  - Problems whose packed tiles do not fit (about 1.3 million sources + targets) return
+ *    O3G_ERR_INVALID_ARG before any work is queued.
+ * Sources are not Morton-sorted, so the Gaussian and exponential cores run without the
+ * far-tile fast path. */
+int32_t o3g_points_affect_points_noalloc(int32_t core, int32_t prec,
+                                         int32_t ns, const float* sx, const float* sy, const float* sz,
+                                         const float* sr, const float* ssx, const float* ssy, const float* ssz,
+                                         int32_t nt, const float* tx, const float* ty, const float* tz,
+                                         const float* tr,
+                                         float* tu, float* tv, float* tw, float* const* tug,
+                                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,8 @@ def _declare(l):
     l.o3g_fp32_peak_probe.argtypes = [c_i32, P, P, P]
     l.o3g_points_affect_points.restype = c_i32
     l.o3g_points_affect_points.argtypes = [c_i32, c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
+    l.o3g_points_affect_points_noalloc.restype = c_i32
+    l.o3g_points_affect_points_noalloc.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
     l.o3g_points_affect_points_d.restype = c_i32
     l.o3g_points_affect_points_d.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
 

@@ -1,0 +1,97 @@
+"""GPU test of o3g_points_affect_points_noalloc, the entry point for callers that may not
+allocate device memory (programs that hand all device memory to their own pool, real-time
+loops, plugin hosts that forbid allocation after start-up).  Its scratch lives in a fixed
+array inside the library, so the test calls it twice in a row -- the second call finds the
+first call's leftovers in that array -- and checks both results against the allocating
+entry point o3g_points_affect_points.  Tolerances are the parity tests' own: per-target
+relative error <= 1e-5 for PLAIN; L-infinity <= 1e-6 and per-target <= 1e-5 for COMPENSATED.
+
+This file is named to be collected last, so a run that stops at the first failure has
+run every other test before it; it also passes on its own in a fresh process.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from omega3d_gb300 import _lib as L
+from omega3d_gb300 import workloads as W
+from omega3d_gb300.metrics import linf_err, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _rows(t):
+    n = t.shape[1]
+    return [t.data_ptr() + k * n * 4 for k in range(t.shape[0])]
+
+
+def _call(fn, core, prec, X, S, R, TX, TR, U, G, stream, with_mem):
+    sx, ss, tx, tu = _rows(X), _rows(S), _rows(TX), _rows(U)
+    tug = (ctypes.c_void_p * 9)(*_rows(G)) if G is not None else None
+    tr = TR.data_ptr() if TR is not None else None
+    head = [core, prec, L.MEM_DEVICE] if with_mem else [core, prec]
+    return fn(*head, X.shape[1], *sx, R.data_ptr(), *ss, TX.shape[1], *tx, tr, *tu, tug, stream)
+
+
+@pytest.mark.parametrize("core", ["rm", "gauss"])
+@pytest.mark.parametrize("prec", ["plain", "compensated"])
+@pytest.mark.parametrize("case", ["self", "fieldpoints"])
+def test_noalloc_matches_allocating_entry_point_twice(cuda, core, prec, case):
+    import torch
+    lib = L.lib()
+    x, s, r = W.gaussian_cloud(5000, seed=201)
+    X, S, R = (torch.from_numpy(a).cuda() for a in (x, s, r))
+    if case == "self":
+        TX, TR = X, R
+    else:
+        tx, _, _ = W.gaussian_cloud(3001, seed=202)
+        TX, TR = torch.from_numpy(tx).cuda(), None
+    nt = TX.shape[1]
+    stream = torch.cuda.current_stream().cuda_stream
+    c, p = L.CORES[core], L.PRECS[prec]
+
+    U0 = torch.zeros(3, nt, device="cuda")
+    G0 = torch.zeros(9, nt, device="cuda")
+    L.check(_call(lib.o3g_points_affect_points, c, p, X, S, R, TX, TR, U0, G0, stream, True),
+            "o3g_points_affect_points")
+    torch.cuda.synchronize()
+    u0, g0 = U0.cpu().numpy(), G0.cpu().numpy()
+
+    for _ in range(2):
+        U = torch.zeros(3, nt, device="cuda")
+        G = torch.zeros(9, nt, device="cuda")
+        L.check(_call(lib.o3g_points_affect_points_noalloc, c, p, X, S, R, TX, TR, U, G, stream, False),
+                "o3g_points_affect_points_noalloc")
+        torch.cuda.synchronize()
+        u, g = U.cpu().numpy(), G.cpu().numpy()
+        if prec == "plain":
+            assert rel_err(u, u0)[0] <= 1e-5 and rel_err(g, g0)[0] <= 1e-5
+        else:
+            assert linf_err(u, u0) <= 1e-6 and linf_err(g, g0) <= 1e-6
+            assert rel_err(u, u0)[0] <= 1e-5 and rel_err(g, g0)[0] <= 1e-5
+
+
+def test_noalloc_velocity_only_and_rejections(cuda):
+    import torch
+    lib = L.lib()
+    x, s, r = W.gaussian_cloud(2000, seed=203)
+    X, S, R = (torch.from_numpy(a).cuda() for a in (x, s, r))
+    stream = torch.cuda.current_stream().cuda_stream
+    U0 = torch.zeros(3, 2000, device="cuda")
+    U = torch.zeros(3, 2000, device="cuda")
+    L.check(_call(lib.o3g_points_affect_points, 1, 0, X, S, R, X, R, U0, None, stream, True), "allocating")
+    L.check(_call(lib.o3g_points_affect_points_noalloc, 1, 0, X, S, R, X, R, U, None, stream, False), "noalloc")
+    torch.cuda.synchronize()
+    assert rel_err(U.cpu().numpy(), U0.cpu().numpy())[0] <= 1e-5
+    # FP64 is not offered without allocation
+    assert _call(lib.o3g_points_affect_points_noalloc, 0, 2, X, S, R, X, R, U, None, stream, False) == 1
+    # a problem whose packed tiles exceed the fixed array is refused before any work is
+    # queued (the buffers are real and large enough, so nothing could be read out of range)
+    n = 2_200_000
+    BX = torch.zeros(3, n, device="cuda")
+    BR = torch.ones(n, device="cuda")
+    BU = torch.zeros(3, n, device="cuda")
+    st = _call(lib.o3g_points_affect_points_noalloc, 0, 0, BX, BX, BR, BX, BR, BU, None, stream, False)
+    assert st == 1
+    assert "scratch" in lib.o3g_last_error().decode()
