@@ -110,6 +110,72 @@ int32_t o3g_points_affect_points_d(int32_t core, int32_t mem,
                                    double* tu, double* tv, double* tw, double* const* tug,
                                    void* stream);
 
+/* ---- surfaces ---------------------------------------------------------------------
+ * A triangulated surface in the reference's Surfaces<S> layout (Surfaces.h:1463-1489):
+ * node positions, three node indices per panel (Int = uint32_t, Omega3D.h:26), panel
+ * areas and the per-panel basis x1 (edge 0->1), x2 (in-plane, toward node 2) and normal. */
+typedef struct {
+  int32_t nn;
+  const float *x, *y, *z;
+  int32_t np;
+  const uint32_t* idx;
+  const float* area;
+  const float *x1x, *x1y, *x1z;
+  const float *x2x, *x2y, *x2z;
+  const float *nx, *ny, *nz;
+} o3g_surface_t;
+
+/* Node/panel counts of an icosahedral sphere refined `levels` times: 10*4^L+2, 20*4^L. */
+int32_t o3g_ovoid_size(int32_t levels, int32_t* num_nodes, int32_t* num_panels);
+/* generate_ovoid, GeomHelper.cpp:41-91 with igl::upsample numbering
+ * (lib/igl/upsample.cpp:17-105): icosahedron of radius 0.5 refined `levels` times,
+ * re-projected to r = 0.5 after each level, then scaled by (rx, ry, rz).  Host arrays. */
+int32_t o3g_generate_ovoid(int32_t levels, float rx, float ry, float rz, float* x, float* y, float* z,
+                           uint32_t* idx);
+/* Surfaces::compute_bases, Surfaces.h:776-816 (host arrays). */
+int32_t o3g_compute_bases(int32_t nn, const float* x, const float* y, const float* z, int32_t np,
+                          const uint32_t* idx, float* x1x, float* x1y, float* x1z, float* x2x, float* x2y,
+                          float* x2z, float* nx, float* ny, float* nz, float* area);
+/* Surfaces::vortex_sheet_to_panel_strength, Surfaces.h:309-335: ts = (ps0 x1 + ps1 x2) area. */
+int32_t o3g_sheet_to_panel_strength(int32_t np, const float* ps0, const float* ps1, const float* x1x,
+                                    const float* x1y, const float* x1z, const float* x2x, const float* x2y,
+                                    const float* x2z, const float* area, float* tsx, float* tsy, float* tsz);
+
+/* ---- panels_affect_points ----------------------------------------------------------
+ * Replaces panels_affect_points<float,A>, Influence.h:557-1099 (rkernel_2vs_0pg / _0p,
+ * Kernels.h:1028-1211): velocity (+ gradient when tug != NULL) at nt points induced by np
+ * flat vortex(+source) panels, adaptively subdivided down to maxlev levels (the reference
+ * uses RECURSIVE_LEVELS = 3, Influence.h:23; accepted 0..6).  ts = absolute panel vortex
+ * strengths (Surfaces::get_str); sss = source sheet strengths or NULL.  The targets' core
+ * radii are not used (Influence.h:872-873).  Accumulates (+=). */
+int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev,
+                                 int32_t nn, const float* nx, const float* ny, const float* nz,
+                                 int32_t np, const uint32_t* idx, const float* area,
+                                 const float* tsx, const float* tsy, const float* tsz, const float* sss,
+                                 int32_t nt, const float* tx, const float* ty, const float* tz,
+                                 float* tu, float* tv, float* tw, float* const* tug, void* stream);
+
+/* ---- points_affect_panels ----------------------------------------------------------
+ * Replaces points_affect_panels<float,A>, Influence.h:1107-1221: panel-averaged velocity
+ * induced by ns vortex particles on np panels (the BEM right-hand side), computed like the
+ * reference by subdividing the target panel as a source carrying the particle's strength
+ * and SUBTRACTING the result (Influence.h:1209-1212).  Particle core radii are not used. */
+int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev,
+                                 int32_t ns, const float* sx, const float* sy, const float* sz,
+                                 const float* ssx, const float* ssy, const float* ssz,
+                                 int32_t nn, const float* nx, const float* ny, const float* nz,
+                                 int32_t np, const uint32_t* idx, const float* area,
+                                 float* pu, float* pv, float* pw, void* stream);
+
+/* ---- panels_on_panels_coeff ----------------------------------------------------------
+ * Replaces panels_on_panels_coeff<float>, Coefficients.h:169-447: the (targ->np*nunk) x
+ * (src->np*nunk) influence block, column-major with leading dimension ld, into `coeffs`
+ * (device memory; all surface arrays device memory).  nunk 2 = tangential vortex sheet
+ * unknowns, 3 = plus the source sheet (Surfaces.h:71,261).  is_self writes the
+ * self-influence diagonal (Coefficients.h:414-436).  maxlev 0..4 (reference: 3). */
+int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int32_t is_self, const o3g_surface_t* src,
+                                   const o3g_surface_t* targ, float* coeffs, int64_t ld, void* stream);
+
 /* ---- points_affect_points without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory
  * after start-up (applications that give all device memory to their own pool, real-time

@@ -41,6 +41,15 @@ class O3GError(RuntimeError):
         super().__init__(msg)
 
 
+class Surface(ctypes.Structure):
+    """o3g_surface_t (include/o3dgpu.h)."""
+    _fields_ = [("nn", ctypes.c_int32), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("np", ctypes.c_int32), ("idx", ctypes.c_void_p), ("area", ctypes.c_void_p),
+                ("x1x", ctypes.c_void_p), ("x1y", ctypes.c_void_p), ("x1z", ctypes.c_void_p),
+                ("x2x", ctypes.c_void_p), ("x2y", ctypes.c_void_p), ("x2z", ctypes.c_void_p),
+                ("nx", ctypes.c_void_p), ("ny", ctypes.c_void_p), ("nz", ctypes.c_void_p)]
+
+
 def _declare(l):
     P = c_vp
     l.o3g_status_string.restype = ctypes.c_char_p
@@ -62,6 +71,21 @@ def _declare(l):
     l.o3g_fp32_peak_probe.argtypes = [c_i32, P, P, P]
     l.o3g_points_affect_points.restype = c_i32
     l.o3g_points_affect_points.argtypes = [c_i32, c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
+    l.o3g_ovoid_size.restype = c_i32
+    l.o3g_ovoid_size.argtypes = [c_i32, P, P]
+    l.o3g_generate_ovoid.restype = c_i32
+    l.o3g_generate_ovoid.argtypes = [c_i32, c_f, c_f, c_f, P, P, P, P]
+    l.o3g_compute_bases.restype = c_i32
+    l.o3g_compute_bases.argtypes = [c_i32, P, P, P, c_i32, P] + [P] * 10
+    l.o3g_sheet_to_panel_strength.restype = c_i32
+    l.o3g_sheet_to_panel_strength.argtypes = [c_i32] + [P] * 12
+    l.o3g_panels_affect_points.restype = c_i32
+    l.o3g_panels_affect_points.argtypes = [c_i32, c_i32, c_i32, P, P, P, c_i32, P, P, P, P, P, P, c_i32, P, P, P,
+                                           P, P, P, P, P]
+    l.o3g_points_affect_panels.restype = c_i32
+    l.o3g_points_affect_panels.argtypes = [c_i32, c_i32, c_i32] + [P] * 6 + [c_i32, P, P, P, c_i32, P, P, P, P, P, P]
+    l.o3g_panels_on_panels_coeff.restype = c_i32
+    l.o3g_panels_on_panels_coeff.argtypes = [c_i32, c_i32, c_i32, P, P, P, ctypes.c_int64, P]
     l.o3g_points_affect_points_noalloc.restype = c_i32
     l.o3g_points_affect_points_noalloc.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
     l.o3g_points_affect_points_d.restype = c_i32

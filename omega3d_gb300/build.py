@@ -17,8 +17,10 @@ LIB = os.path.join(HERE, "libo3dgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no floating-point contraction, so the host-side geometry arithmetic (sphere,
+# bases, areas) rounds exactly like the reference on both x86-64 and aarch64
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-O2", "-I", INCLUDE]
+           "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE]
 LINK_LIBS = ["-lcublas", "-lcudart"]
 
 
@@ -51,9 +53,16 @@ def _compile(src, verbose_ptxas=False):
 def build(force=False, verbose_ptxas=False, jobs=None):
     """Compile every CUDA/C++ source and link libo3dgpu.so; returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join([nvcc()] + ARCH + NVFLAGS + LINK_LIBS)
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        force = True
     if force:
         for f in os.listdir(BUILD):
-            os.remove(os.path.join(BUILD, f))
+            if f.endswith(".o"):
+                os.remove(os.path.join(BUILD, f))
+    with open(stamp, "w") as fh:
+        fh.write(flags)
     srcs = sources()
     jobs = jobs or min(len(srcs), max(1, os.cpu_count() or 1))
     logs = []

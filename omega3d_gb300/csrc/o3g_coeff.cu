@@ -1,0 +1,276 @@
+// o3g_coeff.cu -- BEM influence-matrix block: panels_on_panels_coeff (Coefficients.h:169-447).
+//
+// Column (j*nunk + k) of the block holds the velocity induced by unit strength k of source
+// panel j (k = 0: vortex sheet along x1, 1: along x2, 2: source sheet when nunk == 3),
+// projected on target panel i's x1, x2 (and normal when nunk == 3) at rows i*nunk + l
+// (Coefficients.h:221,283-289).  The block is written column-major with leading dimension
+// `ld`, so it can be written straight into the full BEM matrix.  Self-influence entries of
+// a block of a surface on itself are [0, 2pi; -2pi, 0] (+2pi source-source,
+// Coefficients.h:414-436) and everything is scaled by 1/(4pi) (:443-447).
+//
+// Each (target i, source j) pair is one traversal of rkernel_2vs_2p (Kernels.h:1217-1315):
+// the two centroids are compared against 4*(sqrt(sa)+sqrt(ta)) with the reference's
+// operation order (no FMA) and, when too close, both panels split into 4 children (16
+// child pairs, strength/16) down to maxlev.  The kernel is linear in the source strength,
+// so the 2 or 3 unit strengths share one traversal: each leaf computes r3 and d once.
+#include "o3g_common.cuh"
+
+namespace o3g {
+
+constexpr int kCB = 128;                 // target panels per block == source panels per tile
+constexpr int kCoeffMaxLev = 4;
+constexpr int kCStack = 15 * kCoeffMaxLev + 1;
+
+struct SrcRec {
+  float4 c;   // centroid, sqrt(area)
+  float4 s1;  // x1 * area, area
+  float4 s2;  // x2 * area, -
+};
+struct TriG { float x0, y0, z0, x1, y1, z1, x2, y2, z2; };
+
+__device__ __forceinline__ void cen(const TriG& t, float& cx, float& cy, float& cz) {
+  cx = __fdiv_rn(__fadd_rn(__fadd_rn(t.x0, t.x1), t.x2), 3.0f);
+  cy = __fdiv_rn(__fadd_rn(__fadd_rn(t.y0, t.y1), t.y2), 3.0f);
+  cz = __fdiv_rn(__fadd_rn(__fadd_rn(t.z0, t.z1), t.z2), 3.0f);
+}
+__device__ __forceinline__ float dist_rn3(float ax, float ay, float az, float bx, float by, float bz) {
+  const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+}
+
+// singular leaf at target point t from a source point c with vortex strengths s1, s2 and
+// source strength q (kernel_0vs_0p with sr = 0, Kernels.h:115-133); u[k] += r3 (s_k x d),
+// u[2] += r3 q d
+template <int NUNK>
+__device__ __forceinline__ void leaf3(float tx, float ty, float tz, float cx, float cy, float cz, float s1x, float s1y,
+                                      float s1z, float s2x, float s2y, float s2z, float q, float (*u)[3]) {
+  const float dx = tx - cx, dy = ty - cy, dz = tz - cz;
+  const float rs = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+  const float r3 = rs * rs * rs;
+  u[0][0] = fmaf(r3, dz * s1y - dy * s1z, u[0][0]);
+  u[0][1] = fmaf(r3, dx * s1z - dz * s1x, u[0][1]);
+  u[0][2] = fmaf(r3, dy * s1x - dx * s1y, u[0][2]);
+  u[1][0] = fmaf(r3, dz * s2y - dy * s2z, u[1][0]);
+  u[1][1] = fmaf(r3, dx * s2z - dz * s2x, u[1][1]);
+  u[1][2] = fmaf(r3, dy * s2x - dx * s2y, u[1][2]);
+  if (NUNK == 3) {
+    const float rq = r3 * q;
+    u[2][0] = fmaf(rq, dx, u[2][0]);
+    u[2][1] = fmaf(rq, dy, u[2][1]);
+    u[2][2] = fmaf(rq, dz, u[2][2]);
+  }
+}
+
+// child c (0..3) of triangle p: corner/midpoint list {v0, m01, v1, m02, m12, v2}, children
+// {0,1,3},{1,2,4},{1,4,3},{3,4,5} (Kernels.h:1292)
+__device__ __forceinline__ TriG child(const TriG& p, int c) {
+  const float m01x = 0.5f * (p.x0 + p.x1), m01y = 0.5f * (p.y0 + p.y1), m01z = 0.5f * (p.z0 + p.z1);
+  const float m02x = 0.5f * (p.x0 + p.x2), m02y = 0.5f * (p.y0 + p.y2), m02z = 0.5f * (p.z0 + p.z2);
+  const float m12x = 0.5f * (p.x1 + p.x2), m12y = 0.5f * (p.y1 + p.y2), m12z = 0.5f * (p.z1 + p.z2);
+  if (c == 0) return TriG{p.x0, p.y0, p.z0, m01x, m01y, m01z, m02x, m02y, m02z};
+  if (c == 1) return TriG{m01x, m01y, m01z, p.x1, p.y1, p.z1, m12x, m12y, m12z};
+  if (c == 2) return TriG{m01x, m01y, m01z, m12x, m12y, m12z, m02x, m02y, m02z};
+  return TriG{m02x, m02y, m02z, m12x, m12y, m12z, p.x2, p.y2, p.z2};
+}
+// the sub-triangle reached from `root` by the child indices in `path` (2 bits per level)
+__device__ __forceinline__ TriG descend(const TriG& root, unsigned path, int lev) {
+  TriG t = root;
+  for (int l = 0; l < lev; ++l) t = child(t, (path >> (2 * l)) & 3u);
+  return t;
+}
+
+// Depth-first pair subdivision in the reference's order (source child outer, target child
+// inner).  A stack entry is (level, source path, target path) packed in 32 bits; the
+// sub-triangles are rebuilt from the roots, which keeps the stack at 61 words.
+template <int NUNK>
+__device__ __noinline__ void pair_subdivide(const TriG& s0, const TriG& t0, float sa, float ta, float s1x, float s1y,
+                                            float s1z, float s2x, float s2y, float s2z, float q, int maxlev,
+                                            float (*u)[3]) {
+  unsigned st[kCStack];
+  int sp = 0;
+  auto push = [&](unsigned code) {
+    const unsigned lev = code & 7u, sps = (code >> 3) & 0xffu, tps = (code >> 11) & 0xffu;
+    for (int a = 3; a >= 0; --a)
+      for (int b = 3; b >= 0; --b)
+        st[sp++] = (lev + 1) | ((sps | ((unsigned)a << (2 * lev))) << 3) | ((tps | ((unsigned)b << (2 * lev))) << 11);
+  };
+  push(0u);
+  while (sp > 0) {
+    const unsigned code = st[--sp];
+    const int lev = (int)(code & 7u);
+    const TriG s = descend(s0, (code >> 3) & 0xffu, lev);
+    const TriG t = descend(t0, (code >> 11) & 0xffu, lev);
+    const float f4 = __int_as_float((127 - 2 * lev) << 23);   // 0.25^lev: the children's area factor
+    const float csa = sa * f4, cta = ta * f4;
+    float scx, scy, scz, tcx, tcy, tcz;
+    cen(s, scx, scy, scz);
+    cen(t, tcx, tcy, tcz);
+    const float thr = __fmul_rn(__fadd_rn(__fsqrt_rn(csa), __fsqrt_rn(cta)), 4.0f);
+    if (lev >= maxlev || dist_rn3(tcx, tcy, tcz, scx, scy, scz) > thr) {
+      const float f = f4 * f4;   // 0.0625^lev (Kernels.h:1275-1278)
+      leaf3<NUNK>(tcx, tcy, tcz, scx, scy, scz, s1x * f, s1y * f, s1z * f, s2x * f, s2y * f, s2z * f, q * f, u);
+    } else if (sp + 16 <= kCStack) {
+      push(code);
+    }
+  }
+}
+
+__global__ void k_pack_src_panels(int np, const float* __restrict__ x, const float* __restrict__ y,
+                                  const float* __restrict__ z, const uint32_t* __restrict__ idx,
+                                  const float* __restrict__ area, const float* __restrict__ x1x,
+                                  const float* __restrict__ x1y, const float* __restrict__ x1z,
+                                  const float* __restrict__ x2x, const float* __restrict__ x2y,
+                                  const float* __restrict__ x2z, int np_pad, SrcRec* rec, TriG* tri) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= np_pad) return;
+  SrcRec r;
+  TriG t;
+  if (j < np) {
+    const uint32_t p0 = idx[3 * (size_t)j], p1 = idx[3 * (size_t)j + 1], p2 = idx[3 * (size_t)j + 2];
+    t = TriG{x[p0], y[p0], z[p0], x[p1], y[p1], z[p1], x[p2], y[p2], z[p2]};
+    float cx, cy, cz;
+    cen(t, cx, cy, cz);
+    const float sa = area[j];
+    r.c = make_float4(cx, cy, cz, __fsqrt_rn(sa));
+    r.s1 = make_float4(__fmul_rn(x1x[j], sa), __fmul_rn(x1y[j], sa), __fmul_rn(x1z[j], sa), sa);
+    r.s2 = make_float4(__fmul_rn(x2x[j], sa), __fmul_rn(x2y[j], sa), __fmul_rn(x2z[j], sa), 0.f);
+  } else {
+    t = TriG{0, 0, 0, 0, 0, 0, 0, 0, 0};
+    r.c = make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.f);
+    r.s1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.s2 = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  rec[j] = r;
+  tri[j] = t;
+}
+
+template <int NUNK>
+__global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, const TriG* __restrict__ stri, int snp,
+                                               const TriG* __restrict__ ttri, const float* __restrict__ tarea,
+                                               const float* __restrict__ t1x, const float* __restrict__ t1y,
+                                               const float* __restrict__ t1z, const float* __restrict__ t2x,
+                                               const float* __restrict__ t2y, const float* __restrict__ t2z,
+                                               const float* __restrict__ tnx, const float* __restrict__ tny,
+                                               const float* __restrict__ tnz, int tnp, int is_self, int maxlev,
+                                               float* __restrict__ coeff, long long ld) {
+  __shared__ SrcRec sr[kCB];
+  const int i = blockIdx.x * kCB + threadIdx.x;
+  const int j0 = blockIdx.y * kCB;
+  sr[threadIdx.x] = srec[j0 + threadIdx.x];
+  __syncthreads();
+  if (i >= tnp) return;
+  const TriG tt = ttri[i];
+  float tcx, tcy, tcz;
+  cen(tt, tcx, tcy, tcz);
+  const float ta = tarea[i];
+  const float sqta = __fsqrt_rn(ta);
+  const float b[3][3] = {{t1x[i], t1y[i], t1z[i]}, {t2x[i], t2y[i], t2z[i]},
+                         {NUNK == 3 ? tnx[i] : 0.f, NUNK == 3 ? tny[i] : 0.f, NUNK == 3 ? tnz[i] : 0.f}};
+  const float fac = (float)(1.0 / (4.0 * 3.14159265358979323846));
+  const int jend = min(kCB, snp - j0);
+  for (int jj = 0; jj < jend; ++jj) {
+    const int j = j0 + jj;
+    float* col = coeff + (size_t)j * NUNK * (size_t)ld + (size_t)i * NUNK;
+    if (is_self && j == i) {
+      // Coefficients.h:414-436, then the 1/(4 pi) scale of :443-447, both in float
+      const float tp = (float)(2.0 * 3.14159265358979323846);
+      col[0] = 0.f * fac;
+      col[1] = tp * fac;
+      if (NUNK == 3) col[2] = 0.f;
+      col[(size_t)ld] = -tp * fac;
+      col[(size_t)ld + 1] = 0.f;
+      if (NUNK == 3) {
+        col[(size_t)ld + 2] = 0.f;
+        col[2 * (size_t)ld] = 0.f;
+        col[2 * (size_t)ld + 1] = 0.f;
+        col[2 * (size_t)ld + 2] = tp * fac;
+      }
+      continue;
+    }
+    const SrcRec s = sr[jj];
+    float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    const float thr = __fmul_rn(__fadd_rn(s.c.w, sqta), 4.0f);
+    if (maxlev == 0 || dist_rn3(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z) > thr) {
+      leaf3<NUNK>(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, u);
+    } else {
+      pair_subdivide<NUNK>(stri[j], tt, s.s1.w, ta, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, maxlev,
+                           u);
+    }
+#pragma unroll
+    for (int k = 0; k < NUNK; ++k)
+#pragma unroll
+      for (int l = 0; l < NUNK; ++l)
+        col[(size_t)k * ld + l] = (u[k][0] * b[l][0] + u[k][1] * b[l][1] + u[k][2] * b[l][2]) * fac;
+  }
+}
+
+__global__ void k_pack_tri(int np, const float* __restrict__ x, const float* __restrict__ y,
+                           const float* __restrict__ z, const uint32_t* __restrict__ idx, TriG* tri) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= np) return;
+  const uint32_t p0 = idx[3 * (size_t)j], p1 = idx[3 * (size_t)j + 1], p2 = idx[3 * (size_t)j + 2];
+  tri[j] = TriG{x[p0], y[p0], z[p0], x[p1], y[p1], z[p1], x[p2], y[p2], z[p2]};
+}
+
+}  // namespace o3g
+
+using namespace o3g;
+
+static bool surf_ok(const o3g_surface_t* s, bool need_norm) {
+  if (!s || s->nn < 0 || s->np < 0) return false;
+  if (s->np == 0) return true;
+  if (!s->x || !s->y || !s->z || !s->idx || !s->area || !s->x1x || !s->x1y || !s->x1z || !s->x2x || !s->x2y || !s->x2z)
+    return false;
+  if (need_norm && (!s->nx || !s->ny || !s->nz)) return false;
+  return true;
+}
+
+extern "C" int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int32_t is_self, const o3g_surface_t* src,
+                                              const o3g_surface_t* targ, float* coeffs, int64_t ld, void* stream) {
+  if (maxlev < 0 || maxlev > kCoeffMaxLev || (nunk != 2 && nunk != 3) || !surf_ok(src, false) ||
+      !surf_ok(targ, nunk == 3) || !coeffs) {
+    set_error("panels_on_panels_coeff: bad maxlev (0..4), nunk (2|3), surface or output pointer");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (ld < (int64_t)targ->np * nunk) {
+    set_error("panels_on_panels_coeff: leading dimension smaller than the block's rows");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (is_self && src->np != targ->np) {
+    set_error("panels_on_panels_coeff: is_self needs the same panel count");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (src->np == 0 || targ->np == 0) return O3G_OK;
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int snp = src->np, tnp = targ->np;
+  const int sblocks = (snp + kCB - 1) / kCB, snp_pad = sblocks * kCB;
+  size_t bytes = align_up((size_t)snp_pad * sizeof(SrcRec)) + align_up((size_t)snp_pad * sizeof(TriG)) +
+                 align_up((size_t)tnp * sizeof(TriG));
+  Workspace* ws = nullptr;
+  O3G_TRY(workspace_get(st, bytes, &ws));
+  Carve cv(ws->base);
+  SrcRec* srec = cv.take<SrcRec>(snp_pad);
+  TriG* stri = cv.take<TriG>(snp_pad);
+  TriG* ttri = cv.take<TriG>(tnp);
+  k_pack_src_panels<<<(snp_pad + 255) / 256, 256, 0, st>>>(snp, src->x, src->y, src->z, src->idx, src->area, src->x1x,
+                                                          src->x1y, src->x1z, src->x2x, src->x2y, src->x2z, snp_pad,
+                                                          srec, stri);
+  k_pack_tri<<<(tnp + 255) / 256, 256, 0, st>>>(tnp, targ->x, targ->y, targ->z, targ->idx, ttri);
+  note_launch(2);
+  dim3 grid((tnp + kCB - 1) / kCB, sblocks);
+  KernelTimer& tm = thread_timer();
+  tm.begin(st);
+  if (nunk == 2)
+    k_coeff<2><<<grid, kCB, 0, st>>>(srec, stri, snp, ttri, targ->area, targ->x1x, targ->x1y, targ->x1z, targ->x2x,
+                                     targ->x2y, targ->x2z, nullptr, nullptr, nullptr, tnp, is_self, maxlev, coeffs, ld);
+  else
+    k_coeff<3><<<grid, kCB, 0, st>>>(srec, stri, snp, ttri, targ->area, targ->x1x, targ->x1y, targ->x1z, targ->x2x,
+                                     targ->x2y, targ->x2z, targ->nx, targ->ny, targ->nz, tnp, is_self, maxlev, coeffs,
+                                     ld);
+  note_launch();
+  tm.end(st);
+  O3G_CUDA_TRY(cudaGetLastError());
+  return O3G_OK;
+}

@@ -169,3 +169,135 @@ class InfluenceVisitor:
         if isinstance(src, Points) and isinstance(targ, Points):
             return points_affect_points(src, targ, self.restype, self.env)
         raise NotImplementedError("pairing %s -> %s" % (type(src).__name__, type(targ).__name__))
+
+
+# ------------------------------------------------------------------------------------
+# surfaces
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def generate_ovoid(levels, rx=1.0, ry=1.0, rz=1.0):
+    """GeomHelper.cpp:41-91: icosahedral sphere of radius 0.5 refined `levels` times and
+    scaled by (rx, ry, rz).  Returns nodes x[3, nn] (float32) and idx[3*np] (uint32)."""
+    lib = L.lib()
+    nn, np_ = ctypes.c_int32(), ctypes.c_int32()
+    L.check(lib.o3g_ovoid_size(levels, ctypes.byref(nn), ctypes.byref(np_)), "o3g_ovoid_size")
+    x = np.zeros((3, nn.value), np.float32)
+    idx = np.zeros(3 * np_.value, np.uint32)
+    L.check(lib.o3g_generate_ovoid(levels, rx, ry, rz, *_rows(x, 3), idx.ctypes.data), "o3g_generate_ovoid")
+    return x, idx
+
+
+class Surfaces:
+    """Surfaces<S> (Surfaces.h:60-225): nodes x[3,nn], panel node indices idx[3*np], and
+    per panel the basis x1/x2/norm [3,np], area [np], vortex-sheet strengths ps[3,np] (x1,
+    x2, source), absolute strengths ts[3,np] and panel-centre velocities pu[3,np].  Built
+    on the host (numpy); `to(device)` returns torch copies of the arrays for device calls.
+    nunk = 3 when the source strength is unknown (the reference's default,
+    Surfaces.h:71), 2 for tangential vortex sheets only."""
+
+    def __init__(self, x, idx, nunk=3):
+        self.x = _f32(x)
+        self.idx = np.ascontiguousarray(idx, np.uint32)
+        self.nunk = nunk
+        nn, np_ = self.x.shape[1], self.idx.shape[0] // 3
+        self.x1 = np.zeros((3, np_), np.float32)
+        self.x2 = np.zeros((3, np_), np.float32)
+        self.norm = np.zeros((3, np_), np.float32)
+        self.area = np.zeros(np_, np.float32)
+        L.check(L.lib().o3g_compute_bases(nn, *_rows(self.x, 3), np_, self.idx.ctypes.data, *_rows(self.x1, 3),
+                                          *_rows(self.x2, 3), *_rows(self.norm, 3), self.area.ctypes.data),
+                "o3g_compute_bases")
+        self.ps = np.zeros((3, np_), np.float32)
+        self.ts = np.zeros((3, np_), np.float32)
+        self.pu = np.zeros((3, np_), np.float32)
+
+    @property
+    def npanels(self):
+        return self.area.shape[0]
+
+    @property
+    def nnodes(self):
+        return self.x.shape[1]
+
+    def set_sheet_strengths(self, ps0, ps1, src=None):
+        """Surfaces::set_str (Surfaces.h:267-306) without the BEM offsets."""
+        self.ps[0], self.ps[1] = ps0, ps1
+        if src is not None:
+            self.ps[2] = src
+        L.check(L.lib().o3g_sheet_to_panel_strength(self.npanels, self.ps[0].ctypes.data, self.ps[1].ctypes.data,
+                                                    *_rows(self.x1, 3), *_rows(self.x2, 3), self.area.ctypes.data,
+                                                    *_rows(self.ts, 3)), "o3g_sheet_to_panel_strength")
+
+    def device_arrays(self, device):
+        import torch
+        keys = ("x", "idx", "area", "x1", "x2", "norm", "ps", "ts", "pu")
+        out = {}
+        for k in keys:
+            a = getattr(self, k)
+            t = torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(device)
+            out[k] = t
+        return out
+
+
+def surface_struct(arr, nunk=3):
+    """o3g_surface_t over a dict of arrays (numpy or torch, as returned by device_arrays)."""
+    x, x1, x2, nm = arr["x"], arr["x1"], arr["x2"], arr["norm"]
+    s = L.Surface()
+    s.nn = x.shape[1]
+    s.x, s.y, s.z = _rows(x, 3)
+    s.np = arr["area"].shape[0]
+    s.idx = _base(arr["idx"])
+    s.area = _base(arr["area"])
+    s.x1x, s.x1y, s.x1z = _rows(x1, 3)
+    s.x2x, s.x2y, s.x2z = _rows(x2, 3)
+    s.nx, s.ny, s.nz = _rows(nm, 3)
+    return s
+
+
+def panels_affect_points(src, targ, restype=None, env=None, maxlev=3, arrays=None):
+    """Influence.h:557: accumulate the velocity (and gradients) of the panels of `src` at the
+    points of `targ`.  `arrays` (from src.device_arrays) selects device memory; otherwise
+    the host arrays of `src` are used and targ must be numpy."""
+    restype = restype or ResultsType()
+    env = env or ExecEnv()
+    grads = restype.compute_grad()
+    a = arrays or {"x": src.x, "idx": src.idx, "area": src.area, "ts": src.ts, "ps": src.ps}
+    on_dev = _is_dev(a["x"])
+    if _is_dev(targ.x) != on_dev:
+        raise ValueError("surface and targets must live in the same memory")
+    tug = (ctypes.c_void_p * 9)(*_rows(targ.ug, 9)) if grads else None
+    sss = _rows(a["ps"], 3)[2] if src.nunk == 3 else None
+    st = L.lib().o3g_panels_affect_points(L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev, a["x"].shape[1],
+                                          *_rows(a["x"], 3), a["area"].shape[0], _base(a["idx"]), _base(a["area"]),
+                                          *_rows(a["ts"], 3), sss, targ.n, *_rows(targ.x, 3), *_rows(targ.u, 3),
+                                          tug, env.stream_handle(on_dev))
+    L.check(st, "o3g_panels_affect_points")
+
+
+def points_affect_panels(src, targ, env=None, maxlev=3, arrays=None, pu=None):
+    """Influence.h:1107: subtract the panel-averaged velocity of the particles `src` from the
+    panel velocities of `targ` (pu, or targ.pu on the host)."""
+    env = env or ExecEnv()
+    a = arrays or {"x": targ.x, "idx": targ.idx, "area": targ.area}
+    pu = targ.pu if pu is None else pu
+    on_dev = _is_dev(a["x"])
+    st = L.lib().o3g_points_affect_panels(L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev, src.n, *_rows(src.x, 3),
+                                          *_rows(src.s, 3), a["x"].shape[1], *_rows(a["x"], 3), a["area"].shape[0],
+                                          _base(a["idx"]), _base(a["area"]), *_rows(pu, 3),
+                                          env.stream_handle(on_dev))
+    L.check(st, "o3g_points_affect_panels")
+
+
+def panels_on_panels_coeff(src_arrays, targ_arrays, nunk, is_self, out, ld=None, maxlev=3, stream=None):
+    """Coefficients.h:169: write the column-major (ntarg*nunk) x (nsrc*nunk) block into the
+    device tensor `out` (viewed with leading dimension ld, default ntarg*nunk)."""
+    s = surface_struct(src_arrays)
+    t = surface_struct(targ_arrays)
+    ld = ld or t.np * nunk
+    h = stream if stream is not None else ExecEnv().stream_handle(True)
+    st = L.lib().o3g_panels_on_panels_coeff(maxlev, nunk, int(is_self), ctypes.byref(s), ctypes.byref(t),
+                                            _base(out), ld, h)
+    L.check(st, "o3g_panels_on_panels_coeff")
