@@ -176,6 +176,36 @@ int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev,
 int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int32_t is_self, const o3g_surface_t* src,
                                    const o3g_surface_t* targ, float* coeffs, int64_t ld, void* stream);
 
+/* ---- BEM system ------------------------------------------------------------------------
+ * Replaces BEM<S,I> (BEM.h:44-234).  The handle owns the device-resident n x n FP32 matrix
+ * (column-major, leading dimension from o3g_bem_matrix), its LU factors and scratch.
+ * The reference solves with Eigen GMRES (BEM.h:182-202); here the matrix is factorised
+ * in FP32 with partial pivoting and TF32 tensor-core trailing updates, and solutions are
+ * refined with residuals b - A x formed in FP64 until ||r||/||b|| <= tol (the residual
+ * the reference prints, BEM.h:227-230). */
+typedef struct o3g_bem o3g_bem_t;
+/* allocates the handle and ~2 n^2 floats of device memory (n <= 200000; the panel
+ * factorisation needs n <= ~68000 on 152 SMs) */
+int32_t o3g_bem_create(int64_t n, o3g_bem_t** h);
+int32_t o3g_bem_destroy(o3g_bem_t* h);
+/* device pointer and leading dimension of the matrix, e.g. to assemble blocks in place with
+ * o3g_panels_on_panels_coeff(..., A + cstart*ld + rstart, ld, ...); marks A as changed */
+int32_t o3g_bem_matrix(o3g_bem_t* h, float** A, int64_t* ld);
+/* BEM::set_block, BEM.h:116-136: copy a column-major nrows x ncols block into A */
+int32_t o3g_bem_set_block(o3g_bem_t* h, int64_t rstart, int64_t nrows, int64_t cstart, int64_t ncols,
+                          const float* blk, int32_t mem, void* stream);
+/* LU factorisation of the current A (BEM.h:184-195's solver.compute) */
+int32_t o3g_bem_factor(o3g_bem_t* h, void* stream);
+/* solve A x = b (BEM.h:202): b, x (float) and x64 (double, nullable) in `mem` memory;
+ * returns the refinement count and the final FP64 relative residual; O3G_ERR_NOT_CONVERGED
+ * when tol is not reached within max_iter refinements (x still holds the best iterate) */
+int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
+                      int32_t max_iter, int32_t* iters, double* relres, void* stream);
+/* finalize_vels of panel velocities (u = fs + u/(4 pi), ElementBase.h:187-193) and
+ * vels_to_rhs_panels (RHS.h:92-110) in one pass; device arrays; rhs has np*nunk entries */
+int32_t o3g_panel_vels_to_rhs(int32_t np, int32_t nunk, const double* fs, float* pu, float* pv, float* pw,
+                              const o3g_surface_t* surf, float* rhs, void* stream);
+
 /* ---- points_affect_points without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory
  * after start-up (applications that give all device memory to their own pool, real-time

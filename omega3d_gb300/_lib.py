@@ -86,6 +86,20 @@ def _declare(l):
     l.o3g_points_affect_panels.argtypes = [c_i32, c_i32, c_i32] + [P] * 6 + [c_i32, P, P, P, c_i32, P, P, P, P, P, P]
     l.o3g_panels_on_panels_coeff.restype = c_i32
     l.o3g_panels_on_panels_coeff.argtypes = [c_i32, c_i32, c_i32, P, P, P, ctypes.c_int64, P]
+    l.o3g_bem_create.restype = c_i32
+    l.o3g_bem_create.argtypes = [ctypes.c_int64, P]
+    l.o3g_bem_destroy.restype = c_i32
+    l.o3g_bem_destroy.argtypes = [P]
+    l.o3g_bem_matrix.restype = c_i32
+    l.o3g_bem_matrix.argtypes = [P, P, P]
+    l.o3g_bem_set_block.restype = c_i32
+    l.o3g_bem_set_block.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, P, c_i32, P]
+    l.o3g_bem_factor.restype = c_i32
+    l.o3g_bem_factor.argtypes = [P, P]
+    l.o3g_bem_solve.restype = c_i32
+    l.o3g_bem_solve.argtypes = [P, P, P, P, c_i32, c_d, c_i32, P, P, P]
+    l.o3g_panel_vels_to_rhs.restype = c_i32
+    l.o3g_panel_vels_to_rhs.argtypes = [c_i32, c_i32, P, P, P, P, P, P, P]
     l.o3g_points_affect_points_noalloc.restype = c_i32
     l.o3g_points_affect_points_noalloc.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
     l.o3g_points_affect_points_d.restype = c_i32

@@ -301,3 +301,128 @@ def panels_on_panels_coeff(src_arrays, targ_arrays, nunk, is_self, out, ld=None,
     st = L.lib().o3g_panels_on_panels_coeff(maxlev, nunk, int(is_self), ctypes.byref(s), ctypes.byref(t),
                                             _base(out), ld, h)
     L.check(st, "o3g_panels_on_panels_coeff")
+
+
+# ------------------------------------------------------------------------------------
+# BEM system and solve
+
+class BEM:
+    """BEM<S,I> (BEM.h:44-234) over the device-resident system of libo3dgpu: set_block,
+    set_rhs, solve, get_str.  The matrix is factorised (FP32 LU, TF32 trailing updates)
+    on the first solve after it changed, and solutions are refined with FP64 residuals."""
+
+    def __init__(self, n):
+        self.n = int(n)
+        h = ctypes.c_void_p()
+        L.check(L.lib().o3g_bem_create(self.n, ctypes.byref(h)), "o3g_bem_create")
+        self.h = h
+        self.A_is_current = False
+        self.factored = False
+        self.b = np.zeros(self.n, np.float32)
+        self.strengths = np.zeros(self.n, np.float32)
+        self.iters = 0
+        self.relres = float("nan")
+
+    def __del__(self):
+        try:
+            if self.h:
+                L.lib().o3g_bem_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def matrix(self):
+        p, ld = ctypes.c_void_p(), ctypes.c_int64()
+        L.check(L.lib().o3g_bem_matrix(self.h, ctypes.byref(p), ctypes.byref(ld)), "o3g_bem_matrix")
+        self.factored = False
+        return p.value, ld.value
+
+    def set_block(self, rstart, cstart, blk, stream=None):
+        """BEM::set_block: blk is column-major (ncols, nrows) numpy or torch CUDA."""
+        ncols, nrows = blk.shape
+        on = _is_dev(blk)
+        L.check(L.lib().o3g_bem_set_block(self.h, rstart, nrows, cstart, ncols, _base(blk),
+                                          L.MEM_DEVICE if on else L.MEM_HOST,
+                                          ExecEnv(stream=stream).stream_handle(on)), "o3g_bem_set_block")
+        self.factored = False
+
+    def assemble(self, src_arrays, targ_arrays, nunk, is_self, rstart=0, cstart=0, maxlev=3, stream=None):
+        """Coefficients.h:169 written straight into the system matrix at (rstart, cstart)."""
+        base, ld = self.matrix()
+        s = surface_struct(src_arrays)
+        t = surface_struct(targ_arrays)
+        h = ExecEnv(stream=stream).stream_handle(True)
+        L.check(L.lib().o3g_panels_on_panels_coeff(maxlev, nunk, int(is_self), ctypes.byref(s), ctypes.byref(t),
+                                                   base + 4 * (cstart * ld + rstart), ld, h),
+                "o3g_panels_on_panels_coeff")
+
+    def set_rhs(self, cstart, b):
+        self.b[cstart:cstart + len(b)] = _np_host(b)
+
+    def factor(self, stream=None):
+        L.check(L.lib().o3g_bem_factor(self.h, ExecEnv(stream=stream).stream_handle(True)), "o3g_bem_factor")
+        self.factored = True
+
+    def solve(self, b=None, tol=1e-10, max_iter=30, stream=None, x64=False):
+        """BEM::solve (BEM.h:169-234); returns the FP32 strengths (and FP64 ones if asked)."""
+        if not self.factored:
+            self.factor(stream)
+        b = self.b if b is None else b
+        on = _is_dev(b)
+        it, rr = ctypes.c_int32(), ctypes.c_double()
+        if on:
+            x = torch.empty(self.n, dtype=torch.float32, device=b.device)
+            xd = torch.empty(self.n, dtype=torch.float64, device=b.device) if x64 else None
+        else:
+            b = np.ascontiguousarray(b, np.float32)
+            x = np.empty(self.n, np.float32)
+            xd = np.empty(self.n, np.float64) if x64 else None
+        st = L.lib().o3g_bem_solve(self.h, _base(b), _base(x), None if xd is None else _base(xd),
+                                   L.MEM_DEVICE if on else L.MEM_HOST, tol, max_iter, ctypes.byref(it),
+                                   ctypes.byref(rr), ExecEnv(stream=stream).stream_handle(on))
+        self.iters, self.relres = it.value, rr.value
+        L.check(st, "o3g_bem_solve")
+        if not on:
+            self.strengths = x
+        return (x, xd) if x64 else x
+
+    def get_str(self, cstart, ncols):
+        return self.strengths[cstart:cstart + ncols]
+
+
+def _np_host(a):
+    if _is_dev(a):
+        return a.detach().cpu().numpy()
+    return np.asarray(a)
+
+
+def solve_bem(fs, vort, bdry, bem, env=None, maxlev=3, tol=1e-10, max_iter=30):
+    """solve_bem (BEMHelper.h:43-265) for one boundary collection `bdry` (Surfaces) and a
+    list of vortex-particle collections `vort` (host Points): RHS from the particles'
+    panel-averaged velocity plus the freestream, the matrix assembled and factorised when
+    it is not current, the FP32/TF32 LU solve refined in FP64, and the strengths scattered
+    back (Surfaces::set_str, Surfaces.h:267-306)."""
+    env = env or ExecEnv()
+    dev = "cuda"
+    arr = bdry.device_arrays(dev)
+    nunk = bdry.nunk
+    np_ = bdry.npanels
+    pu = torch.zeros((3, np_), dtype=torch.float32, device=dev)
+    for v in vort:
+        src = Points(*(torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (v.x, v.s, v.r)))
+        points_affect_panels(src, bdry, env, maxlev=maxlev, arrays=arr, pu=pu)
+    rhs = torch.empty(np_ * nunk, dtype=torch.float32, device=dev)
+    fsd = (ctypes.c_double * 3)(*fs)
+    s = surface_struct(arr)
+    L.check(L.lib().o3g_panel_vels_to_rhs(np_, nunk, fsd, *_rows(pu, 3), ctypes.byref(s), _base(rhs),
+                                          env.stream_handle(True)), "o3g_panel_vels_to_rhs")
+    if not bem.A_is_current:
+        bem.assemble(arr, arr, nunk, True, maxlev=maxlev)
+        bem.factor()
+        bem.A_is_current = True
+    x = bem.solve(rhs, tol=tol, max_iter=max_iter)
+    xs = x.cpu().numpy()
+    bdry.pu[...] = pu.cpu().numpy()
+    bdry.set_sheet_strengths(xs[0::nunk], xs[1::nunk], xs[2::nunk] if nunk == 3 else None)
+    bem.strengths = xs
+    return xs

@@ -1,0 +1,144 @@
+"""GPU tests of the BEM system through the C-ABI: FP32 LU with partial pivoting (TF32
+trailing updates) plus FP64-residual refinement, against an FP64 LU oracle (numpy/LAPACK
+on the same matrix) and the potential-flow known answer on a sphere.
+
+Tolerances: refined solutions reach ||b - A x||/||b|| <= 1e-10 (FP64 residual of the FP32
+matrix) and agree with the FP64 LU solution of the same matrix to 1e-9 relative (the
+matrices here have condition numbers below 1e3)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+import omega3d_gb300 as G
+from omega3d_gb300 import _lib as L
+from omega3d_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(A, b, tol=1e-10, max_iter=30):
+    n = A.shape[0]
+    bem = G.BEM(n)
+    bem.set_block(0, 0, np.ascontiguousarray(A.T.astype(np.float32)))   # column-major block
+    x, x64 = bem.solve(b.astype(np.float32), tol=tol, max_iter=max_iter, x64=True)
+    return bem, x, x64
+
+
+@pytest.mark.parametrize("n", [1, 7, 128, 129, 1000, 2500])
+def test_lu_refined_solve_matches_fp64_lu(cuda, n):
+    rng = np.random.default_rng(n)
+    A = rng.normal(size=(n, n)) / np.sqrt(n) + 2.0 * np.eye(n)
+    b = rng.normal(size=n)
+    bem, x, x64 = _solve(A, b)
+    A32 = A.astype(np.float32).astype(np.float64)
+    b32 = b.astype(np.float32).astype(np.float64)
+    xref = np.linalg.solve(A32, b32)
+    assert bem.relres <= 1e-10
+    assert np.linalg.norm(b32 - A32 @ x64) / np.linalg.norm(b32) <= 1e-10
+    assert np.abs(x64 - xref).max() <= 1e-9 * np.abs(xref).max()
+    assert np.abs(x - xref).max() <= 1e-6 * np.abs(xref).max()
+
+
+def test_pivoting_is_required_and_done(cuda):
+    # zero diagonal everywhere: LU without row interchanges fails at the first column
+    n = 700
+    rng = np.random.default_rng(1)
+    P = np.eye(n)[rng.permutation(n)]
+    A = P @ (np.eye(n) * 3.0 + rng.normal(size=(n, n)) / np.sqrt(n))
+    np.fill_diagonal(A, 0.0)
+    b = rng.normal(size=n)
+    bem, x, x64 = _solve(A, b)
+    A32 = A.astype(np.float32).astype(np.float64)
+    assert np.linalg.norm(b.astype(np.float32) - A32 @ x64) / np.linalg.norm(b.astype(np.float32)) <= 1e-10
+
+
+def test_singular_matrix_is_reported(cuda):
+    n = 300
+    rng = np.random.default_rng(2)
+    A = rng.normal(size=(n, n))
+    A[:, 17] = 0.0
+    bem = G.BEM(n)
+    bem.set_block(0, 0, np.ascontiguousarray(A.T.astype(np.float32)))
+    with pytest.raises(G.O3GError) as ei:
+        bem.factor()
+    assert ei.value.status == 7
+
+
+def test_solve_before_factor_and_bad_args(cuda):
+    lib = L.lib()
+    h = ctypes.c_void_p()
+    assert lib.o3g_bem_create(0, ctypes.byref(h)) == 1
+    L.check(lib.o3g_bem_create(16, ctypes.byref(h)), "create")
+    b = np.ones(16, np.float32)
+    x = np.zeros(16, np.float32)
+    it, rr = ctypes.c_int32(), ctypes.c_double()
+    assert lib.o3g_bem_solve(h, b.ctypes.data, x.ctypes.data, None, 0, 1e-10, 5, ctypes.byref(it),
+                             ctypes.byref(rr), None) == 9
+    blk = np.ones((4, 4), np.float32)
+    assert lib.o3g_bem_set_block(h, 14, 4, 0, 4, blk.ctypes.data, 0, None) == 1
+    L.check(lib.o3g_bem_destroy(h), "destroy")
+
+
+@pytest.mark.parametrize("nunk", [2, 3])
+def test_sphere_bem_vs_fp64_lu_oracle(cuda, nunk):
+    import torch
+    x, i = G.generate_ovoid(3, 2.0, 2.0, 2.0)          # unit sphere, 1280 panels
+    s = G.Surfaces(x, i, nunk=nunk)
+    px, ps, pr = W.shell_particles(4000, seed=31)
+    bem = G.BEM(s.npanels * nunk)
+    xs = G.solve_bem((1.0, 0.0, 0.0), [G.Points(px, ps, pr)], s, bem)
+    assert bem.relres <= 1e-10 and bem.iters <= 10
+    # oracle: the same RHS from the oracle's points_affect_panels + finalize + vels_to_rhs,
+    # and the GPU-assembled matrix solved by LAPACK in FP64
+    pu = O.points_affect_panels(px, ps, s.x, s.idx, s.area, "rm", 1)
+    O.finalize_vels(pu, None, (1.0, 0.0, 0.0))
+    rhs = O.vels_to_rhs_panels(pu, s.x1, s.x2, s.norm, nunk)
+    arr = s.device_arrays("cuda")
+    n = s.npanels * nunk
+    Ac = torch.empty((n, n), device="cuda")
+    G.panels_on_panels_coeff(arr, arr, nunk, True, Ac)
+    A = Ac.cpu().numpy().T.astype(np.float64)
+    xref = np.linalg.solve(A, rhs.astype(np.float64))
+    assert np.abs(xs - xref).max() <= 1e-5 * np.abs(xref).max()
+
+
+def test_sphere_potential_flow_slip_speed(cuda):
+    # inviscid flow past a sphere: the vortex sheet strength equals the slip speed 1.5 U sin(theta)
+    x, i = G.generate_ovoid(4, 2.0, 2.0, 2.0)
+    s = G.Surfaces(x, i, nunk=2)
+    bem = G.BEM(s.npanels * 2)
+    G.solve_bem((1.0, 0.0, 0.0), [], s, bem)
+    gam = s.ps[0][None, :] * s.x1 + s.ps[1][None, :] * s.x2
+    f = i.reshape(-1, 3)
+    cen = (x[:, f[:, 0]] + x[:, f[:, 1]] + x[:, f[:, 2]]) / 3
+    th = np.arccos(np.clip(cen[0] / np.linalg.norm(cen, axis=0), -1, 1))
+    ref = 1.5 * np.sin(th)
+    mag = np.linalg.norm(gam, axis=0)
+    assert np.sqrt(((mag - ref) ** 2).mean()) / np.sqrt((ref ** 2).mean()) < 5e-3
+    # the sheet is tangential and turns the flow around the body: gamma . (n x U) > 0
+    assert np.abs((gam * s.norm).sum(0)).max() < 1e-6
+
+
+def test_panel_vels_to_rhs_matches_oracle(cuda):
+    import torch
+    x, i = G.generate_ovoid(2, 2.0, 2.0, 2.0)
+    s = G.Surfaces(x, i, nunk=3)
+    rng = np.random.default_rng(4)
+    pu = rng.normal(size=(3, s.npanels)).astype(np.float32)
+    fs = (0.3, -1.0, 2.0)
+    for nunk in (2, 3):
+        pr = pu.copy()
+        O.finalize_vels(pr, None, fs)
+        ref = O.vels_to_rhs_panels(pr, s.x1, s.x2, s.norm, nunk)
+        arr = s.device_arrays("cuda")
+        P = torch.from_numpy(pu.copy()).cuda()
+        rhs = torch.empty(s.npanels * nunk, device="cuda")
+        st = G.influence.surface_struct(arr)
+        L.check(L.lib().o3g_panel_vels_to_rhs(s.npanels, nunk, (ctypes.c_double * 3)(*fs),
+                                              *[P.data_ptr() + k * s.npanels * 4 for k in range(3)],
+                                              ctypes.byref(st), rhs.data_ptr(), None), "rhs")
+        torch.cuda.synchronize()
+        assert np.array_equal(rhs.cpu().numpy(), ref)
+        assert np.array_equal(P.cpu().numpy(), pr)
