@@ -22,6 +22,7 @@
 
 #include <cublas_v2.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -30,7 +31,7 @@ namespace o3g {
 
 constexpr int kNb = 128;              // panel width
 constexpr int kPanelThreads = 256;
-constexpr int kSolveThreads = 256;
+constexpr int kSolveThreads = 1024;
 constexpr unsigned long long kSpinLimit = 1ull << 25;
 
 struct Barrier {
@@ -71,6 +72,31 @@ __device__ bool grid_sync(const Barrier& b) {
   return ok != 0;
 }
 
+// global -> shared copy of a column-major rows x cols block (leading dimension ld), with 8
+// loads in flight per thread before the stores (a plain load->store loop is latency-bound)
+__device__ __forceinline__ void stage_in(float* __restrict__ dst, int ldd, const float* __restrict__ src, long long ld,
+                                         int rows, int cols) {
+  const int total = rows * cols;
+  for (int e0 = threadIdx.x; e0 < total; e0 += 8 * blockDim.x) {
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * blockDim.x;
+      v[q] = e < total ? __ldg(src + (size_t)(e / rows) * ld + (e % rows)) : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * blockDim.x;
+      if (e < total) dst[(size_t)(e / rows) * ldd + (e % rows)] = v[q];
+    }
+  }
+}
+__device__ __forceinline__ void stage_out(float* __restrict__ dst, long long ld, const float* __restrict__ src, int lds,
+                                          int rows, int cols) {
+  const int total = rows * cols;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) dst[(size_t)(e / rows) * ld + (e % rows)] = src[(size_t)(e / rows) * lds + (e % rows)];
+}
+
 struct PanelArgs {
   float* A;
   long long ld;
@@ -84,141 +110,164 @@ struct PanelArgs {
   Barrier bar;
 };
 
+__device__ __forceinline__ void argmax_merge(float& v, int& i, float ov, int oi) {
+  if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
+}
+
 __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
   extern __shared__ float smem[];
   const int G = gridDim.x, b = blockIdx.x, jb = a.jb, R = a.R;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* slab = smem;                       // [jb][R]
   float* prow = smem + (size_t)jb * R;      // [jb] pivot row
   __shared__ float rv[kPanelThreads / 32];
   __shared__ int ri[kPanelThreads / 32];
-  __shared__ int sg_row, sg_owner;
-  __shared__ float sg_val;
+  __shared__ int sg_row;
   const int r0 = a.k0 + b * R;
   const int nr = max(0, min(a.n, r0 + R) - r0);
-  for (int j = 0; j < jb; ++j)
-    for (int r = threadIdx.x; r < nr; r += blockDim.x) slab[(size_t)j * R + r] = a.A[(size_t)(a.k0 + j) * a.ld + r0 + r];
+  if (nr > 0) stage_in(slab, R, a.A + (size_t)a.k0 * a.ld + r0, a.ld, nr, jb);
   __syncthreads();
+  // this thread's best |a(i, c)| over its rows i >= c for the current column
+  float best = -1.f;
+  int bi = 0x7fffffff;
+  for (int r = threadIdx.x; r < nr; r += blockDim.x) argmax_merge(best, bi, fabsf(slab[r]), r0 + r);
   for (int j = 0; j < jb; ++j) {
     const int c = a.k0 + j, par = j & 1;
-    // local argmax of |a(i, c)| over my rows i >= c (first index on ties)
-    float best = -1.f;
-    int bi = 0x7fffffff;
-    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-      if (r0 + r < c) continue;
-      const float v = fabsf(slab[(size_t)j * R + r]);
-      if (v > best || (v == best && r0 + r < bi)) { best = v; bi = r0 + r; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-    }
-    if ((threadIdx.x & 31) == 0) { rv[threadIdx.x >> 5] = best; ri[threadIdx.x >> 5] = bi; }
+    // block argmax (first index on ties) -> candidate (value, row, whole row) published
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
+    if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int w = 1; w < kPanelThreads / 32; ++w)
-        if (rv[w] > rv[0] || (rv[w] == rv[0] && ri[w] < ri[0])) { rv[0] = rv[w]; ri[0] = ri[w]; }
-      a.cval[par * G + b] = rv[0];
-      a.crow[par * G + b] = ri[0];
+    if (warp == 0) {
+      float v = lane < kPanelThreads / 32 ? rv[lane] : -1.f;
+      int i = lane < kPanelThreads / 32 ? ri[lane] : 0x7fffffff;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
+      if (lane == 0) {
+        a.cval[par * G + b] = v;
+        a.crow[par * G + b] = i;
+      }
+      if (v >= 0.f)
+        for (int jj = lane; jj < jb; jj += 32) a.crows[((size_t)par * G + b) * jb + jj] = slab[(size_t)jj * R + (i - r0)];
+    } else if (warp == 1 && c >= r0 && c < r0 + nr) {
+      for (int jj = lane; jj < jb; jj += 32) a.drow[par * jb + jj] = slab[(size_t)jj * R + (c - r0)];
     }
-    __syncthreads();
-    const int lrow = ri[0];
-    if (rv[0] >= 0.f)
-      for (int jj = threadIdx.x; jj < jb; jj += blockDim.x)
-        a.crows[((size_t)par * G + b) * jb + jj] = slab[(size_t)jj * R + (lrow - r0)];
-    if (c >= r0 && c < r0 + nr)
-      for (int jj = threadIdx.x; jj < jb; jj += blockDim.x) a.drow[par * jb + jj] = slab[(size_t)jj * R + (c - r0)];
     if (!grid_sync(a.bar)) return;
-    // global pivot: every block scans all candidates (same answer everywhere)
-    best = -1.f;
-    bi = 0x7fffffff;
-    int bo = 0;
-    for (int g = threadIdx.x; g < G; g += blockDim.x) {
-      const float v = a.cval[par * G + g];
-      const int i = a.crow[par * G + g];
-      if (v > best || (v == best && i < bi)) { best = v; bi = i; bo = g; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      const int oo = __shfl_xor_sync(0xffffffffu, bo, o);
-      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; bo = oo; }
-    }
-    if ((threadIdx.x & 31) == 0) { rv[threadIdx.x >> 5] = best; ri[threadIdx.x >> 5] = bi; smem[(size_t)jb * R + jb + (threadIdx.x >> 5)] = __int_as_float(bo); }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float v = rv[0];
-      int i = ri[0], ow = __float_as_int(smem[(size_t)jb * R + jb]);
-      for (int w = 1; w < kPanelThreads / 32; ++w)
-        if (rv[w] > v || (rv[w] == v && ri[w] < i)) { v = rv[w]; i = ri[w]; ow = __float_as_int(smem[(size_t)jb * R + jb + w]); }
-      if (!(v >= 0.f) || i < c || i >= a.n) {   // no finite candidate (a NaN column): keep the row
+    // warp 0: global pivot (same answer in every block) and the pivot row
+    if (warp == 0) {
+      float v = -1.f;
+      int i = 0x7fffffff, ow = -1;
+      for (int g = lane; g < G; g += 32) {
+        const float gv = a.cval[par * G + g];
+        const int gi = a.crow[par * G + g];
+        if (gv > v || (gv == v && gi < i)) { v = gv; i = gi; ow = g; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+        const int oo = __shfl_xor_sync(0xffffffffu, ow, o);
+        if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; ow = oo; }
+      }
+      if (!(v >= 0.f) || i < c || i >= a.n || ow < 0) {   // no finite candidate (a NaN column): keep the row
         i = c;
         ow = -1;
         v = 0.f;
       }
-      sg_val = v;
-      sg_row = i;
-      sg_owner = ow;
-      if (b == 0) a.piv[c] = i;
-      if (b == 0 && !(v > 0.f) && *a.singular == 0) *a.singular = c + 1;
+      for (int jj = lane; jj < jb; jj += 32)
+        prow[jj] = ow >= 0 ? a.crows[((size_t)par * G + ow) * jb + jj] : a.drow[par * jb + jj];
+      if (lane == 0) {
+        sg_row = i;
+        if (b == 0) {
+          a.piv[c] = i;
+          if (!(v > 0.f) && *a.singular == 0) *a.singular = c + 1;
+        }
+      }
     }
     __syncthreads();
     const int prow_i = sg_row;
-    for (int jj = threadIdx.x; jj < jb; jj += blockDim.x)
-      prow[jj] = sg_owner >= 0 ? a.crows[((size_t)par * G + sg_owner) * jb + jj] : a.drow[par * jb + jj];
-    __syncthreads();
     if (prow_i != c) {
       if (c >= r0 && c < r0 + nr)
         for (int jj = threadIdx.x; jj < jb; jj += blockDim.x) slab[(size_t)jj * R + (c - r0)] = prow[jj];
       if (prow_i >= r0 && prow_i < r0 + nr)
         for (int jj = threadIdx.x; jj < jb; jj += blockDim.x)
           slab[(size_t)jj * R + (prow_i - r0)] = a.drow[par * jb + jj];
+      __syncthreads();
     }
-    __syncthreads();
+    // multipliers, rank-1 update, and the next column's local argmax on the fly
     const float p = prow[j];
-    if (p != 0.f) {
-      for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-        if (r0 + r <= c) continue;
-        const float l = slab[(size_t)j * R + r] / p;
-        slab[(size_t)j * R + r] = l;
-        for (int jj = j + 1; jj < jb; ++jj) slab[(size_t)jj * R + r] = fmaf(-l, prow[jj], slab[(size_t)jj * R + r]);
+    best = -1.f;
+    bi = 0x7fffffff;
+    const bool nxt = (j + 1 < jb);
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+      if (r0 + r <= c) continue;
+      float* row = slab + r;
+      if (p != 0.f) {
+        const float l = row[(size_t)j * R] / p;
+        row[(size_t)j * R] = l;
+        for (int jj = j + 1; jj < jb; ++jj) row[(size_t)jj * R] = fmaf(-l, prow[jj], row[(size_t)jj * R]);
       }
+      if (nxt) argmax_merge(best, bi, fabsf(row[(size_t)(j + 1) * R]), r0 + r);
     }
     __syncthreads();
   }
-  for (int j = 0; j < jb; ++j)
-    for (int r = threadIdx.x; r < nr; r += blockDim.x) a.A[(size_t)(a.k0 + j) * a.ld + r0 + r] = slab[(size_t)j * R + r];
+  if (nr > 0) stage_out(a.A + (size_t)a.k0 * a.ld + r0, a.ld, slab, R, nr, jb);
 }
 
-// row interchanges k0..k0+jb-1 applied to the columns outside the panel
-__global__ void k_laswp(float* A, long long ld, int n, int k0, int jb, const int* piv) {
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nother = n - jb;
-  if (col >= nother) return;
-  if (col >= k0) col += jb;
-  float* a = A + (size_t)col * ld;
-  for (int i = k0; i < k0 + jb; ++i) {
-    const int p = piv[i];
-    if (p != i && p > i && p < n) {
-      const float t = a[i];
-      a[i] = a[p];
-      a[p] = t;
-    }
-  }
-}
-
-// U12 = L11^-1 A12: one warp per column of A12, L11 (unit lower, jb x jb) in shared memory
-__global__ void __launch_bounds__(256) k_trsm_unit_lower(float* A, long long ld, int n, int k0, int jb) {
-  extern __shared__ float L[];   // [jb][jb] column-major
-  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
-    const int i = e % jb, j = e / jb;
-    L[e] = A[(size_t)(k0 + j) * ld + k0 + i];
-  }
+// row interchanges p0..p1-1 (piv) applied to the columns [c0, c1) outside [s0, s1): one warp
+// per column stages the column's rows [p0, p1) in shared memory (coalesced), lane 0 applies
+// the interchanges in order there (rows below p1 are swapped in global memory), and the
+// segment is written back
+constexpr int kSwapMax = 512;
+__global__ void __launch_bounds__(256) k_laswp(float* A, long long ld, int n, int p0, int p1, const int* piv, int c0,
+                                               int c1, int s0, int s1) {
+  __shared__ float seg[8][kSwapMax];
+  __shared__ int pv[kSwapMax];
+  const int np_ = p1 - p0;
+  for (int e = threadIdx.x; e < np_; e += blockDim.x) pv[e] = piv[p0 + e];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ncols = n - k0 - jb;
+  const int skip = (s1 > s0) ? (s1 - s0) : 0;
+  const int ncol = c1 - c0 - skip;
+  for (int t = blockIdx.x * 8 + warp; t < ncol; t += gridDim.x * 8) {
+    int col = c0 + t;
+    if (skip && col >= s0) col += skip;
+    float* a = A + (size_t)col * ld;
+    for (int e = lane; e < np_; e += 32) seg[warp][e] = a[p0 + e];
+    __syncwarp();
+    if (lane == 0) {
+      for (int e = 0; e < np_; ++e) {
+        const int p = pv[e];
+        if (p == p0 + e || p < p0 + e || p >= n) continue;
+        const float t0 = seg[warp][e];
+        if (p < p1) {
+          seg[warp][e] = seg[warp][p - p0];
+          seg[warp][p - p0] = t0;
+        } else {
+          seg[warp][e] = a[p];
+          a[p] = t0;
+        }
+      }
+    }
+    __syncwarp();
+    for (int e = lane; e < np_; e += 32) a[p0 + e] = seg[warp][e];
+    __syncwarp();
+  }
+}
+
+// B = L^-1 B for a unit lower jb x jb L (column-major at Lp, leading dimension ldl) and the
+// ncols columns of B (jb rows at Bp, leading dimension ldb): one warp per column of B, L in
+// shared memory
+__global__ void __launch_bounds__(256) k_trsm_unit_lower(const float* Lp, long long ldl, int jb, float* Bp,
+                                                         long long ldb, int ncols) {
+  extern __shared__ float L[];   // [jb][jb] column-major
+  stage_in(L, jb, Lp, ldl, jb, jb);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int cidx = blockIdx.x * (blockDim.x / 32) + warp; cidx < ncols; cidx += gridDim.x * (blockDim.x / 32)) {
-    float* col = A + (size_t)(k0 + jb + cidx) * ld + k0;
+    float* col = Bp + (size_t)cidx * ldb;
     float x[kNb / 32];
 #pragma unroll
     for (int q = 0; q < kNb / 32; ++q) x[q] = (q * 32 + lane < jb) ? col[q * 32 + lane] : 0.f;
@@ -236,6 +285,12 @@ __global__ void __launch_bounds__(256) k_trsm_unit_lower(float* A, long long ld,
   }
 }
 
+// identity into a jb x jb column-major block
+__global__ void k_eye(float* E, int jb) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < jb * jb) E[e] = (e % jb == e / jb) ? 1.f : 0.f;
+}
+
 // ------------------------------------------------------------------------------------
 // solves with the factors: y = P b (gather), L y = y (unit lower), U x = y (upper)
 __global__ void k_permute_to_float(const double* r, const int* perm, float* y, int n) {
@@ -243,100 +298,166 @@ __global__ void k_permute_to_float(const double* r, const int* perm, float* y, i
   if (i < n) y[i] = (float)r[perm[i]];
 }
 
+// sum_m col[m*ld] * yd[m] for m < jb; the full-width case is unrolled so every load of the
+// row is in flight at once (the loop is latency-bound otherwise)
+__device__ __forceinline__ float panel_dot(const float* __restrict__ col, long long ld, const float* yd, int jb) {
+  if (jb == kNb) {
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < kNb; ++m) s[m & 7] = fmaf(__ldg(col + (size_t)m * ld), yd[m], s[m & 7]);
+    return ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+  }
+  float s = 0.f;
+  for (int m = 0; m < jb; ++m) s = fmaf(col[(size_t)m * ld], yd[m], s);
+  return s;
+}
+
+// Inverses of the diagonal kNb x kNb blocks of the factors, one block per CUDA block:
+// Linv (unit lower) and Uinv (upper) column-major at dinv + kb*2*kNb*kNb (+kNb*kNb).
+// Columns of the identity are solved by one warp each (forward / back substitution).
+__global__ void __launch_bounds__(256) k_diag_inverses(const float* __restrict__ LU, long long ld, int n,
+                                                       float* __restrict__ dinv) {
+  extern __shared__ float D[];   // [jb][jb] diagonal block
+  const int kb = blockIdx.x, k0 = kb * kNb, jb = min(kNb, n - k0);
+  stage_in(D, jb, LU + (size_t)k0 * ld + k0, ld, jb, jb);
+  __syncthreads();
+  float* Li = dinv + (size_t)kb * 2 * kNb * kNb;
+  float* Ui = Li + (size_t)kNb * kNb;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = warp; c < jb; c += blockDim.x / 32) {
+    float x[kNb / 32];
+    // L x = e_c
+#pragma unroll
+    for (int q = 0; q < kNb / 32; ++q) x[q] = (q * 32 + lane == c) ? 1.f : 0.f;
+    for (int i = c; i < jb; ++i) {
+      const float xi = __shfl_sync(0xffffffffu, x[i >> 5], i & 31);
+#pragma unroll
+      for (int q = 0; q < kNb / 32; ++q) {
+        const int m = q * 32 + lane;
+        if (m > i && m < jb) x[q] = fmaf(-D[(size_t)i * jb + m], xi, x[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kNb / 32; ++q) {
+      const int m = q * 32 + lane;
+      if (m < kNb) Li[(size_t)c * kNb + m] = m < jb ? x[q] : 0.f;
+    }
+    // U x = e_c
+#pragma unroll
+    for (int q = 0; q < kNb / 32; ++q) x[q] = (q * 32 + lane == c) ? 1.f : 0.f;
+    for (int i = c; i >= 0; --i) {
+      if ((i & 31) == lane) x[i >> 5] = x[i >> 5] / D[(size_t)i * jb + i];
+      const float xi = __shfl_sync(0xffffffffu, x[i >> 5], i & 31);
+#pragma unroll
+      for (int q = 0; q < kNb / 32; ++q) {
+        const int m = q * 32 + lane;
+        if (m < i) x[q] = fmaf(-D[(size_t)i * jb + m], xi, x[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kNb / 32; ++q) {
+      const int m = q * 32 + lane;
+      if (m < kNb) Ui[(size_t)c * kNb + m] = m < jb ? x[q] : 0.f;
+    }
+  }
+}
+
+// yd = Dinv y[k0 : k0+jb] (Dinv kNb x kNb column-major) by the whole block
+__device__ __forceinline__ void diag_apply(const float* __restrict__ Dinv, const float* y, int jb, float* yin,
+                                           float* part, float* yd) {
+  if (threadIdx.x < jb) yin[threadIdx.x] = y[threadIdx.x];
+  __syncthreads();
+  constexpr int kQ = kSolveThreads / kNb;   // 8 column chunks
+  const int m = threadIdx.x % kNb, q = threadIdx.x / kNb;
+  float s = 0.f;
+  if (m < jb) {
+    for (int k = q * (kNb / kQ); k < (q + 1) * (kNb / kQ); ++k)
+      if (k < jb) s = fmaf(__ldg(Dinv + (size_t)k * kNb + m), yin[k], s);
+  }
+  part[q * kNb + m] = s;
+  __syncthreads();
+  if (threadIdx.x < jb) {
+    float t = 0.f;
+#pragma unroll
+    for (int qq = 0; qq < kQ; ++qq) t += part[qq * kNb + threadIdx.x];
+    yd[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// y[i] -= sum_m M(i, k0+m) yd[m] for the rows [i0, i1) of this block: the 128 columns are
+// split in 4 chunks of 32 so every thread of the block has loads in flight (one row per
+// thread leaves most threads idle and each row latency-bound); partials meet in `part`
+__device__ __forceinline__ void update_rows(const float* __restrict__ LU, long long ld, int k0, int jb, int i0, int i1,
+                                            const float* yd, float* y, float* part) {
+  const int nr = i1 - i0;
+  if (nr <= 0) return;
+  if (jb != kNb) {
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) y[i] -= panel_dot(LU + (size_t)k0 * ld + i, ld, yd, jb);
+    return;
+  }
+  constexpr int kChunks = 4, kW = kNb / kChunks;
+  for (int r0 = 0; r0 < nr; r0 += kSolveThreads / kChunks) {
+    const int rows = min(kSolveThreads / kChunks, nr - r0);
+    const int q = threadIdx.x / (kSolveThreads / kChunks), r = threadIdx.x % (kSolveThreads / kChunks);
+    if (r < rows) {
+      const float* col = LU + (size_t)(k0 + q * kW) * ld + i0 + r0 + r;
+      float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int m = 0; m < kW; ++m) s[m & 3] = fmaf(__ldg(col + (size_t)m * ld), yd[q * kW + m], s[m & 3]);
+      part[q * (kSolveThreads / kChunks) + r] = (s[0] + s[1]) + (s[2] + s[3]);
+    }
+    __syncthreads();
+    if (threadIdx.x < rows) {
+      const int rr = threadIdx.x;
+      float t = 0.f;
+#pragma unroll
+      for (int qq = 0; qq < kChunks; ++qq) t += part[qq * (kSolveThreads / kChunks) + rr];
+      y[i0 + r0 + rr] -= t;
+    }
+    __syncthreads();
+  }
+}
+
 struct TrsvArgs {
   const float* LU;
+  const float* dinv;
   long long ld;
   int n;
   float* y;
   Barrier bar;
 };
 
-// forward substitution with the unit lower factor: per block column, every block solves the
-// diagonal block redundantly (from L2), then updates its share of the rows below
+// forward substitution with the unit lower factor: per block column, every block applies
+// the block's inverse to the (final) y segment, then updates its share of the rows below
 __global__ void __launch_bounds__(kSolveThreads) k_trsv_lower(TrsvArgs a) {
-  __shared__ float yd[kNb];
+  __shared__ float yd[kNb], yin[kNb];
+  __shared__ float part[kSolveThreads];
   const int G = gridDim.x;
   for (int k0 = 0; k0 < a.n; k0 += kNb) {
     const int jb = min(kNb, a.n - k0);
-    if (threadIdx.x < 32) {
-      float x[kNb / 32];
-#pragma unroll
-      for (int q = 0; q < kNb / 32; ++q) {
-        const int m = q * 32 + threadIdx.x;
-        x[q] = m < jb ? a.y[k0 + m] : 0.f;
-      }
-      for (int i = 0; i < jb; ++i) {
-        const float xi = __shfl_sync(0xffffffffu, x[i >> 5], i & 31);
-        const float* Lc = a.LU + (size_t)(k0 + i) * a.ld + k0;
-#pragma unroll
-        for (int q = 0; q < kNb / 32; ++q) {
-          const int m = q * 32 + threadIdx.x;
-          if (m > i && m < jb) x[q] = fmaf(-Lc[m], xi, x[q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < kNb / 32; ++q) {
-        const int m = q * 32 + threadIdx.x;
-        if (m < jb) yd[m] = x[q];
-      }
-    }
-    __syncthreads();
-    // rows below the block: y[i] -= sum_m L(i, k0+m) yd[m]
+    diag_apply(a.dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb, a.y + k0, jb, yin, part, yd);
     const int rest = a.n - k0 - jb;
     const int chunk = (rest + G - 1) / G;
     const int i0 = k0 + jb + blockIdx.x * chunk, i1 = min(a.n, i0 + chunk);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      float s = 0.f;
-      for (int m = 0; m < jb; ++m) s = fmaf(a.LU[(size_t)(k0 + m) * a.ld + i], yd[m], s);
-      a.y[i] -= s;
-    }
+    update_rows(a.LU, a.ld, k0, jb, i0, i1, yd, a.y, part);
     if (blockIdx.x == 0 && threadIdx.x < jb) a.y[k0 + threadIdx.x] = yd[threadIdx.x];
     if (!grid_sync(a.bar)) return;
   }
 }
 
-// back substitution with the upper factor (non-unit diagonal)
+// back substitution with the upper factor
 __global__ void __launch_bounds__(kSolveThreads) k_trsv_upper(TrsvArgs a) {
-  __shared__ float yd[kNb];
+  __shared__ float yd[kNb], yin[kNb];
+  __shared__ float part[kSolveThreads];
   const int G = gridDim.x;
   const int nblk = (a.n + kNb - 1) / kNb;
   for (int kb = nblk - 1; kb >= 0; --kb) {
     const int k0 = kb * kNb, jb = min(kNb, a.n - k0);
-    if (threadIdx.x < 32) {
-      float x[kNb / 32];
-#pragma unroll
-      for (int q = 0; q < kNb / 32; ++q) {
-        const int m = q * 32 + threadIdx.x;
-        x[q] = m < jb ? a.y[k0 + m] : 0.f;
-      }
-      for (int i = jb - 1; i >= 0; --i) {
-        const float* Uc = a.LU + (size_t)(k0 + i) * a.ld + k0;
-        // x_i = y_i / U_ii on the owning lane, then broadcast
-        const float d = Uc[i];
-        float xi = 0.f;
-        if ((i & 31) == (int)threadIdx.x) { x[i >> 5] = x[i >> 5] / d; }
-        xi = __shfl_sync(0xffffffffu, x[i >> 5], i & 31);
-#pragma unroll
-        for (int q = 0; q < kNb / 32; ++q) {
-          const int m = q * 32 + threadIdx.x;
-          if (m < i) x[q] = fmaf(-Uc[m], xi, x[q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < kNb / 32; ++q) {
-        const int m = q * 32 + threadIdx.x;
-        if (m < jb) yd[m] = x[q];
-      }
-    }
-    __syncthreads();
-    // rows above: y[i] -= sum_m U(i, k0+m) yd[m], i < k0
+    diag_apply(a.dinv + (size_t)kb * 2 * kNb * kNb + (size_t)kNb * kNb, a.y + k0, jb, yin, part, yd);
     const int chunk = (k0 + G - 1) / G;
     const int i0 = blockIdx.x * chunk, i1 = min(k0, i0 + chunk);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      float s = 0.f;
-      for (int m = 0; m < jb; ++m) s = fmaf(a.LU[(size_t)(k0 + m) * a.ld + i], yd[m], s);
-      a.y[i] -= s;
-    }
+    update_rows(a.LU, a.ld, k0, jb, i0, i1, yd, a.y, part);
     if (blockIdx.x == 0 && threadIdx.x < jb) a.y[k0 + threadIdx.x] = yd[threadIdx.x];
     if (!grid_sync(a.bar)) return;
   }
@@ -349,9 +470,17 @@ __global__ void k_resid_part(const float* __restrict__ A, long long ld, int n, c
   const int cb = blockIdx.y;
   if (i >= n) return;
   const int j0 = cb * cchunk, j1 = min(n, j0 + cchunk);
-  double s = 0.0;
-  for (int j = j0; j < j1; ++j) s = fma((double)A[(size_t)j * ld + i], x[j], s);
-  part[(size_t)cb * n + i] = s;
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  int j = j0;
+  for (; j + 8 <= j1; j += 8) {
+    float av[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) av[q] = __ldg(A + (size_t)(j + q) * ld + i);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s[q & 3] = fma((double)av[q], x[j + q], s[q & 3]);
+  }
+  for (; j < j1; ++j) s[0] = fma((double)A[(size_t)j * ld + i], x[j], s[0]);
+  part[(size_t)cb * n + i] = (s[0] + s[1]) + (s[2] + s[3]);
 }
 // r = b - sum_cb part[cb]; also accumulates ||r||^2 and ||b||^2 per block into nrm[2*blockIdx]
 __global__ void k_resid_finish(const double* __restrict__ part, int ncb, int n, const double* __restrict__ b,
@@ -452,6 +581,7 @@ struct o3g_bem {
   float* LU = nullptr;    // factors
   int* piv = nullptr;     // per-column pivot rows
   int* perm = nullptr;    // composed row permutation: (P b)[i] = b[perm[i]]
+  float* dinv = nullptr;  // inverses of the diagonal blocks of L and U
   char* scratch = nullptr;
   size_t scratch_bytes = 0;
   int* flags = nullptr;   // [0] barrier error, [1] singular column + 1, [2..3] barrier count/gen
@@ -494,10 +624,11 @@ extern "C" int32_t o3g_bem_create(int64_t n, o3g_bem_t** out) {
   if (e == cudaSuccess) e = cudaMalloc((void**)&h->piv, n * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&h->perm, n * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&h->flags, 64 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&h->dinv, (size_t)((n + kNb - 1) / kNb) * 2 * kNb * kNb * sizeof(float));
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error_cuda("o3g_bem_create: cudaMalloc", e);
-    cudaFree(h->A); cudaFree(h->LU); cudaFree(h->piv); cudaFree(h->perm); cudaFree(h->flags);
+    cudaFree(h->A); cudaFree(h->LU); cudaFree(h->piv); cudaFree(h->perm); cudaFree(h->flags); cudaFree(h->dinv);
     delete h;
     return O3G_ERR_ALLOC;
   }
@@ -517,6 +648,7 @@ extern "C" int32_t o3g_bem_destroy(o3g_bem_t* h) {
   if (!h) return O3G_OK;
   cudaDeviceSynchronize();
   cudaFree(h->A); cudaFree(h->LU); cudaFree(h->piv); cudaFree(h->perm); cudaFree(h->flags); cudaFree(h->scratch);
+  cudaFree(h->dinv);
   if (h->cublas) cublasDestroy(h->cublas);
   h->A = nullptr;
   delete h;
@@ -594,7 +726,7 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   }
   const size_t cand = align_up(2 * (size_t)G * sizeof(float)) + align_up(2 * (size_t)G * sizeof(int)) +
                       align_up(2 * (size_t)G * kNb * sizeof(float)) + align_up(2 * (size_t)kNb * sizeof(float));
-  O3G_TRY(bem_scratch(h, cand + align_up((size_t)n * 64)));
+  O3G_TRY(bem_scratch(h, cand + align_up((size_t)kNb * kNb * 4) + align_up((size_t)kNb * n * 4) + (1 << 20)));
   Carve cv(h->scratch);
   float* cval = cv.take<float>(2 * (size_t)G);
   int* crow = cv.take<int>(2 * (size_t)G);
@@ -607,47 +739,105 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   KernelTimer& tm = thread_timer();
   tm.begin(st);
   const float minus1 = -1.f, one = 1.f;
-  for (int k0 = 0; k0 < n; k0 += kNb) {
-    const int jb = n - k0 < kNb ? n - k0 : kNb;
-    const int m = n - k0;
-    int g = G;
-    int r = (m + g - 1) / g;
-    if (r < 32) {   // short panels: fewer blocks
-      g = (m + 31) / 32;
-      r = (m + g - 1) / g;
+  const size_t tsm = (size_t)kNb * kNb * sizeof(float);
+  O3G_CUDA_TRY(cudaFuncSetAttribute(k_trsm_unit_lower, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  // C = C - A B with TF32 tensor cores (all operands column-major in LU)
+  auto gemm = [&](int m, int nn, int kk, const float* Am, const float* Bm, float* Cm) -> int32_t {
+    if (m <= 0 || nn <= 0 || kk <= 0) return O3G_OK;
+    const cublasStatus_t cs = cublasGemmEx(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, nn, kk, &minus1, Am, CUDA_R_32F,
+                                           (int)ld, Bm, CUDA_R_32F, (int)ld, &one, Cm, CUDA_R_32F, (int)ld,
+                                           CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT);
+    if (cs != CUBLAS_STATUS_SUCCESS) {
+      set_error("o3g_bem_factor: cublasGemmEx (TF32 update) failed");
+      return O3G_ERR_CUDA;
     }
-    PanelArgs pa;
-    pa.A = h->LU; pa.ld = ld; pa.n = n; pa.k0 = k0; pa.jb = jb; pa.R = r;
-    pa.piv = h->piv; pa.cval = cval; pa.crow = crow; pa.crows = crows; pa.drow = drow;
-    pa.singular = h->flags + 1;
-    pa.bar = Barrier{(unsigned*)(h->flags + 2), (unsigned*)(h->flags + 3), h->flags};
-    void* args[] = {&pa};
-    const size_t sm = ((size_t)jb * r + jb + 32) * sizeof(float);
-    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_panel_lu, dim3(g), dim3(kPanelThreads), args, sm, st));
+    return O3G_OK;
+  };
+  auto trsm = [&](int k0, int jb, int c0, int ncols) {
+    if (ncols <= 0) return;
+    int tb = (ncols + 7) / 8;
+    if (tb > 4 * df.num_sms) tb = 4 * df.num_sms;
+    k_trsm_unit_lower<<<tb, 256, (size_t)jb * jb * sizeof(float), st>>>(h->LU + (size_t)k0 * ld + k0, ld, jb,
+                                                                         h->LU + (size_t)c0 * ld + k0, ld, ncols);
     note_launch();
-    if (n - jb > 0) {
-      k_laswp<<<(n - jb + 255) / 256, 256, 0, st>>>(h->LU, ld, n, k0, jb, h->piv);
-      note_launch();
+  };
+  // the same solve for a wide right-hand side: Linv = L11^-1 once (TRSM on the identity),
+  // then B <- Linv B as an FP32 GEMM through a scratch copy
+  float* linv = cv.take<float>((size_t)kNb * kNb);
+  float* tmp = cv.take<float>((size_t)kNb * n);
+  auto trsm_wide = [&](int k0, int jb, int c0, int ncols) -> int32_t {
+    if (ncols <= 0) return O3G_OK;
+    k_eye<<<(jb * jb + 255) / 256, 256, 0, st>>>(linv, jb);
+    k_trsm_unit_lower<<<(jb + 7) / 8, 256, (size_t)jb * jb * sizeof(float), st>>>(h->LU + (size_t)k0 * ld + k0, ld,
+                                                                                 jb, linv, jb, jb);
+    note_launch(2);
+    float* B = h->LU + (size_t)c0 * ld + k0;
+    O3G_CUDA_TRY(cudaMemcpy2DAsync(tmp, (size_t)jb * sizeof(float), B, ld * sizeof(float), (size_t)jb * sizeof(float),
+                                   ncols, cudaMemcpyDeviceToDevice, st));
+    const float zero = 0.f;
+    const cublasStatus_t cs = cublasGemmEx(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, jb, ncols, jb, &one, linv, CUDA_R_32F,
+                                           jb, tmp, CUDA_R_32F, jb, &zero, B, CUDA_R_32F, (int)ld,
+                                           CUBLAS_COMPUTE_32F_PEDANTIC, CUBLAS_GEMM_DEFAULT);
+    if (cs != CUBLAS_STATUS_SUCCESS) {
+      set_error("o3g_bem_factor: cublasGemmEx (triangular solve) failed");
+      return O3G_ERR_CUDA;
     }
-    const int rest = n - k0 - jb;
-    if (rest > 0) {
-      const size_t tsm = (size_t)jb * jb * sizeof(float);
-      O3G_CUDA_TRY(cudaFuncSetAttribute(k_trsm_unit_lower, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-      int tb = (rest + 7) / 8;
-      if (tb > 4 * df.num_sms) tb = 4 * df.num_sms;
-      k_trsm_unit_lower<<<tb, 256, tsm, st>>>(h->LU, ld, n, k0, jb);
+    return O3G_OK;
+  };
+  auto laswp = [&](int p0, int p1, int c0, int c1, int s0, int s1) {
+    const int cnt = (c1 - c0) - (s1 > s0 ? s1 - s0 : 0);
+    if (cnt <= 0) return;
+    const int lb = std::min((cnt + 7) / 8, 8 * df.num_sms);
+    k_laswp<<<lb, 256, 0, st>>>(h->LU, ld, n, p0, p1, h->piv, c0, c1, s0, s1);
+    note_launch();
+  };
+  auto at = [&](int r, int c) { return h->LU + (size_t)c * ld + r; };
+  // two-level right-looking LU: kNb-column panels inside kNbOuter-column outer panels; the
+  // big trailing update of each outer panel has k = kNbOuter
+  constexpr int kNbOuter = 512;
+  for (int K0 = 0; K0 < n; K0 += kNbOuter) {
+    const int KB = std::min(kNbOuter, n - K0), K1 = K0 + KB;
+    for (int k0 = K0; k0 < K1; k0 += kNb) {
+      const int jb = std::min(kNb, K1 - k0);
+      const int m = n - k0;
+      int g = G;
+      int r = (m + g - 1) / g;
+      if (r < 32) {   // short panels: fewer blocks
+        g = (m + 31) / 32;
+        r = (m + g - 1) / g;
+      }
+      PanelArgs pa;
+      pa.A = h->LU; pa.ld = ld; pa.n = n; pa.k0 = k0; pa.jb = jb; pa.R = r;
+      pa.piv = h->piv; pa.cval = cval; pa.crow = crow; pa.crows = crows; pa.drow = drow;
+      pa.singular = h->flags + 1;
+      pa.bar = Barrier{(unsigned*)(h->flags + 2), (unsigned*)(h->flags + 3), h->flags};
+      void* args[] = {&pa};
+      const size_t sm = ((size_t)jb * r + jb + 32) * sizeof(float);
+      O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_panel_lu, dim3(g), dim3(kPanelThreads), args, sm, st));
       note_launch();
-      float* A21 = h->LU + (size_t)k0 * ld + k0 + jb;
-      float* A12 = h->LU + (size_t)(k0 + jb) * ld + k0;
-      float* A22 = h->LU + (size_t)(k0 + jb) * ld + k0 + jb;
-      const cublasStatus_t cs = cublasGemmEx(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, rest, rest, jb, &minus1, A21,
-                                             CUDA_R_32F, (int)ld, A12, CUDA_R_32F, (int)ld, &one, A22, CUDA_R_32F,
-                                             (int)ld, CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT);
-      if (cs != CUBLAS_STATUS_SUCCESS) {
-        set_error("o3g_bem_factor: cublasGemmEx (TF32 trailing update) failed");
-        return O3G_ERR_CUDA;
+      // interchanges inside the outer panel; the other columns get them once per outer panel
+      laswp(k0, k0 + jb, K0, K1, k0, k0 + jb);
+      if (k0 + jb < K1) {
+        trsm(k0, jb, k0 + jb, K1 - k0 - jb);
+        O3G_TRY(gemm(n - k0 - jb, K1 - k0 - jb, jb, at(k0 + jb, k0), at(k0, k0 + jb), at(k0 + jb, k0 + jb)));
       }
     }
+    laswp(K0, K1, 0, n, K0, K1);
+    if (K1 < n) {
+      // U12 = L11^-1 A12 for the KB x KB unit lower L11, block by block
+      for (int k0 = K0; k0 < K1; k0 += kNb) {
+        const int jb = std::min(kNb, K1 - k0);
+        O3G_TRY(trsm_wide(k0, jb, K1, n - K1));
+        if (k0 + jb < K1) O3G_TRY(gemm(K1 - k0 - jb, n - K1, jb, at(k0 + jb, k0), at(k0, K1), at(k0 + jb, K1)));
+      }
+      O3G_TRY(gemm(n - K1, n - K1, KB, at(K1, K0), at(K0, K1), at(K1, K1)));
+    }
+  }
+  {
+    const size_t dsm = (size_t)kNb * kNb * sizeof(float);
+    O3G_CUDA_TRY(cudaFuncSetAttribute(k_diag_inverses, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    k_diag_inverses<<<(n + kNb - 1) / kNb, 256, dsm, st>>>(h->LU, ld, n, h->dinv);
+    note_launch();
   }
   tm.end(st);
   O3G_CUDA_TRY(cudaGetLastError());
@@ -699,7 +889,7 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   const long long ld = h->ld;
   DeviceFacts df;
   O3G_TRY(device_facts(&df));
-  const int cchunk = 2048;
+  const int cchunk = 1024;
   const int ncb = (n + cchunk - 1) / cchunk;
   const int nrb = (n + 255) / 256;
   const size_t need = align_up((size_t)n * 8) * 3 + align_up((size_t)n * 4) * 3 + align_up((size_t)ncb * n * 8) +
@@ -723,10 +913,11 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   // cooperative solve kernels: one block per SM
   int G = df.num_sms;
   int per_sm = 0;
-  O3G_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower, kSolveThreads, 0));
+  const size_t dsm = 0;
+  O3G_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower, kSolveThreads, dsm));
   if (per_sm < 1) return O3G_ERR_CUDA;
   TrsvArgs ta;
-  ta.LU = h->LU; ta.ld = ld; ta.n = n; ta.y = y;
+  ta.LU = h->LU; ta.dinv = h->dinv; ta.ld = ld; ta.n = n; ta.y = y;
   ta.bar = Barrier{(unsigned*)(h->flags + 2), (unsigned*)(h->flags + 3), h->flags};
   void* targs[] = {&ta};
   std::vector<double> hn(2 * (size_t)nrb);
@@ -752,8 +943,8 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
     rel = bnorm > 0.0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
     if (rel <= tol || it == max_iter) break;
     k_permute_to_float<<<nrb, 256, 0, st>>>(rd, h->perm, y, n);
-    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_lower, dim3(G), dim3(kSolveThreads), targs, 0, st));
-    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_upper, dim3(G), dim3(kSolveThreads), targs, 0, st));
+    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_lower, dim3(G), dim3(kSolveThreads), targs, dsm, st));
+    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_upper, dim3(G), dim3(kSolveThreads), targs, dsm, st));
     k_axpy_f2d<<<nrb, 256, 0, st>>>(xd, y, n);
     note_launch(4);
   }

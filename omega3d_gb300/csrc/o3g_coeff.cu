@@ -15,6 +15,8 @@
 // so the 2 or 3 unit strengths share one traversal: each leaf computes r3 and d once.
 #include "o3g_common.cuh"
 
+#include <algorithm>
+
 namespace o3g {
 
 constexpr int kCB = 128;                 // target panels per block == source panels per tile
@@ -144,6 +146,12 @@ __global__ void k_pack_src_panels(int np, const float* __restrict__ x, const flo
   tri[j] = t;
 }
 
+struct NearList {
+  uint2* pairs;        // (target i, source j) of pairs that need subdivision
+  unsigned* count;
+  unsigned cap;        // 0: subdivide in the thread that found the pair
+};
+
 template <int NUNK>
 __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, const TriG* __restrict__ stri, int snp,
                                                const TriG* __restrict__ ttri, const float* __restrict__ tarea,
@@ -152,7 +160,7 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
                                                const float* __restrict__ t2y, const float* __restrict__ t2z,
                                                const float* __restrict__ tnx, const float* __restrict__ tny,
                                                const float* __restrict__ tnz, int tnp, int is_self, int maxlev,
-                                               float* __restrict__ coeff, long long ld) {
+                                               float* __restrict__ coeff, long long ld, NearList nl) {
   __shared__ SrcRec sr[kCB];
   const int i = blockIdx.x * kCB + threadIdx.x;
   const int j0 = blockIdx.y * kCB;
@@ -193,6 +201,13 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
     if (maxlev == 0 || dist_rn3(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z) > thr) {
       leaf3<NUNK>(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, u);
     } else {
+      if (nl.cap > 0) {
+        const unsigned slot = atomicAdd(nl.count, 1u);
+        if (slot < nl.cap) {
+          nl.pairs[slot] = make_uint2((unsigned)i, (unsigned)j);
+          continue;   // written by k_coeff_near
+        }
+      }
       pair_subdivide<NUNK>(stri[j], tt, s.s1.w, ta, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, maxlev,
                            u);
     }
@@ -201,6 +216,96 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
 #pragma unroll
       for (int l = 0; l < NUNK; ++l)
         col[(size_t)k * ld + l] = (u[k][0] * b[l][0] + u[k][1] * b[l][1] + u[k][2] * b[l][2]) * fac;
+  }
+}
+
+// One warp per listed pair (maxlev <= 3): the subdivision tree is expanded level by level.
+// Level 1 has 16 child pairs (source child a outer, target child b inner, one lane each);
+// every child pair that is neither well separated nor at maxlev contributes 16 pairs to the
+// next level, kept in a per-warp list in shared memory in enumeration order.  Leaves are
+// summed per lane and reduced across the warp in a fixed order.
+constexpr int kNearWarps = 4;
+template <int NUNK>
+__global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __restrict__ srec,
+                                                               const TriG* __restrict__ stri,
+                                                               const TriG* __restrict__ ttri,
+                                                               const float* __restrict__ tarea,
+                                                               const float* __restrict__ t1x,
+                                                               const float* __restrict__ t1y,
+                                                               const float* __restrict__ t1z,
+                                                               const float* __restrict__ t2x,
+                                                               const float* __restrict__ t2y,
+                                                               const float* __restrict__ t2z,
+                                                               const float* __restrict__ tnx,
+                                                               const float* __restrict__ tny,
+                                                               const float* __restrict__ tnz, int maxlev,
+                                                               float* __restrict__ coeff, long long ld, NearList nl) {
+  __shared__ unsigned lst[kNearWarps][2][256];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned total = min(*nl.count, nl.cap);
+  const float fac = (float)(1.0 / (4.0 * 3.14159265358979323846));
+  for (unsigned p = blockIdx.x * kNearWarps + warp; p < total; p += gridDim.x * kNearWarps) {
+    const uint2 ij = nl.pairs[p];
+    const int i = (int)ij.x, j = (int)ij.y;
+    const SrcRec s = srec[j];
+    const TriG S0 = stri[j], T0 = ttri[i];
+    const float sa = s.s1.w, ta = tarea[i];
+    float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    // level L items: (parent index in the level L-1 list, child 0..15); codes keep the
+    // source path in bits 0..7 and the target path in bits 8..15 (2 bits per level)
+    int nparent = 1;
+    for (int lev = 1; lev <= maxlev; ++lev) {
+      const int nitems = nparent * 16;
+      const int cur = lev & 1, prev = cur ^ 1;
+      int nnext = 0;
+      const float f4 = __int_as_float((127 - 2 * lev) << 23);
+      for (int base = 0; base < nitems; base += 32) {
+        const int k = base + lane;
+        bool expand = false;
+        unsigned code = 0;
+        if (k < nitems) {
+          const unsigned pc = lev == 1 ? 0u : lst[warp][prev][k >> 4];
+          const unsigned a = (unsigned)((k & 15) >> 2), b = (unsigned)(k & 3);
+          const unsigned sp = (pc & 0xffu) | (a << (2 * (lev - 1)));
+          const unsigned tp = ((pc >> 8) & 0xffu) | (b << (2 * (lev - 1)));
+          code = sp | (tp << 8);
+          const TriG S = descend(S0, sp, lev), T = descend(T0, tp, lev);
+          float scx, scy, scz, tcx, tcy, tcz;
+          cen(S, scx, scy, scz);
+          cen(T, tcx, tcy, tcz);
+          const float thr = __fmul_rn(__fadd_rn(__fsqrt_rn(sa * f4), __fsqrt_rn(ta * f4)), 4.0f);
+          if (lev >= maxlev || dist_rn3(tcx, tcy, tcz, scx, scy, scz) > thr) {
+            const float f = f4 * f4;
+            leaf3<NUNK>(tcx, tcy, tcz, scx, scy, scz, s.s1.x * f, s.s1.y * f, s.s1.z * f, s.s2.x * f, s.s2.y * f,
+                        s.s2.z * f, s.s1.w * f, u);
+          } else {
+            expand = true;
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, expand);
+        if (expand) lst[warp][cur][nnext + __popc(m & ((1u << lane) - 1u))] = code;
+        nnext += __popc(m);
+      }
+      __syncwarp();
+      nparent = nnext;
+      if (nparent == 0) break;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) u[k][c] += __shfl_xor_sync(0xffffffffu, u[k][c], o);
+    if (lane < NUNK * NUNK) {
+      const int k = lane / NUNK, l = lane % NUNK;
+      float bx, by, bz;
+      if (l == 0) { bx = t1x[i]; by = t1y[i]; bz = t1z[i]; }
+      else if (l == 1) { bx = t2x[i]; by = t2y[i]; bz = t2z[i]; }
+      else { bx = tnx[i]; by = tny[i]; bz = tnz[i]; }
+      float* col = coeff + (size_t)j * NUNK * (size_t)ld + (size_t)i * NUNK;
+      col[(size_t)k * ld + l] = (u[k][0] * bx + u[k][1] * by + u[k][2] * bz) * fac;
+    }
+    __syncwarp();
   }
 }
 
@@ -246,14 +351,22 @@ extern "C" int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int3
   cudaStream_t st = (cudaStream_t)stream;
   const int snp = src->np, tnp = targ->np;
   const int sblocks = (snp + kCB - 1) / kCB, snp_pad = sblocks * kCB;
+  // near-pair list for the warp-cooperative subdivision (maxlev <= 3; deeper trees stay in-thread)
+  const unsigned cap = maxlev <= 3 ? (unsigned)std::min<long long>((long long)snp * tnp, 512LL * (tnp > snp ? tnp : snp))
+                                   : 0u;
   size_t bytes = align_up((size_t)snp_pad * sizeof(SrcRec)) + align_up((size_t)snp_pad * sizeof(TriG)) +
-                 align_up((size_t)tnp * sizeof(TriG));
+                 align_up((size_t)tnp * sizeof(TriG)) + align_up(sizeof(unsigned)) + align_up((size_t)cap * 8);
   Workspace* ws = nullptr;
   O3G_TRY(workspace_get(st, bytes, &ws));
   Carve cv(ws->base);
   SrcRec* srec = cv.take<SrcRec>(snp_pad);
   TriG* stri = cv.take<TriG>(snp_pad);
   TriG* ttri = cv.take<TriG>(tnp);
+  NearList nl;
+  nl.count = cv.take<unsigned>(1);
+  nl.pairs = cv.take<uint2>(cap > 0 ? cap : 1);
+  nl.cap = cap;
+  O3G_CUDA_TRY(cudaMemsetAsync(nl.count, 0, sizeof(unsigned), st));
   k_pack_src_panels<<<(snp_pad + 255) / 256, 256, 0, st>>>(snp, src->x, src->y, src->z, src->idx, src->area, src->x1x,
                                                           src->x1y, src->x1z, src->x2x, src->x2y, src->x2z, snp_pad,
                                                           srec, stri);
@@ -262,14 +375,25 @@ extern "C" int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int3
   dim3 grid((tnp + kCB - 1) / kCB, sblocks);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
-  if (nunk == 2)
+  const int nearblocks = 8 * df.num_sms;
+  if (nunk == 2) {
     k_coeff<2><<<grid, kCB, 0, st>>>(srec, stri, snp, ttri, targ->area, targ->x1x, targ->x1y, targ->x1z, targ->x2x,
-                                     targ->x2y, targ->x2z, nullptr, nullptr, nullptr, tnp, is_self, maxlev, coeffs, ld);
-  else
+                                     targ->x2y, targ->x2z, nullptr, nullptr, nullptr, tnp, is_self, maxlev, coeffs, ld,
+                                     nl);
+    if (cap > 0)
+      k_coeff_near<2><<<nearblocks, 32 * kNearWarps, 0, st>>>(srec, stri, ttri, targ->area, targ->x1x, targ->x1y,
+                                                              targ->x1z, targ->x2x, targ->x2y, targ->x2z, nullptr,
+                                                              nullptr, nullptr, maxlev, coeffs, ld, nl);
+  } else {
     k_coeff<3><<<grid, kCB, 0, st>>>(srec, stri, snp, ttri, targ->area, targ->x1x, targ->x1y, targ->x1z, targ->x2x,
                                      targ->x2y, targ->x2z, targ->nx, targ->ny, targ->nz, tnp, is_self, maxlev, coeffs,
-                                     ld);
-  note_launch();
+                                     ld, nl);
+    if (cap > 0)
+      k_coeff_near<3><<<nearblocks, 32 * kNearWarps, 0, st>>>(srec, stri, ttri, targ->area, targ->x1x, targ->x1y,
+                                                              targ->x1z, targ->x2x, targ->x2y, targ->x2z, targ->nx,
+                                                              targ->ny, targ->nz, maxlev, coeffs, ld, nl);
+  }
+  note_launch(cap > 0 ? 2 : 1);
   tm.end(st);
   O3G_CUDA_TRY(cudaGetLastError());
   return O3G_OK;
