@@ -206,6 +206,33 @@ int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double* x64, int32
 int32_t o3g_panel_vels_to_rhs(int32_t np, int32_t nunk, const double* fs, float* pu, float* pv, float* pw,
                               const o3g_surface_t* surf, float* rhs, void* stream);
 
+/* ---- convection: finalize_vels, moves, Ralston RK2 ------------------------------------------
+ * Device arrays; u/s/x are arrays of 3 component pointers, ug of 9.  The element-wise
+ * kernels reproduce the reference's float/double arithmetic exactly. */
+/* finalize_vels, ElementBase.h:187-193 + Points.h:265-277: u = fs + u/(4 pi), ug *= 1/(4 pi) */
+int32_t o3g_points_finalize(int32_t n, const double* fs, float* const* u, float* const* ug, void* stream);
+/* Points::move first order, ElementBase.h:253-273 + Points.h:288-351: x += dt*wt1*u and, when
+ * s, elong and ug are given, vortex stretching of s and elong */
+int32_t o3g_points_move_euler(int32_t n, double dt, double wt1, float* const* x, float* const* s, float* elong,
+                              float* const* u, float* const* ug, void* stream);
+/* Points::move second order, ElementBase.h:276-304 + Points.h:356-439: u1 <- wt1 u1 + wt2 u2,
+ * x += dt u1, stretching with wt1 ug1 + wt2 ug2 applied to the stage-0 strengths */
+int32_t o3g_points_move_rk2(int32_t n, double dt, double wt1, float* const* u1, float* const* ug1, double wt2,
+                            float* const* u2, float* const* ug2, float* const* x, float* const* s, float* elong,
+                            void* stream);
+/* Convection::advect_2nd_ralston (Convection.h:349-425) for a boundary-free set of n vortex
+ * particles (x, s, r, elong: the caller's device arrays, advanced in place) and nf field points
+ * (fx, may be 0): per step two vel+grad evaluations (core, prec PLAIN or COMPENSATED), the
+ * 2/3 dt interim move and the 0.25/0.75 combine.  With use_graph != 0 the first step runs
+ * directly and the step is then captured into a CUDA graph and replayed (stream must then be
+ * a non-default stream).  o3g_rk2_velocities gives the stage-1 velocities of the last step. */
+typedef struct o3g_rk2 o3g_rk2_t;
+int32_t o3g_rk2_create(int32_t core, int32_t prec, int32_t n, float* const* x, float* const* s, float* r,
+                       float* elong, int32_t nf, float* const* fx, int32_t use_graph, o3g_rk2_t** h);
+int32_t o3g_rk2_step(o3g_rk2_t* h, double dt, const double* fs, int32_t nsteps, void* stream);
+int32_t o3g_rk2_velocities(o3g_rk2_t* h, float** u, float** ug);
+int32_t o3g_rk2_destroy(o3g_rk2_t* h);
+
 /* ---- points_affect_points without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory
  * after start-up (applications that give all device memory to their own pool, real-time

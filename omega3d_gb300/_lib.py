@@ -100,6 +100,20 @@ def _declare(l):
     l.o3g_bem_solve.argtypes = [P, P, P, P, c_i32, c_d, c_i32, P, P, P]
     l.o3g_panel_vels_to_rhs.restype = c_i32
     l.o3g_panel_vels_to_rhs.argtypes = [c_i32, c_i32, P, P, P, P, P, P, P]
+    l.o3g_points_finalize.restype = c_i32
+    l.o3g_points_finalize.argtypes = [c_i32, P, P, P, P]
+    l.o3g_points_move_euler.restype = c_i32
+    l.o3g_points_move_euler.argtypes = [c_i32, c_d, c_d, P, P, P, P, P, P]
+    l.o3g_points_move_rk2.restype = c_i32
+    l.o3g_points_move_rk2.argtypes = [c_i32, c_d, c_d, P, P, c_d, P, P, P, P, P, P]
+    l.o3g_rk2_create.restype = c_i32
+    l.o3g_rk2_create.argtypes = [c_i32, c_i32, c_i32, P, P, P, P, c_i32, P, c_i32, P]
+    l.o3g_rk2_step.restype = c_i32
+    l.o3g_rk2_step.argtypes = [P, c_d, P, c_i32, P]
+    l.o3g_rk2_velocities.restype = c_i32
+    l.o3g_rk2_velocities.argtypes = [P, P, P]
+    l.o3g_rk2_destroy.restype = c_i32
+    l.o3g_rk2_destroy.argtypes = [P]
     l.o3g_points_affect_points_noalloc.restype = c_i32
     l.o3g_points_affect_points_noalloc.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
     l.o3g_points_affect_points_d.restype = c_i32

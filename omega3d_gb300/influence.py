@@ -426,3 +426,51 @@ def solve_bem(fs, vort, bdry, bem, env=None, maxlev=3, tol=1e-10, max_iter=30):
     bdry.set_sheet_strengths(xs[0::nunk], xs[1::nunk], xs[2::nunk] if nunk == 3 else None)
     bem.strengths = xs
     return xs
+
+
+# ------------------------------------------------------------------------------------
+# convection
+
+def _ptrs(t, k):
+    return (ctypes.c_void_p * k)(*_rows(t, k))
+
+
+class Ralston:
+    """Convection::advect_2nd_ralston (Convection.h:349-425) for a boundary-free set of
+    vortex particles held in torch CUDA tensors x[3,n], s[3,n], r[n], elong[n] (advanced in
+    place) and optional field points f[3,nf].  Each step: two vel+grad evaluations, the
+    2/3 dt interim Euler move with stretching, and the 0.25/0.75 combine.  Steps after the
+    first replay a captured CUDA graph."""
+
+    def __init__(self, x, s, r, elong, fieldpts=None, env=None, use_graph=True):
+        env = env or ExecEnv()
+        self.x, self.s, self.r, self.elong, self.f = x, s, r, elong, fieldpts
+        self.stream = torch.cuda.Stream(device=x.device) if use_graph else torch.cuda.current_stream(x.device)
+        h = ctypes.c_void_p()
+        nf = 0 if fieldpts is None else fieldpts.shape[1]
+        L.check(L.lib().o3g_rk2_create(L.CORES[env.core], L.PRECS[env.precision], x.shape[1], _ptrs(x, 3),
+                                       _ptrs(s, 3), _base(r), _base(elong), nf,
+                                       _ptrs(fieldpts, 3) if nf else None, int(use_graph), ctypes.byref(h)),
+                "o3g_rk2_create")
+        self.h = h
+
+    def step(self, dt, fs=(0.0, 0.0, 0.0), nsteps=1):
+        fsd = (ctypes.c_double * 3)(*fs)
+        self.stream.wait_stream(torch.cuda.current_stream(self.x.device))
+        L.check(L.lib().o3g_rk2_step(self.h, dt, fsd, nsteps, self.stream.cuda_stream), "o3g_rk2_step")
+        torch.cuda.current_stream(self.x.device).wait_stream(self.stream)
+
+    def velocities(self):
+        """Stage-1 velocity and gradient device pointers of the last step (u[3], ug[9])."""
+        u = (ctypes.c_void_p * 3)()
+        g = (ctypes.c_void_p * 9)()
+        L.check(L.lib().o3g_rk2_velocities(self.h, u, g), "o3g_rk2_velocities")
+        return list(u), list(g)
+
+    def __del__(self):
+        try:
+            if self.h:
+                L.lib().o3g_rk2_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
