@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--skip-bem", action="store_true")
     ap.add_argument("--skip-bem-fp64", action="store_true", help="skip the FP64 LU comparator (~50 s)")
     ap.add_argument("--skip-ring", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
     return ap.parse_args()
 
 
@@ -256,6 +257,153 @@ def bench_ring(args, G, torch, W):
             "rk2_steps": 10, "dt": 0.01, "graph": True}
 
 
+def bench_batch(args, G, torch, W, flush):
+    """Batching: 64 independent particle systems (sizes log-uniform in [1,024, 65,536], seed 4),
+    each a Gaussian blob with 4,096 field points on a jittered grid; Gaussian core; velocity +
+    gradient of every system in ONE persistent launch with the autotuned configuration (the
+    first run tunes and caches it; reported separately), L2 flushed before every timed run.
+    Compared with one points_affect_points call per (system, target set) and, for errors,
+    with the FP64 path on the same GPU for every 8th system.  Then 100 Ralston steps of all
+    systems replayed from a CUDA graph (each step: two batched evaluations)."""
+    import ctypes
+    from omega3d_gb300 import _lib as L
+    from omega3d_gb300.metrics import linf_err, rel_err
+    lib = L.lib()
+    syst = W.batch_systems(64, seed=4)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    z = lambda *sh: torch.zeros(*sh, device="cuda")  # noqa: E731
+    npart = sum(q[0].shape[1] for q in syst)
+    nfld = sum(q[3].shape[1] for q in syst)
+    pairs = float(sum(q[0].shape[1] * (q[0].shape[1] + q[3].shape[1]) for q in syst))
+    out = {"systems": len(syst), "particles": npart, "field_points": nfld, "interactions_per_eval": pairs,
+           "core": "gauss", "l2": "flushed before every timed evaluation"}
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def make():
+        return [G.BatchSystem(t(x), t(s), t(r), z(3, x.shape[1]), z(9, x.shape[1]), t(f), z(3, f.shape[1]),
+                              z(9, f.shape[1])) for x, s, r, f in syst]
+
+    results = {}
+    for core, prec in (("gauss", "compensated"), ("gauss", "plain"), ("rm", "compensated"), ("rm", "plain")):
+        devs = make()
+        b = G.Batch(devs, G.ExecEnv(core, prec))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run()
+        torch.cuda.synchronize()
+        first_s = time.perf_counter() - t0
+        for _ in range(2):
+            b.run()
+        lib.o3g_set_timing(1)
+        run_ms, kern_ms = [], []
+        n0 = L.launch_count()
+        reps = 5
+        for _ in range(reps):
+            flush.fill_(1)
+            e0, e1 = ev(), ev()
+            e0.record()
+            b.run()
+            e1.record()
+            e1.synchronize()
+            run_ms.append(e0.elapsed_time(e1))
+            km = ctypes.c_float(0)
+            L.check(lib.o3g_last_kernel_ms(ctypes.byref(km)), "o3g_last_kernel_ms")
+            kern_ms.append(float(km.value))
+        launches = (L.launch_count() - n0) / reps
+        lib.o3g_set_timing(0)
+        for d in devs:
+            for a in (d.u, d.ug, d.fu, d.fug):
+                a.zero_()
+        b.run()
+        torch.cuda.synchronize()
+        results[(core, prec)] = devs
+        rm, km = statistics.median(run_ms), statistics.median(kern_ms)
+        out.setdefault(core, {})[prec] = {
+            "value": pairs / (rm * 1e-3), "unit": UNIT, "run_ms": rm, "persistent_kernel_ms": km,
+            "kernel_interactions_per_s": pairs / (km * 1e-3), "launches_per_run": launches,
+            "first_run_s_incl_tuning": first_s, "config": b.config()}
+        del b
+    for core in ("gauss", "rm"):
+        out[core]["compensated_over_plain"] = out[core]["plain"]["run_ms"] / out[core]["compensated"]["run_ms"]
+
+    # one call per (system, target set): the unbatched way through the same library
+    pts = [(G.Points(q.x, q.s, q.r), G.Points(q.f, None, None, inert=True)) for q in make()]
+    for _ in range(2):
+        for p, f in pts:
+            p.zero_vels()
+            f.zero_vels()
+            G.points_affect_points(p, p, G.ResultsType(), G.ExecEnv("gauss", "compensated"))
+            G.points_affect_points(p, f, G.ResultsType(), G.ExecEnv("gauss", "compensated"))
+    loop_ms = []
+    for _ in range(3):
+        flush.fill_(1)
+        e0, e1 = ev(), ev()
+        e0.record()
+        for p, f in pts:
+            G.points_affect_points(p, p, G.ResultsType(), G.ExecEnv("gauss", "compensated"))
+            G.points_affect_points(p, f, G.ResultsType(), G.ExecEnv("gauss", "compensated"))
+        e1.record()
+        e1.synchronize()
+        loop_ms.append(e0.elapsed_time(e1))
+    lm = statistics.median(loop_ms)
+    out["per_system_calls"] = {"value": pairs / (lm * 1e-3), "unit": UNIT, "ms": lm, "calls": 2 * len(syst),
+                               "core": "gauss", "precision": "compensated"}
+    out["batched_over_per_system_calls"] = lm / out["gauss"]["compensated"]["run_ms"]
+    del pts
+
+    # errors against the FP64 path on the same GPU, every 8th system
+    errs = {}
+    for core, prec in results:
+        mu = mg = 0.0
+        su = sg = 0.0
+        cnt = 0
+        lu = lg = 0.0
+        for k in range(0, len(syst), 8):
+            x, s, r, f = syst[k]
+            d = results[(core, prec)][k]
+            src = G.Points(t(x.astype(np.float64)), t(s.astype(np.float64)), t(r.astype(np.float64)))
+            for tx, tr, u, g in ((x, r, d.u, d.ug), (f, None, d.fu, d.fug)):
+                tq = G.Points(t(tx.astype(np.float64)), None, None if tr is None else t(tr.astype(np.float64)),
+                              inert=tr is None)
+                G.points_affect_points(src, tq, G.ResultsType(), G.ExecEnv(core, "fp64"))
+                u64, g64 = tq.u.cpu().numpy(), tq.ug.cpu().numpy()
+                eu, eg = rel_err(u.cpu().numpy(), u64), rel_err(g.cpu().numpy(), g64)
+                mu, mg = max(mu, eu[0]), max(mg, eg[0])
+                su, sg, cnt = su + eu[1] ** 2, sg + eg[1] ** 2, cnt + 1
+                lu = max(lu, linf_err(u.cpu().numpy(), u64))
+                lg = max(lg, linf_err(g.cpu().numpy(), g64))
+        errs["%s_%s" % (core, prec)] = {"u_max": mu, "u_rms": (su / cnt) ** 0.5, "grad_max": mg, "grad_rms": (sg / cnt) ** 0.5,
+                      "u_linf": lu, "grad_linf": lg, "systems_checked": cnt // 2}
+    out["errors_vs_fp64"] = errs
+    # time step from the initial velocity gradients (dt * max |grad u| = 0.05): random-strength
+    # blobs stretch their particles at a rate set by the largest gradient
+    gmax = max(float(torch.linalg.norm(d.ug, dim=0).max().item()) for d in results[("gauss", "compensated")])
+    dt = 0.05 / (gmax / (4 * np.pi))
+    del results
+
+    # 100 Ralston steps of all systems under a CUDA graph
+    X = t(np.concatenate([q[0] for q in syst], axis=1))
+    S = t(np.concatenate([q[1] for q in syst], axis=1))
+    R = t(np.concatenate([q[2] for q in syst]))
+    F = t(np.concatenate([q[3] for q in syst], axis=1))
+    E = torch.ones(npart, device="cuda")
+    rk = G.BatchRalston([q[0].shape[1] for q in syst], [q[3].shape[1] for q in syst], X, S, R, E, F,
+                        G.ExecEnv("gauss", "compensated"))
+    rk.step(dt, (0.0, 0.0, 0.0), 2)                 # direct step (sizes workspaces) + capture
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record(rk.stream)
+    rk.step(dt, (0.0, 0.0, 0.0), 100)
+    e1.record(rk.stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out["rk2"] = {"steps": 100, "dt": dt, "core": "gauss", "precision": "compensated", "graph": True, "total_ms": ms,
+                  "step_ms": ms / 100, "interactions_per_s": 2 * pairs * 100 / (ms * 1e-3),
+                  "finite": bool(torch.isfinite(X).all().item())}
+    del rk
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -410,6 +558,9 @@ def run_ours(args):
     ring = None
     if not args.skip_ring:
         ring = bench_ring(args, G, torch, W)
+    batch = None
+    if not args.skip_batch:
+        batch = bench_batch(args, G, torch, W, flush)
 
     if rank == 0:
         cpu_v, cpu_cores, cpu_sample, _ = cpu_reference(args)
@@ -437,7 +588,7 @@ def run_ours(args):
             "fp64_same_gpu": fp64 and {"value": fp64["value"], "unit": UNIT, "targets": fp64["targets"],
                                        "compensated_speedup": local_rate / fp64["value"]},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_sample},
-            "bem_solve": bem, "ring_rk2": ring,
+            "bem_solve": bem, "ring_rk2": ring, "batch": batch,
             "clocks": clk, "gpu_launches": comp_launches, "num_sms": nsm,
             "wall_s_timed_region": comp_wall,
         }

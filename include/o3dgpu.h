@@ -233,6 +233,69 @@ int32_t o3g_rk2_step(o3g_rk2_t* h, double dt, const double* fs, int32_t nsteps, 
 int32_t o3g_rk2_velocities(o3g_rk2_t* h, float** u, float** ug);
 int32_t o3g_rk2_destroy(o3g_rk2_t* h);
 
+/* ---- many independent particle systems in one launch ----------------------------------
+ * No counterpart in the reference, which runs points_affect_points once per (source
+ * collection, target collection) pair (Convection.h:144-172).  Each system's particles are
+ * the sources and the thick-cored targets of that system only; its field points are
+ * further targets (no radius).  Sums ACCUMULATE (+=) like o3g_points_affect_points.
+ * All arrays are device arrays.  precision PLAIN or COMPENSATED; grads != 0 needs ug (and
+ * fug when nf > 0); grads == 0 computes velocities only. */
+typedef struct {
+  int32_t np;                        /* particles                                           */
+  const float *x, *y, *z, *r;        /* positions and core radii                            */
+  const float *sx, *sy, *sz;         /* strengths                                           */
+  float *u, *v, *w;                  /* particle velocity sums (+=)                         */
+  float* ug[9];                      /* particle gradient sums (+=)                         */
+  int32_t nf;                        /* field points (may be 0)                             */
+  const float *fx, *fy, *fz;
+  float *fu, *fv, *fw;
+  float* fug[9];
+} o3g_system_t;
+
+/* The batch handle: packed copies of the systems (Morton-ordered per system for the
+ * Gaussian and exponential cores), a plan of (target block, source-tile range) work items
+ * drained by ONE persistent kernel launch, and its tuned configuration.  The descriptor
+ * pointers are fixed at creation; their contents may change between runs. */
+typedef struct o3g_batch o3g_batch_t;
+int32_t o3g_batch_create(int32_t core, int32_t prec, int32_t grads, int32_t nsys, const o3g_system_t* systems,
+                         o3g_batch_t** h);
+/* Queues one evaluation on `stream`.  When the shape -- (core, precision, grads, SM count,
+ * every system's (np, nf)) -- has no cached configuration and the stream is not capturing,
+ * the first run first times the candidate configurations (targets per thread, work-item
+ * size, blocks per SM) on this data, caches the fastest (in the process and in the text
+ * file $O3G_TUNE_CACHE, default ~/.cache/o3dgpu/batch_tune.txt) and synchronises the
+ * stream.  O3G_BATCH_TUNE=0 disables tuning.  Capturable into a graph once tuned. */
+int32_t o3g_batch_run(o3g_batch_t* h, void* stream);
+/* Retunes now (synchronous). */
+int32_t o3g_batch_tune(o3g_batch_t* h, void* stream);
+/* Forces a configuration: tpt in {1, 2, 4} ({1, 2} for compensated with gradients),
+ * blocks_per_sm (0 = full occupancy), split in {0, 4, 16}.  Synchronises the device. */
+int32_t o3g_batch_set_config(o3g_batch_t* h, int32_t tpt, int32_t blocks_per_sm, int32_t split);
+/* Current configuration: targets per thread, grid size (blocks), split, largest item in
+ * source tiles, number of work items, and whether it was tuned (or set / cached). */
+int32_t o3g_batch_get_config(const o3g_batch_t* h, int32_t* tpt, int32_t* grid, int32_t* split, int32_t* chunk,
+                             int32_t* nitems, int32_t* tuned);
+int32_t o3g_batch_destroy(o3g_batch_t* h);
+/* One-shot: create, run, synchronise `stream`, destroy. */
+int32_t o3g_batch_velgrad(int32_t core, int32_t prec, int32_t grads, int32_t nsys, const o3g_system_t* systems,
+                          void* stream);
+/* Host only (no device needed): the work-item plan for per-system counts np, nf at tpt
+ * targets per thread, `grid` resident blocks and `split`: counts of items and target blocks,
+ * the largest item in source tiles and the partial-sum slabs.  When not NULL, items receives
+ * {target block, first tile, end tile, split index} and tbs {system, first target slot,
+ * first slab or -1, number of splits}, 4 int32 each, items longest first. */
+int32_t o3g_batch_plan(int32_t nsys, const int32_t* np, const int32_t* nf, int32_t tpt, int32_t grid, int32_t split,
+                       int32_t* nitems, int32_t* ntbs, int32_t* chunk, int64_t* nslabs, int32_t* items,
+                       int32_t* tbs);
+/* Ralston RK2 (as o3g_rk2_create) of nsys independent systems stored back to back in the
+ * device arrays x, s, r, elong (system i: particles [P_i, P_i + np[i]), P_i = sum of the
+ * earlier np) and fx (field points, likewise by nf).  Both velocity evaluations of a step
+ * are one batched persistent launch each.  Step, read and destroy with o3g_rk2_step,
+ * o3g_rk2_velocities, o3g_rk2_destroy. */
+int32_t o3g_batch_rk2_create(int32_t core, int32_t prec, int32_t nsys, const int32_t* np, const int32_t* nf,
+                             float* const* x, float* const* s, float* r, float* elong, float* const* fx,
+                             int32_t use_graph, o3g_rk2_t** h);
+
 /* ---- points_affect_points without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory
  * after start-up (applications that give all device memory to their own pool, real-time

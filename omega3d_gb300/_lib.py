@@ -50,6 +50,15 @@ class Surface(ctypes.Structure):
                 ("nx", ctypes.c_void_p), ("ny", ctypes.c_void_p), ("nz", ctypes.c_void_p)]
 
 
+class System(ctypes.Structure):
+    """o3g_system_t (include/o3dgpu.h): one independent particle system of a batch."""
+    _fields_ = [("np", ctypes.c_int32), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("r", ctypes.c_void_p), ("sx", ctypes.c_void_p), ("sy", ctypes.c_void_p), ("sz", ctypes.c_void_p),
+                ("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("w", ctypes.c_void_p), ("ug", ctypes.c_void_p * 9),
+                ("nf", ctypes.c_int32), ("fx", ctypes.c_void_p), ("fy", ctypes.c_void_p), ("fz", ctypes.c_void_p),
+                ("fu", ctypes.c_void_p), ("fv", ctypes.c_void_p), ("fw", ctypes.c_void_p), ("fug", ctypes.c_void_p * 9)]
+
+
 def _declare(l):
     P = c_vp
     l.o3g_status_string.restype = ctypes.c_char_p
@@ -116,6 +125,24 @@ def _declare(l):
     l.o3g_rk2_destroy.argtypes = [P]
     l.o3g_points_affect_points_noalloc.restype = c_i32
     l.o3g_points_affect_points_noalloc.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
+    l.o3g_batch_create.restype = c_i32
+    l.o3g_batch_create.argtypes = [c_i32, c_i32, c_i32, c_i32, P, P]
+    l.o3g_batch_run.restype = c_i32
+    l.o3g_batch_run.argtypes = [P, P]
+    l.o3g_batch_tune.restype = c_i32
+    l.o3g_batch_tune.argtypes = [P, P]
+    l.o3g_batch_set_config.restype = c_i32
+    l.o3g_batch_set_config.argtypes = [P, c_i32, c_i32, c_i32]
+    l.o3g_batch_get_config.restype = c_i32
+    l.o3g_batch_get_config.argtypes = [P, P, P, P, P, P, P]
+    l.o3g_batch_destroy.restype = c_i32
+    l.o3g_batch_destroy.argtypes = [P]
+    l.o3g_batch_velgrad.restype = c_i32
+    l.o3g_batch_velgrad.argtypes = [c_i32, c_i32, c_i32, c_i32, P, P]
+    l.o3g_batch_plan.restype = c_i32
+    l.o3g_batch_plan.argtypes = [c_i32, P, P, c_i32, c_i32, c_i32, P, P, P, P, P, P]
+    l.o3g_batch_rk2_create.restype = c_i32
+    l.o3g_batch_rk2_create.argtypes = [c_i32, c_i32, c_i32, P, P, P, P, P, P, P, c_i32, P]
     l.o3g_points_affect_points_d.restype = c_i32
     l.o3g_points_affect_points_d.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
 

@@ -9,9 +9,10 @@
 //   zero -> pair sums (vel+grad) -> finalize -> Euler move to t + 2dt/3 ->
 //   zero -> pair sums at the interim state -> finalize -> 0.25/0.75 combine + stretch
 // and is captured once into a CUDA graph that later steps replay (o3g_rk2_step).
-#include "o3g_pair_impl.cuh"
+#include "o3g_batch.cuh"
 
 #include <cstring>
+#include <vector>
 
 namespace o3g {
 
@@ -209,19 +210,32 @@ struct o3g_rk2 {
   bool use_graph = true;
   bool warmed = false;
   cudaStream_t warm_stream = nullptr;   // stream whose workspace the warm-up step sized
+  size_t na = 0, fa = 0;                // bytes per particle / field-point component array
+  o3g_batch_t* batch = nullptr;         // many independent systems: one plan, bindings 0 (x) and 1 (xi)
 };
+
+// velocities and gradients (zeroed first) of stage 0 (state x, s -> u1, fu1) or stage 1
+// (interim state xi, si -> u2, fu2); the 3 + 9 component arrays of a stage are contiguous
+static int32_t rk2_eval(o3g_rk2_t* h, int stage, cudaStream_t st) {
+  const int n = h->n, nf = h->nf;
+  float** u = stage == 0 ? h->u1 : h->u2;
+  float** ug = stage == 0 ? h->ug1 : h->ug2;
+  float** fu = stage == 0 ? h->fu1 : h->fu2;
+  float** fug = stage == 0 ? h->fug1 : h->fug2;
+  O3G_CUDA_TRY(cudaMemsetAsync(u[0], 0, 12 * h->na, st));
+  if (nf > 0) O3G_CUDA_TRY(cudaMemsetAsync(fu[0], 0, 12 * h->fa, st));
+  if (h->batch) return batch_run(h->batch, stage, st);
+  float** x = stage == 0 ? h->x : h->xi;
+  float** s = stage == 0 ? h->s : h->si;
+  float** f = stage == 0 ? h->f : h->fxi;
+  O3G_TRY(ptpt_dev(h->core, h->prec, n, x, h->r, s, n, x, h->r, u, ug, st));
+  if (nf > 0) O3G_TRY(ptpt_dev(h->core, h->prec, n, x, h->r, s, nf, f, nullptr, fu, fug, st));
+  return O3G_OK;
+}
 
 static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStream_t st) {
   const int n = h->n, nf = h->nf;
-  const size_t nb = (size_t)n * sizeof(float), fb = (size_t)nf * sizeof(float);
-  for (int d = 0; d < 3; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->u1[d], 0, nb, st));
-  for (int d = 0; d < 9; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->ug1[d], 0, nb, st));
-  O3G_TRY(ptpt_dev(h->core, h->prec, n, h->x, h->r, h->s, n, h->x, h->r, h->u1, h->ug1, st));
-  if (nf > 0) {
-    for (int d = 0; d < 3; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->fu1[d], 0, fb, st));
-    for (int d = 0; d < 9; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->fug1[d], 0, fb, st));
-    O3G_TRY(ptpt_dev(h->core, h->prec, n, h->x, h->r, h->s, nf, h->f, nullptr, h->fu1, h->fug1, st));
-  }
+  O3G_TRY(rk2_eval(h, 0, st));
   O3G_TRY(o3g_points_finalize(n, fs, h->u1, h->ug1, st));
   if (nf > 0) O3G_TRY(o3g_points_finalize(nf, fs, h->fu1, h->fug1, st));
   // interim state at t + 2dt/3 (Convection.h:366-378)
@@ -239,14 +253,7 @@ static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStrea
       note_launch();
     }
   }
-  for (int d = 0; d < 3; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->u2[d], 0, nb, st));
-  for (int d = 0; d < 9; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->ug2[d], 0, nb, st));
-  O3G_TRY(ptpt_dev(h->core, h->prec, n, h->xi, h->r, h->si, n, h->xi, h->r, h->u2, h->ug2, st));
-  if (nf > 0) {
-    for (int d = 0; d < 3; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->fu2[d], 0, fb, st));
-    for (int d = 0; d < 9; ++d) O3G_CUDA_TRY(cudaMemsetAsync(h->fug2[d], 0, fb, st));
-    O3G_TRY(ptpt_dev(h->core, h->prec, n, h->xi, h->r, h->si, nf, h->fxi, nullptr, h->fu2, h->fug2, st));
-  }
+  O3G_TRY(rk2_eval(h, 1, st));
   O3G_TRY(o3g_points_finalize(n, fs, h->u2, h->ug2, st));
   if (nf > 0) O3G_TRY(o3g_points_finalize(nf, fs, h->fu2, h->fug2, st));
   // 0.25 / 0.75 combine with stretching by the stage-0 strengths (Convection.h:389-425)
@@ -256,19 +263,16 @@ static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStrea
   return O3G_OK;
 }
 
-extern "C" int32_t o3g_rk2_create(int32_t core, int32_t prec, int32_t n, float* const* x, float* const* s, float* r,
-                                  float* elong, int32_t nf, float* const* fx, int32_t use_graph, o3g_rk2_t** out) {
-  if (!out || core < 0 || core > 4 || (prec != O3G_PREC_PLAIN && prec != O3G_PREC_COMPENSATED) || n <= 0 || nf < 0 ||
-      !x || !s || !r || !elong || (nf > 0 && !fx)) {
-    set_error("o3g_rk2_create: bad arguments");
-    return O3G_ERR_INVALID_ARG;
-  }
+static int32_t rk2_alloc(int32_t core, int32_t prec, int32_t n, float* const* x, float* const* s, float* r,
+                         float* elong, int32_t nf, float* const* fx, int32_t use_graph, o3g_rk2_t** out) {
   DeviceFacts df;
   O3G_TRY(device_facts(&df));
   o3g_rk2_t* h = new o3g_rk2_t();
   h->core = core; h->prec = prec; h->n = n; h->nf = nf; h->r = r; h->elong = elong; h->use_graph = use_graph != 0;
   for (int d = 0; d < 3; ++d) { h->x[d] = x[d]; h->s[d] = s[d]; h->f[d] = nf > 0 ? fx[d] : nullptr; }
   const size_t na = align_up((size_t)n * sizeof(float)), fa = align_up((size_t)(nf > 0 ? nf : 1) * sizeof(float));
+  h->na = na;
+  h->fa = fa;
   const size_t total = na * (3 + 9 + 3 + 9 + 3 + 3 + 1) + fa * (3 + 9 + 3 + 9 + 3);
   cudaError_t e = cudaMalloc((void**)&h->buf, total);
   if (e != cudaSuccess) {
@@ -295,11 +299,89 @@ extern "C" int32_t o3g_rk2_create(int32_t core, int32_t prec, int32_t n, float* 
   return O3G_OK;
 }
 
+extern "C" int32_t o3g_rk2_create(int32_t core, int32_t prec, int32_t n, float* const* x, float* const* s, float* r,
+                                  float* elong, int32_t nf, float* const* fx, int32_t use_graph, o3g_rk2_t** out) {
+  if (!out || core < 0 || core > 4 || (prec != O3G_PREC_PLAIN && prec != O3G_PREC_COMPENSATED) || n <= 0 || nf < 0 ||
+      !x || !s || !r || !elong || (nf > 0 && !fx)) {
+    set_error("o3g_rk2_create: bad arguments");
+    return O3G_ERR_INVALID_ARG;
+  }
+  return rk2_alloc(core, prec, n, x, s, r, elong, nf, fx, use_graph, out);
+}
+
+// Many independent systems stored back to back: system i owns particles [P_i, P_i + np[i])
+// and field points [F_i, F_i + nf[i]) of the concatenated arrays (P_i, F_i prefix sums).
+// Each stage's velocities come from ONE batched persistent launch over all systems.
+extern "C" int32_t o3g_batch_rk2_create(int32_t core, int32_t prec, int32_t nsys, const int32_t* np,
+                                        const int32_t* nf, float* const* x, float* const* s, float* r, float* elong,
+                                        float* const* fx, int32_t use_graph, o3g_rk2_t** out) {
+  if (!out || core < 0 || core > 4 || (prec != O3G_PREC_PLAIN && prec != O3G_PREC_COMPENSATED) || nsys < 1 || !np ||
+      !nf || !x || !s || !r || !elong) {
+    set_error("o3g_batch_rk2_create: bad arguments");
+    return O3G_ERR_INVALID_ARG;
+  }
+  long long tp = 0, tf = 0;
+  for (int i = 0; i < nsys; ++i) {
+    if (np[i] < 0 || nf[i] < 0) {
+      set_error("o3g_batch_rk2_create: negative count");
+      return O3G_ERR_INVALID_ARG;
+    }
+    tp += np[i];
+    tf += nf[i];
+  }
+  if (tp < 1 || tp >= (1LL << 30) || tf >= (1LL << 30) || (tf > 0 && !fx)) {
+    set_error("o3g_batch_rk2_create: need 1 <= total particles < 2^30 and field arrays when nf > 0");
+    return O3G_ERR_INVALID_ARG;
+  }
+  o3g_rk2_t* h = nullptr;
+  O3G_TRY(rk2_alloc(core, prec, (int)tp, x, s, r, elong, (int)tf, fx, use_graph, &h));
+  std::vector<BatchSysDev> b0(nsys), b1(nsys);
+  int P = 0, F = 0;
+  for (int i = 0; i < nsys; ++i) {
+    for (int stage = 0; stage < 2; ++stage) {
+      BatchSysDev& d = stage == 0 ? b0[i] : b1[i];
+      float* const* xs = stage == 0 ? h->x : h->xi;
+      float* const* ss = stage == 0 ? h->s : h->si;
+      float* const* fs = stage == 0 ? h->f : h->fxi;
+      float* const* u = stage == 0 ? h->u1 : h->u2;
+      float* const* ug = stage == 0 ? h->ug1 : h->ug2;
+      float* const* fu = stage == 0 ? h->fu1 : h->fu2;
+      float* const* fug = stage == 0 ? h->fug1 : h->fug2;
+      d = BatchSysDev{};
+      for (int k = 0; k < 3; ++k) {
+        d.p[k] = xs[k] + P;
+        d.p[4 + k] = ss[k] + P;
+        d.out[k] = u[k] + P;
+        d.f[k] = tf > 0 ? fs[k] + F : nullptr;
+        d.fout[k] = tf > 0 ? fu[k] + F : nullptr;
+      }
+      d.p[3] = h->r + P;
+      for (int k = 0; k < 9; ++k) {
+        d.out[3 + k] = ug[k] + P;
+        d.fout[3 + k] = tf > 0 ? fug[k] + F : nullptr;
+      }
+      d.np = np[i];
+      d.nf = nf[i];
+    }
+    P += np[i];
+    F += nf[i];
+  }
+  const BatchSysDev* binds[2] = {b0.data(), b1.data()};
+  const int32_t rc = batch_create(core, prec, true, nsys, binds, 2, &h->batch);
+  if (rc != O3G_OK) {
+    o3g_rk2_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return O3G_OK;
+}
+
 extern "C" int32_t o3g_rk2_destroy(o3g_rk2_t* h) {
   if (!h) return O3G_OK;
   cudaDeviceSynchronize();
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
+  if (h->batch) o3g_batch_destroy(h->batch);
   cudaFree(h->buf);
   delete h;
   return O3G_OK;

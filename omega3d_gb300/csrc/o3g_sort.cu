@@ -42,16 +42,6 @@ __global__ void k_bbox(const I* __restrict__ x, const I* __restrict__ y, const I
   }
 }
 
-// spread the low 10 bits of v so that bit k lands at bit 3k
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000ffu;
-  v = (v | (v << 8)) & 0x0300f00fu;
-  v = (v | (v << 4)) & 0x030c30c3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
-
 template <class I>
 __global__ void k_morton(const I* __restrict__ x, const I* __restrict__ y, const I* __restrict__ z, int n,
                          const int* __restrict__ bb, uint32_t* code, uint32_t* idx) {

@@ -474,3 +474,102 @@ class Ralston:
                 self.h = None
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------------------------
+# many independent systems in one launch
+
+class BatchSystem:
+    """One independent particle system of a batch, on the device: particles x[3,np],
+    s[3,np], r[np] with result arrays u[3,np] (+ ug[9,np]), and optional field points
+    f[3,nf] with fu[3,nf] (+ fug[9,nf]).  Results accumulate (+=)."""
+
+    def __init__(self, x, s, r, u, ug=None, f=None, fu=None, fug=None):
+        self.x, self.s, self.r, self.u, self.ug = x, s, r, u, ug
+        self.f, self.fu, self.fug = f, fu, fug
+
+    def struct(self, grads):
+        st = L.System()
+        n = self.x.shape[1]
+        for t, k in ((self.x, 3), (self.s, 3), (self.u, 3)):
+            if not (_is_dev(t) and t.dtype == torch.float32 and t.is_contiguous() and tuple(t.shape) == (k, n)):
+                raise ValueError("batch system arrays must be contiguous float32 CUDA tensors [k, np]")
+        st.np = n
+        st.x, st.y, st.z = _rows(self.x, 3)
+        st.r = _base(self.r)
+        st.sx, st.sy, st.sz = _rows(self.s, 3)
+        st.u, st.v, st.w = _rows(self.u, 3)
+        if grads:
+            for k, p in enumerate(_rows(self.ug, 9)):
+                st.ug[k] = p
+        nf = 0 if self.f is None else self.f.shape[1]
+        st.nf = nf
+        if nf:
+            st.fx, st.fy, st.fz = _rows(self.f, 3)
+            st.fu, st.fv, st.fw = _rows(self.fu, 3)
+            if grads:
+                for k, p in enumerate(_rows(self.fug, 9)):
+                    st.fug[k] = p
+        return st
+
+
+class Batch:
+    """Pair sums of many independent systems (BatchSystem) in one persistent launch per
+    run, with autotuned, per-shape cached configuration (o3g_batch_*)."""
+
+    def __init__(self, systems, env=None, grads=True):
+        env = env or ExecEnv()
+        self.env, self.grads, self.systems = env, grads, list(systems)
+        arr = (L.System * len(self.systems))(*[s.struct(grads) for s in self.systems])
+        h = ctypes.c_void_p()
+        L.check(L.lib().o3g_batch_create(L.CORES[env.core], L.PRECS[env.precision], int(grads), len(self.systems),
+                                         arr, ctypes.byref(h)), "o3g_batch_create")
+        self.h = h
+
+    def run(self, stream=None):
+        st = stream if stream is not None else self.env.stream_handle(True)
+        if torch is not None and isinstance(st, torch.cuda.Stream):
+            st = st.cuda_stream
+        L.check(L.lib().o3g_batch_run(self.h, st), "o3g_batch_run")
+
+    def tune(self, stream=None):
+        st = stream if stream is not None else self.env.stream_handle(True)
+        L.check(L.lib().o3g_batch_tune(self.h, st), "o3g_batch_tune")
+
+    def set_config(self, tpt, blocks_per_sm=0, split=4):
+        L.check(L.lib().o3g_batch_set_config(self.h, tpt, blocks_per_sm, split), "o3g_batch_set_config")
+
+    def config(self):
+        v = [ctypes.c_int32() for _ in range(6)]
+        L.check(L.lib().o3g_batch_get_config(self.h, *[ctypes.byref(x) for x in v]), "o3g_batch_get_config")
+        return dict(zip(("tpt", "grid", "split", "chunk", "nitems", "tuned"), [x.value for x in v]))
+
+    def __del__(self):
+        try:
+            if self.h:
+                L.lib().o3g_batch_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class BatchRalston(Ralston):
+    """Ralston RK2 of many independent systems stored back to back in x[3,N], s[3,N], r[N],
+    elong[N] (system i owns np[i] consecutive particles) and field points f[3,NF] (nf[i]
+    each); both evaluations of a step are one batched persistent launch each."""
+
+    def __init__(self, np_counts, nf_counts, x, s, r, elong, fieldpts=None, env=None, use_graph=True):
+        env = env or ExecEnv()
+        self.x, self.s, self.r, self.elong, self.f = x, s, r, elong, fieldpts
+        self.stream = torch.cuda.Stream(device=x.device) if use_graph else torch.cuda.current_stream(x.device)
+        nsys = len(np_counts)
+        npa = (ctypes.c_int32 * nsys)(*[int(v) for v in np_counts])
+        nfa = (ctypes.c_int32 * nsys)(*[int(v) for v in nf_counts])
+        if sum(np_counts) != x.shape[1] or (sum(nf_counts) != (0 if fieldpts is None else fieldpts.shape[1])):
+            raise ValueError("per-system counts do not add up to the array sizes")
+        h = ctypes.c_void_p()
+        L.check(L.lib().o3g_batch_rk2_create(L.CORES[env.core], L.PRECS[env.precision], nsys, npa, nfa, _ptrs(x, 3),
+                                             _ptrs(s, 3), _base(r), _base(elong),
+                                             _ptrs(fieldpts, 3) if sum(nf_counts) else None, int(use_graph),
+                                             ctypes.byref(h)), "o3g_batch_rk2_create")
+        self.h = h

@@ -7,6 +7,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# the batch autotuner's per-shape cache: keep the test session's choices out of the user's
+# cache directory (the library reads this variable when it stores or first loads choices)
+if "O3G_TUNE_CACHE" not in os.environ:
+    import tempfile
+    os.environ["O3G_TUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="o3g_tune_"), "batch_tune.txt")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103a) GPU; calls the CUDA path through the C-ABI")
