@@ -147,8 +147,10 @@ int32_t o3g_sheet_to_panel_strength(int32_t np, const float* ps0, const float* p
  * flat vortex(+source) panels, adaptively subdivided down to maxlev levels (the reference
  * uses RECURSIVE_LEVELS = 3, Influence.h:23; accepted 0..6).  ts = absolute panel vortex
  * strengths (Surfaces::get_str); sss = source sheet strengths or NULL.  The targets' core
- * radii are not used (Influence.h:872-873).  Accumulates (+=). */
-int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev,
+ * radii are not used (Influence.h:872-873).  Accumulates (+=).  prec PLAIN (FP32 sums, the
+ * reference's arithmetic) or COMPENSATED (Newton-refined rsqrt, two-sum accumulators folded
+ * per tile of 128 panels, partial sums added in double). */
+int32_t o3g_panels_affect_points(int32_t prec, int32_t mem, int32_t maxlev,
                                  int32_t nn, const float* nx, const float* ny, const float* nz,
                                  int32_t np, const uint32_t* idx, const float* area,
                                  const float* tsx, const float* tsy, const float* tsz, const float* sss,
@@ -159,8 +161,9 @@ int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev,
  * Replaces points_affect_panels<float,A>, Influence.h:1107-1221: panel-averaged velocity
  * induced by ns vortex particles on np panels (the BEM right-hand side), computed like the
  * reference by subdividing the target panel as a source carrying the particle's strength
- * and SUBTRACTING the result (Influence.h:1209-1212).  Particle core radii are not used. */
-int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev,
+ * and SUBTRACTING the result (Influence.h:1209-1212).  Particle core radii are not used.
+ * prec PLAIN or COMPENSATED as for o3g_panels_affect_points (tiles of 128 particles). */
+int32_t o3g_points_affect_panels(int32_t prec, int32_t mem, int32_t maxlev,
                                  int32_t ns, const float* sx, const float* sy, const float* sz,
                                  const float* ssx, const float* ssy, const float* ssz,
                                  int32_t nn, const float* nx, const float* ny, const float* nz,
@@ -184,6 +187,8 @@ int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int32_t is_self
  * refined with residuals b - A x formed in FP64 until ||r||/||b|| <= tol (the residual
  * the reference prints, BEM.h:227-230). */
 typedef struct o3g_bem o3g_bem_t;
+/* number of unknowns of the system */
+int32_t o3g_bem_size(const o3g_bem_t* h, int64_t* n);
 /* allocates the handle and ~2 n^2 floats of device memory (n <= 200000; the panel
  * factorisation needs n <= ~68000 on 152 SMs) */
 int32_t o3g_bem_create(int64_t n, o3g_bem_t** h);
@@ -225,13 +230,33 @@ int32_t o3g_points_move_rk2(int32_t n, double dt, double wt1, float* const* u1, 
  * (fx, may be 0): per step two vel+grad evaluations (core, prec PLAIN or COMPENSATED), the
  * 2/3 dt interim move and the 0.25/0.75 combine.  With use_graph != 0 the first step runs
  * directly and the step is then captured into a CUDA graph and replayed (stream must then be
- * a non-default stream).  o3g_rk2_velocities gives the stage-1 velocities of the last step. */
+ * a non-default stream).  o3g_rk2_velocities gives the velocities the last step moved the
+ * particles with (0.25 u1 + 0.75 u2, Points.h:356-439) and its stage-1 gradients. */
 typedef struct o3g_rk2 o3g_rk2_t;
 int32_t o3g_rk2_create(int32_t core, int32_t prec, int32_t n, float* const* x, float* const* s, float* r,
                        float* elong, int32_t nf, float* const* fx, int32_t use_graph, o3g_rk2_t** h);
 int32_t o3g_rk2_step(o3g_rk2_t* h, double dt, const double* fs, int32_t nsteps, void* stream);
 int32_t o3g_rk2_velocities(o3g_rk2_t* h, float** u, float** ug);
 int32_t o3g_rk2_destroy(o3g_rk2_t* h);
+/* Adds one fixed body (Surfaces, device arrays) to a single-system RK2 handle: every stage
+ * then first solves the BEM for that stage's particles -- solve_bem, BEMHelper.h:43-265:
+ * panel velocities from the particles (o3g_points_affect_panels), freestream, RHS.h's
+ * vels_to_rhs, the refined solve, Surfaces::set_str (Surfaces.h:267-335) -- and adds the
+ * panels' velocity and gradient (o3g_panels_affect_points) to the particles' and field
+ * points' sums before finalize_vels, as Convection::find_vels does (Convection.h:131-182).
+ * The matrix (nunk unknowns per panel, subdivision maxlev) is assembled into `bem` and
+ * factorised here, once: the body does not move.  The pair and panel sums use the handle's
+ * precision.  Steps with a body run directly (the solves' convergence checks read the
+ * residual on the host), not from a graph.  clear_inner_layer (Reflect.h) is not applied. */
+int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, int32_t nunk, int32_t maxlev, o3g_bem_t* bem,
+                            double tol, int32_t max_iter, void* stream);
+/* Solve statistics of the attached body: number of solves, refinements and relative residual
+ * of the last one, the largest final residual over all solves. */
+int32_t o3g_rk2_body_stats(const o3g_rk2_t* h, int64_t* solves, int32_t* last_iters, double* last_relres,
+                           double* max_relres);
+/* Copies the body's panel strengths ts[3] (np each) and BEM solution (np * nunk) of the last
+ * stage solved into the caller's arrays (host or device; either may be NULL) and waits. */
+int32_t o3g_rk2_body_strengths(const o3g_rk2_t* h, float* const* ts, float* solution, void* stream);
 
 /* ---- many independent particle systems in one launch ----------------------------------
  * No counterpart in the reference, which runs points_affect_points once per (source

@@ -89,10 +89,11 @@ def _declare(l):
     l.o3g_sheet_to_panel_strength.restype = c_i32
     l.o3g_sheet_to_panel_strength.argtypes = [c_i32] + [P] * 12
     l.o3g_panels_affect_points.restype = c_i32
-    l.o3g_panels_affect_points.argtypes = [c_i32, c_i32, c_i32, P, P, P, c_i32, P, P, P, P, P, P, c_i32, P, P, P,
+    l.o3g_panels_affect_points.argtypes = [c_i32, c_i32, c_i32, c_i32, P, P, P, c_i32, P, P, P, P, P, P, c_i32, P, P, P,
                                            P, P, P, P, P]
     l.o3g_points_affect_panels.restype = c_i32
-    l.o3g_points_affect_panels.argtypes = [c_i32, c_i32, c_i32] + [P] * 6 + [c_i32, P, P, P, c_i32, P, P, P, P, P, P]
+    l.o3g_points_affect_panels.argtypes = [c_i32, c_i32, c_i32, c_i32] + [P] * 6 + [c_i32, P, P, P, c_i32, P, P, P, P, P,
+                                                                           P]
     l.o3g_panels_on_panels_coeff.restype = c_i32
     l.o3g_panels_on_panels_coeff.argtypes = [c_i32, c_i32, c_i32, P, P, P, ctypes.c_int64, P]
     l.o3g_bem_create.restype = c_i32
@@ -123,6 +124,14 @@ def _declare(l):
     l.o3g_rk2_velocities.argtypes = [P, P, P]
     l.o3g_rk2_destroy.restype = c_i32
     l.o3g_rk2_destroy.argtypes = [P]
+    l.o3g_rk2_attach_body.restype = c_i32
+    l.o3g_rk2_attach_body.argtypes = [P, P, c_i32, c_i32, P, c_d, c_i32, P]
+    l.o3g_rk2_body_stats.restype = c_i32
+    l.o3g_rk2_body_stats.argtypes = [P, P, P, P, P]
+    l.o3g_rk2_body_strengths.restype = c_i32
+    l.o3g_rk2_body_strengths.argtypes = [P, P, P, P]
+    l.o3g_bem_size.restype = c_i32
+    l.o3g_bem_size.argtypes = [P, P]
     l.o3g_points_affect_points_noalloc.restype = c_i32
     l.o3g_points_affect_points_noalloc.argtypes = [c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
     l.o3g_batch_create.restype = c_i32

@@ -592,6 +592,12 @@ struct o3g_bem {
 
 using namespace o3g;
 
+extern "C" int32_t o3g_bem_size(const o3g_bem_t* h, int64_t* n) {
+  if (!h || !n) return O3G_ERR_INVALID_ARG;
+  *n = h->n;
+  return O3G_OK;
+}
+
 static int32_t bem_check(o3g_bem_t* h) {
   if (!h || !h->A) {
     set_error("o3g_bem: null or destroyed handle");

@@ -54,12 +54,12 @@ __device__ __forceinline__ bool well_sep(float tx, float ty, float tz, float cx,
 
 // singular vortex+source point at (cx,cy,cz) with strength (sx,sy,sz), ss on target t:
 // kernel_0vs_0pg with sr = 0 (Kernels.h:294-345); a[0..2] velocity, a[3..11] gradient
-template <bool GRADS, bool SRC>
+template <bool GRADS, bool SRC, bool ACC = false>
 __device__ __forceinline__ void leaf(float tx, float ty, float tz, float cx, float cy, float cz, float sx, float sy,
                                      float sz, float ss, float* a) {
   const float dx = tx - cx, dy = ty - cy, dz = tz - cz;
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-  const float rs = rsqrtf(r2);
+  const float rs = rsq<ACC>(r2);
   const float rs2 = rs * rs;
   const float r3 = rs2 * rs;
   float cxw = dz * sy - dy * sz;
@@ -98,7 +98,7 @@ __device__ __forceinline__ void leaf(float tx, float ty, float tz, float cx, flo
 }
 
 // depth-first subdivision of a triangle that failed the level-0 test
-template <bool GRADS, bool SRC>
+template <bool GRADS, bool SRC, bool ACC = false>
 __device__ __noinline__ void subdivide(float tx, float ty, float tz, const Tri& root, float sx, float sy, float sz,
                                        float ss, int maxlev, float* a) {
   Tri st[kStack];
@@ -124,10 +124,30 @@ __device__ __noinline__ void subdivide(float tx, float ty, float tz, const Tri& 
     if (t.lev >= maxlev || well_sep(tx, ty, tz, cx, cy, cz, t.area)) {
       // 0.25^lev, exact powers of two (the reference scales by 0.25 per split, Kernels.h:1072-1075)
       const float f = __int_as_float((127 - 2 * t.lev) << 23);
-      leaf<GRADS, SRC>(tx, ty, tz, cx, cy, cz, sx * f, sy * f, sz * f, ss * f, a);
+      leaf<GRADS, SRC, ACC>(tx, ty, tz, cx, cy, cz, sx * f, sy * f, sz * f, ss * f, a);
     } else if (sp + 4 <= kStack) {
       push_children(t);
     }
+  }
+}
+
+// error-free a + b = s + e (Knuth's two-sum)
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// compensated mode: fold the plain partial sums of one tile into (hi, lo) and restart them
+template <int NC>
+__device__ __forceinline__ void fold_tile(float* a, float* hi, float* lo) {
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    float sum, err;
+    two_sum_f(hi[c], a[c], sum, err);
+    hi[c] = sum;
+    lo[c] += err;
+    a[c] = 0.f;
   }
 }
 
@@ -168,13 +188,14 @@ __global__ void k_pack_panels(int np, const float* __restrict__ nx, const float*
   nearr[j] = n;
 }
 
-template <bool GRADS, bool SRC>
+template <bool GRADS, bool SRC, bool ACC>
 __global__ void __launch_bounds__(kPB) k_panpt(const PanelFar* __restrict__ far, const PanelNear* __restrict__ nearr,
                                                int ntiles, int tiles_per_split, int maxlev, int nt,
                                                const float* __restrict__ tx, const float* __restrict__ ty,
                                                const float* __restrict__ tz, float* partial, int nt_pad,
                                                OutPtrs<float> out) {
   constexpr int NC = GRADS ? 12 : 3;
+  constexpr int NH = ACC ? NC : 1;
   __shared__ PanelFar sf[kPB];
   const int i = blockIdx.x * kPB + threadIdx.x;
   const bool live = i < nt;
@@ -182,6 +203,9 @@ __global__ void __launch_bounds__(kPB) k_panpt(const PanelFar* __restrict__ far,
   float a[12];
 #pragma unroll
   for (int c = 0; c < 12; ++c) a[c] = 0.f;
+  float hi[NH], lo[NH];
+#pragma unroll
+  for (int c = 0; c < NH; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
   const int t0 = blockIdx.y * tiles_per_split;
   const int t1 = min(ntiles, t0 + tiles_per_split);
   for (int tile = t0; tile < t1; ++tile) {
@@ -192,30 +216,45 @@ __global__ void __launch_bounds__(kPB) k_panpt(const PanelFar* __restrict__ far,
     for (int jj = 0; jj < kPB; ++jj) {
       const PanelFar f = sf[jj];
       if (maxlev == 0 || dist_rn(px, py, pz, f.c.x, f.c.y, f.c.z) > f.c.w) {
-        leaf<GRADS, SRC>(px, py, pz, f.c.x, f.c.y, f.c.z, f.s.x, f.s.y, f.s.z, f.s.w, a);
+        leaf<GRADS, SRC, ACC>(px, py, pz, f.c.x, f.c.y, f.c.z, f.s.x, f.s.y, f.s.z, f.s.w, a);
       } else {
         const PanelNear nr = nearr[(size_t)tile * kPB + jj];
         const Tri root{nr.a.x, nr.a.y, nr.a.z, nr.a.w, nr.b.x, nr.b.y, nr.b.z, nr.b.w, nr.d.x, nr.d.y, 0};
-        subdivide<GRADS, SRC>(px, py, pz, root, f.s.x, f.s.y, f.s.z, f.s.w, maxlev, a);
+        subdivide<GRADS, SRC, ACC>(px, py, pz, root, f.s.x, f.s.y, f.s.z, f.s.w, maxlev, a);
       }
     }
+    if (ACC) fold_tile<NC>(a, hi, lo);
   }
   if (partial) {
-    float* base = partial + (size_t)blockIdx.y * NC * nt_pad;
+    if (ACC) {
+      float* base = partial + (size_t)blockIdx.y * 2 * NC * nt_pad;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) base[(size_t)c * nt_pad + i] = a[c];
+      for (int c = 0; c < NC; ++c) {
+        base[(size_t)c * nt_pad + i] = hi[c];
+        base[(size_t)(NC + c) * nt_pad + i] = lo[c];
+      }
+    } else {
+      float* base = partial + (size_t)blockIdx.y * NC * nt_pad;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) base[(size_t)c * nt_pad + i] = a[c];
+    }
   } else if (live) {
 #pragma unroll
-    for (int c = 0; c < NC; ++c) out.p[c][i] += a[c];
+    for (int c = 0; c < NC; ++c) {
+      if (ACC) out.p[c][i] = (float)((double)out.p[c][i] + ((double)hi[c] + (double)lo[c]));
+      else     out.p[c][i] += a[c];
+    }
   }
 }
 
 // points_affect_panels: thread per target panel, sweep particle tiles; the panel is the
 // subdivided "source" with the particle's strength, evaluated at the particle, negated.
+template <bool ACC>
 __global__ void __launch_bounds__(kPB) k_ptpan(const PanelFar* __restrict__ far, const PanelNear* __restrict__ nearr,
                                                int np, const float4* __restrict__ ppos, int ntiles,
                                                int tiles_per_split, int maxlev, float* partial, int np_pad,
                                                OutPtrs<float> out) {
+  constexpr int NH = ACC ? 3 : 1;
   __shared__ float4 sp[kPB], sw[kPB];
   const int i = blockIdx.x * kPB + threadIdx.x;
   const PanelFar f = far[i];
@@ -223,6 +262,9 @@ __global__ void __launch_bounds__(kPB) k_ptpan(const PanelFar* __restrict__ far,
   float a[12];
 #pragma unroll
   for (int c = 0; c < 3; ++c) a[c] = 0.f;
+  float hi[NH], lo[NH];
+#pragma unroll
+  for (int c = 0; c < NH; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
   const int t0 = blockIdx.y * tiles_per_split;
   const int t1 = min(ntiles, t0 + tiles_per_split);
   for (int tile = t0; tile < t1; ++tile) {
@@ -234,20 +276,33 @@ __global__ void __launch_bounds__(kPB) k_ptpan(const PanelFar* __restrict__ far,
     for (int jj = 0; jj < kPB; ++jj) {
       const float4 p = sp[jj], w = sw[jj];
       if (maxlev == 0 || dist_rn(p.x, p.y, p.z, f.c.x, f.c.y, f.c.z) > f.c.w) {
-        leaf<false, false>(p.x, p.y, p.z, f.c.x, f.c.y, f.c.z, w.x, w.y, w.z, 0.f, a);
+        leaf<false, false, ACC>(p.x, p.y, p.z, f.c.x, f.c.y, f.c.z, w.x, w.y, w.z, 0.f, a);
       } else {
         const Tri root{nr.a.x, nr.a.y, nr.a.z, nr.a.w, nr.b.x, nr.b.y, nr.b.z, nr.b.w, nr.d.x, nr.d.y, 0};
-        subdivide<false, false>(p.x, p.y, p.z, root, w.x, w.y, w.z, 0.f, maxlev, a);
+        subdivide<false, false, ACC>(p.x, p.y, p.z, root, w.x, w.y, w.z, 0.f, maxlev, a);
       }
     }
+    if (ACC) fold_tile<3>(a, hi, lo);
   }
   if (partial) {
-    float* base = partial + (size_t)blockIdx.y * 3 * np_pad;
+    if (ACC) {
+      float* base = partial + (size_t)blockIdx.y * 6 * np_pad;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) base[(size_t)c * np_pad + i] = a[c];
+      for (int c = 0; c < 3; ++c) {
+        base[(size_t)c * np_pad + i] = hi[c];
+        base[(size_t)(3 + c) * np_pad + i] = lo[c];
+      }
+    } else {
+      float* base = partial + (size_t)blockIdx.y * 3 * np_pad;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) base[(size_t)c * np_pad + i] = a[c];
+    }
   } else if (i < np) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) out.p[c][i] -= a[c];
+    for (int c = 0; c < 3; ++c) {
+      if (ACC) out.p[c][i] = (float)((double)out.p[c][i] - ((double)hi[c] + (double)lo[c]));
+      else     out.p[c][i] -= a[c];
+    }
   }
 }
 
@@ -265,14 +320,23 @@ __global__ void k_pack_particles(int n, int n_pad, const float* __restrict__ x, 
   }
 }
 
-template <int NC, int SIGN>
+template <int NC, int SIGN, bool ACC>
 __global__ void k_reduce_panel(const float* __restrict__ partial, int nsplit, int n, int n_pad, OutPtrs<float> out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (i >= n) return;
-  float s = 0.f;
-  for (int k = 0; k < nsplit; ++k) s += partial[((size_t)k * NC + c) * n_pad + i];
-  out.p[c][i] += SIGN * s;
+  if (ACC) {
+    double s = 0.0;
+    for (int k = 0; k < nsplit; ++k) {
+      s += (double)partial[((size_t)k * 2 * NC + c) * n_pad + i];
+      s += (double)partial[((size_t)k * 2 * NC + NC + c) * n_pad + i];
+    }
+    out.p[c][i] = (float)((double)out.p[c][i] + SIGN * s);
+  } else {
+    float s = 0.f;
+    for (int k = 0; k < nsplit; ++k) s += partial[((size_t)k * NC + c) * n_pad + i];
+    out.p[c][i] += SIGN * s;
+  }
 }
 
 static void plan_split(int nunits_outer, int ninner_tiles, int slots, int* nsplit, int* tps) {
@@ -289,16 +353,18 @@ static void plan_split(int nunits_outer, int ninner_tiles, int slots, int* nspli
 
 using namespace o3g;
 
-extern "C" int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev, int32_t nn, const float* nx, const float* ny,
-                                            const float* nz, int32_t np, const uint32_t* idx, const float* area,
-                                            const float* tsx, const float* tsy, const float* tsz, const float* sss,
-                                            int32_t nt, const float* tx, const float* ty, const float* tz, float* tu,
-                                            float* tv, float* tw, float* const* tug, void* stream) {
+extern "C" int32_t o3g_panels_affect_points(int32_t prec, int32_t mem, int32_t maxlev, int32_t nn, const float* nx,
+                                            const float* ny, const float* nz, int32_t np, const uint32_t* idx,
+                                            const float* area, const float* tsx, const float* tsy, const float* tsz,
+                                            const float* sss, int32_t nt, const float* tx, const float* ty,
+                                            const float* tz, float* tu, float* tv, float* tw, float* const* tug,
+                                            void* stream) {
   if ((mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || maxlev < 0 || maxlev > kMaxLev || nn < 0 || np < 0 ||
-      nt < 0) {
-    set_error("panels_affect_points: bad mem, maxlev (0..6) or negative count");
+      nt < 0 || (prec != O3G_PREC_PLAIN && prec != O3G_PREC_COMPENSATED)) {
+    set_error("panels_affect_points: bad precision (PLAIN or COMPENSATED), mem, maxlev (0..6) or negative count");
     return O3G_ERR_INVALID_ARG;
   }
+  const bool comp = prec == O3G_PREC_COMPENSATED;
   if (np > 0 && (!nx || !ny || !nz || !idx || !area || !tsx || !tsy || !tsz)) {
     set_error("panels_affect_points: null panel array");
     return O3G_ERR_INVALID_ARG;
@@ -323,14 +389,18 @@ extern "C" int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev, int32_t
   const int ntiles = (np + kPB - 1) / kPB, np_pad = ntiles * kPB;
   const int tb = (nt + kPB - 1) / kPB, nt_pad = tb * kPB;
   int nb = 0;
-  const void* kp = grads ? (sss ? (const void*)&k_panpt<true, true> : (const void*)&k_panpt<true, false>)
-                         : (sss ? (const void*)&k_panpt<false, true> : (const void*)&k_panpt<false, false>);
+  const void* kp;
+  if (comp) kp = grads ? (sss ? (const void*)&k_panpt<true, true, true> : (const void*)&k_panpt<true, false, true>)
+                       : (sss ? (const void*)&k_panpt<false, true, true> : (const void*)&k_panpt<false, false, true>);
+  else kp = grads ? (sss ? (const void*)&k_panpt<true, true, false> : (const void*)&k_panpt<true, false, false>)
+                  : (sss ? (const void*)&k_panpt<false, true, false> : (const void*)&k_panpt<false, false, false>);
   O3G_TRY(occupancy_blocks(kp, kPB, &nb));
+  const int PC = comp ? 2 * NC : NC;   // partial components per split
   int nsplit = 1, tps = ntiles;
   plan_split(tb, ntiles, nb * df.num_sms, &nsplit, &tps);
 
   size_t bytes = align_up((size_t)np_pad * sizeof(PanelFar)) + align_up((size_t)np_pad * sizeof(PanelNear));
-  if (nsplit > 1) bytes += align_up((size_t)nsplit * NC * nt_pad * sizeof(float));
+  if (nsplit > 1) bytes += align_up((size_t)nsplit * PC * nt_pad * sizeof(float));
   size_t staging = 0;
   if (mem == O3G_MEM_HOST)
     staging = 3 * align_up((size_t)nn * 4) + align_up((size_t)np * 12) + 4 * align_up((size_t)np * 4) +
@@ -364,25 +434,29 @@ extern "C" int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev, int32_t
   Carve cw(ws->base + staging);
   PanelFar* far = cw.take<PanelFar>(np_pad);
   PanelNear* nearr = cw.take<PanelNear>(np_pad);
-  float* partial = nsplit > 1 ? cw.take<float>((size_t)nsplit * NC * nt_pad) : nullptr;
+  float* partial = nsplit > 1 ? cw.take<float>((size_t)nsplit * PC * nt_pad) : nullptr;
   k_pack_panels<<<(np_pad + 255) / 256, 256, 0, st>>>(np, dnx, dny, dnz, didx, dar, dtsx, dtsy, dtsz, dsss, np_pad,
                                                      far, nearr);
   note_launch();
   dim3 grid(tb, nsplit);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
-  if (grads) {
-    if (sss) k_panpt<true, true><<<grid, kPB, 0, st>>>(far, nearr, ntiles, tps, maxlev, nt, dtx, dty, dtz, partial, nt_pad, out);
-    else     k_panpt<true, false><<<grid, kPB, 0, st>>>(far, nearr, ntiles, tps, maxlev, nt, dtx, dty, dtz, partial, nt_pad, out);
-  } else {
-    if (sss) k_panpt<false, true><<<grid, kPB, 0, st>>>(far, nearr, ntiles, tps, maxlev, nt, dtx, dty, dtz, partial, nt_pad, out);
-    else     k_panpt<false, false><<<grid, kPB, 0, st>>>(far, nearr, ntiles, tps, maxlev, nt, dtx, dty, dtz, partial, nt_pad, out);
+  {
+    int ntl = ntiles, mxl = maxlev, ntt = nt, ntp = nt_pad;
+    void* args[] = {&far, &nearr, &ntl, &tps, &mxl, &ntt, &dtx, &dty, &dtz, &partial, &ntp, &out};
+    O3G_CUDA_TRY(cudaLaunchKernel(kp, grid, dim3(kPB), args, 0, st));
   }
   note_launch();
   tm.end(st);
   if (nsplit > 1) {
-    if (grads) k_reduce_panel<12, 1><<<dim3((nt + 255) / 256, 12), 256, 0, st>>>(partial, nsplit, nt, nt_pad, out);
-    else       k_reduce_panel<3, 1><<<dim3((nt + 255) / 256, 3), 256, 0, st>>>(partial, nsplit, nt, nt_pad, out);
+    const dim3 rg((nt + 255) / 256, NC);
+    if (comp) {
+      if (grads) k_reduce_panel<12, 1, true><<<rg, 256, 0, st>>>(partial, nsplit, nt, nt_pad, out);
+      else       k_reduce_panel<3, 1, true><<<rg, 256, 0, st>>>(partial, nsplit, nt, nt_pad, out);
+    } else {
+      if (grads) k_reduce_panel<12, 1, false><<<rg, 256, 0, st>>>(partial, nsplit, nt, nt_pad, out);
+      else       k_reduce_panel<3, 1, false><<<rg, 256, 0, st>>>(partial, nsplit, nt, nt_pad, out);
+    }
     note_launch();
   }
   O3G_CUDA_TRY(cudaGetLastError());
@@ -394,16 +468,17 @@ extern "C" int32_t o3g_panels_affect_points(int32_t mem, int32_t maxlev, int32_t
   return O3G_OK;
 }
 
-extern "C" int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev, int32_t ns, const float* sx, const float* sy,
-                                            const float* sz, const float* ssx, const float* ssy, const float* ssz,
-                                            int32_t nn, const float* nx, const float* ny, const float* nz, int32_t np,
-                                            const uint32_t* idx, const float* area, float* pu, float* pv, float* pw,
-                                            void* stream) {
+extern "C" int32_t o3g_points_affect_panels(int32_t prec, int32_t mem, int32_t maxlev, int32_t ns, const float* sx,
+                                            const float* sy, const float* sz, const float* ssx, const float* ssy,
+                                            const float* ssz, int32_t nn, const float* nx, const float* ny,
+                                            const float* nz, int32_t np, const uint32_t* idx, const float* area,
+                                            float* pu, float* pv, float* pw, void* stream) {
   if ((mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || maxlev < 0 || maxlev > kMaxLev || nn < 0 || np < 0 ||
-      ns < 0) {
-    set_error("points_affect_panels: bad mem, maxlev (0..6) or negative count");
+      ns < 0 || (prec != O3G_PREC_PLAIN && prec != O3G_PREC_COMPENSATED)) {
+    set_error("points_affect_panels: bad precision (PLAIN or COMPENSATED), mem, maxlev (0..6) or negative count");
     return O3G_ERR_INVALID_ARG;
   }
+  const bool comp = prec == O3G_PREC_COMPENSATED;
   if (ns > 0 && (!sx || !sy || !sz || !ssx || !ssy || !ssz)) {
     set_error("points_affect_panels: null particle array");
     return O3G_ERR_INVALID_ARG;
@@ -423,12 +498,14 @@ extern "C" int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev, int32_t
   const int ptiles = (ns + kPB - 1) / kPB, ns_pad = ptiles * kPB;
   const int tb = (np + kPB - 1) / kPB, np_pad = tb * kPB;
   int nb = 0;
-  O3G_TRY(occupancy_blocks((const void*)&k_ptpan, kPB, &nb));
+  const void* kp = comp ? (const void*)&k_ptpan<true> : (const void*)&k_ptpan<false>;
+  O3G_TRY(occupancy_blocks(kp, kPB, &nb));
   int nsplit = 1, tps = ptiles;
   plan_split(tb, ptiles, nb * df.num_sms, &nsplit, &tps);
+  const int PC = comp ? 6 : 3;
   size_t bytes = align_up((size_t)np_pad * sizeof(PanelFar)) + align_up((size_t)np_pad * sizeof(PanelNear)) +
                  align_up((size_t)ns_pad * 2 * sizeof(float4));
-  if (nsplit > 1) bytes += align_up((size_t)nsplit * 3 * np_pad * sizeof(float));
+  if (nsplit > 1) bytes += align_up((size_t)nsplit * PC * np_pad * sizeof(float));
   // zero strengths for the panel pack (the panels here are targets)
   bytes += align_up((size_t)np * sizeof(float));
   size_t staging = 0;
@@ -464,7 +541,7 @@ extern "C" int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev, int32_t
   PanelFar* far = cw.take<PanelFar>(np_pad);
   PanelNear* nearr = cw.take<PanelNear>(np_pad);
   float4* pp = cw.take<float4>((size_t)ns_pad * 2);
-  float* partial = nsplit > 1 ? cw.take<float>((size_t)nsplit * 3 * np_pad) : nullptr;
+  float* partial = nsplit > 1 ? cw.take<float>((size_t)nsplit * PC * np_pad) : nullptr;
   float* zero = cw.take<float>(np);
   O3G_CUDA_TRY(cudaMemsetAsync(zero, 0, (size_t)np * sizeof(float), st));
   k_pack_panels<<<(np_pad + 255) / 256, 256, 0, st>>>(np, dnx, dny, dnz, didx, dar, zero, zero, zero, nullptr, np_pad,
@@ -473,11 +550,13 @@ extern "C" int32_t o3g_points_affect_panels(int32_t mem, int32_t maxlev, int32_t
   note_launch(2);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
-  k_ptpan<<<dim3(tb, nsplit), kPB, 0, st>>>(far, nearr, np, pp, ptiles, tps, maxlev, partial, np_pad, out);
+  if (comp) k_ptpan<true><<<dim3(tb, nsplit), kPB, 0, st>>>(far, nearr, np, pp, ptiles, tps, maxlev, partial, np_pad, out);
+  else      k_ptpan<false><<<dim3(tb, nsplit), kPB, 0, st>>>(far, nearr, np, pp, ptiles, tps, maxlev, partial, np_pad, out);
   note_launch();
   tm.end(st);
   if (nsplit > 1) {
-    k_reduce_panel<3, -1><<<dim3((np + 255) / 256, 3), 256, 0, st>>>(partial, nsplit, np, np_pad, out);
+    if (comp) k_reduce_panel<3, -1, true><<<dim3((np + 255) / 256, 3), 256, 0, st>>>(partial, nsplit, np, np_pad, out);
+    else      k_reduce_panel<3, -1, false><<<dim3((np + 255) / 256, 3), 256, 0, st>>>(partial, nsplit, np, np_pad, out);
     note_launch();
   }
   O3G_CUDA_TRY(cudaGetLastError());

@@ -212,11 +212,71 @@ struct o3g_rk2 {
   cudaStream_t warm_stream = nullptr;   // stream whose workspace the warm-up step sized
   size_t na = 0, fa = 0;                // bytes per particle / field-point component array
   o3g_batch_t* batch = nullptr;         // many independent systems: one plan, bindings 0 (x) and 1 (xi)
+  struct Body {
+    o3g_surface_t surf;                 // caller's device arrays
+    int nunk = 2, maxlev = 3;
+    o3g_bem_t* bem = nullptr;           // caller's handle, assembled and factorised at attach
+    double tol = 1e-10;
+    int max_iter = 30;
+    float* buf = nullptr;
+    float *pu[3], *rhs, *sol, *ts[3], *sss;
+    long long solves = 0;
+    int last_iters = 0;
+    double last_relres = 0.0, max_relres = 0.0;
+  };
+  Body* body = nullptr;
 };
+
+// Surfaces::set_str + vortex_sheet_to_panel_strength (Surfaces.h:267-335) in float without
+// contraction: ts = (ps0 x1 + ps1 x2) * area; the source sheet strength of nunk == 3
+__global__ void k_set_str(int np, int nunk, const float* __restrict__ sol, const float* __restrict__ x1x,
+                          const float* __restrict__ x1y, const float* __restrict__ x1z, const float* __restrict__ x2x,
+                          const float* __restrict__ x2y, const float* __restrict__ x2z,
+                          const float* __restrict__ area, float* tsx, float* tsy, float* tsz, float* sss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const float p0 = sol[(size_t)nunk * i], p1 = sol[(size_t)nunk * i + 1], a = area[i];
+  tsx[i] = __fmul_rn(__fadd_rn(__fmul_rn(p0, x1x[i]), __fmul_rn(p1, x2x[i])), a);
+  tsy[i] = __fmul_rn(__fadd_rn(__fmul_rn(p0, x1y[i]), __fmul_rn(p1, x2y[i])), a);
+  tsz[i] = __fmul_rn(__fadd_rn(__fmul_rn(p0, x1z[i]), __fmul_rn(p1, x2z[i])), a);
+  if (nunk == 3) sss[i] = sol[3 * (size_t)i + 2];
+}
+
+// solve_bem (BEMHelper.h:43-265) for the stage state (x, s): strengths into body->ts / sss
+static int32_t body_solve(o3g_rk2_t* h, float* const* x, float* const* s, const double* fs, cudaStream_t st) {
+  o3g_rk2::Body& b = *h->body;
+  const o3g_surface_t& g = b.surf;
+  const int np = g.np;
+  O3G_CUDA_TRY(cudaMemsetAsync(b.pu[0], 0, 3 * align_up((size_t)np * sizeof(float)), st));
+  O3G_TRY(o3g_points_affect_panels(h->prec, O3G_MEM_DEVICE, b.maxlev, h->n, x[0], x[1], x[2], s[0], s[1], s[2],
+                                   g.nn, g.x, g.y, g.z, np, g.idx, g.area, b.pu[0], b.pu[1], b.pu[2], st));
+  O3G_TRY(o3g_panel_vels_to_rhs(np, b.nunk, fs, b.pu[0], b.pu[1], b.pu[2], &g, b.rhs, st));
+  int it = 0;
+  double rr = 0.0;
+  O3G_TRY(o3g_bem_solve(b.bem, b.rhs, b.sol, nullptr, O3G_MEM_DEVICE, b.tol, b.max_iter, &it, &rr, st));
+  b.solves += 1;
+  b.last_iters = it;
+  b.last_relres = rr;
+  if (rr > b.max_relres) b.max_relres = rr;
+  k_set_str<<<(np + 255) / 256, 256, 0, st>>>(np, b.nunk, b.sol, g.x1x, g.x1y, g.x1z, g.x2x, g.x2y, g.x2z, g.area,
+                                              b.ts[0], b.ts[1], b.ts[2], b.sss);
+  note_launch();
+  O3G_CUDA_TRY(cudaGetLastError());
+  return O3G_OK;
+}
+
+static int32_t body_velocities(o3g_rk2_t* h, int nt, float* const* t, float* const* u, float* const* ug,
+                               cudaStream_t st) {
+  o3g_rk2::Body& b = *h->body;
+  const o3g_surface_t& g = b.surf;
+  return o3g_panels_affect_points(h->prec, O3G_MEM_DEVICE, b.maxlev, g.nn, g.x, g.y, g.z, g.np, g.idx, g.area,
+                                  b.ts[0], b.ts[1], b.ts[2], b.nunk == 3 ? b.sss : nullptr, nt, t[0], t[1], t[2],
+                                  u[0], u[1], u[2], ug, st);
+}
 
 // velocities and gradients (zeroed first) of stage 0 (state x, s -> u1, fu1) or stage 1
 // (interim state xi, si -> u2, fu2); the 3 + 9 component arrays of a stage are contiguous
-static int32_t rk2_eval(o3g_rk2_t* h, int stage, cudaStream_t st) {
+static int32_t rk2_eval(o3g_rk2_t* h, int stage, const double* fs, cudaStream_t st) {
   const int n = h->n, nf = h->nf;
   float** u = stage == 0 ? h->u1 : h->u2;
   float** ug = stage == 0 ? h->ug1 : h->ug2;
@@ -228,14 +288,20 @@ static int32_t rk2_eval(o3g_rk2_t* h, int stage, cudaStream_t st) {
   float** x = stage == 0 ? h->x : h->xi;
   float** s = stage == 0 ? h->s : h->si;
   float** f = stage == 0 ? h->f : h->fxi;
+  if (h->body) O3G_TRY(body_solve(h, x, s, fs, st));
+  // vorticity first, then the boundary (Convection.h:158-168)
   O3G_TRY(ptpt_dev(h->core, h->prec, n, x, h->r, s, n, x, h->r, u, ug, st));
-  if (nf > 0) O3G_TRY(ptpt_dev(h->core, h->prec, n, x, h->r, s, nf, f, nullptr, fu, fug, st));
+  if (h->body) O3G_TRY(body_velocities(h, n, x, u, ug, st));
+  if (nf > 0) {
+    O3G_TRY(ptpt_dev(h->core, h->prec, n, x, h->r, s, nf, f, nullptr, fu, fug, st));
+    if (h->body) O3G_TRY(body_velocities(h, nf, f, fu, fug, st));
+  }
   return O3G_OK;
 }
 
 static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStream_t st) {
   const int n = h->n, nf = h->nf;
-  O3G_TRY(rk2_eval(h, 0, st));
+  O3G_TRY(rk2_eval(h, 0, fs, st));
   O3G_TRY(o3g_points_finalize(n, fs, h->u1, h->ug1, st));
   if (nf > 0) O3G_TRY(o3g_points_finalize(nf, fs, h->fu1, h->fug1, st));
   // interim state at t + 2dt/3 (Convection.h:366-378)
@@ -253,7 +319,7 @@ static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStrea
       note_launch();
     }
   }
-  O3G_TRY(rk2_eval(h, 1, st));
+  O3G_TRY(rk2_eval(h, 1, fs, st));
   O3G_TRY(o3g_points_finalize(n, fs, h->u2, h->ug2, st));
   if (nf > 0) O3G_TRY(o3g_points_finalize(nf, fs, h->fu2, h->fug2, st));
   // 0.25 / 0.75 combine with stretching by the stage-0 strengths (Convection.h:389-425)
@@ -382,6 +448,10 @@ extern "C" int32_t o3g_rk2_destroy(o3g_rk2_t* h) {
   if (h->exec) cudaGraphExecDestroy(h->exec);
   if (h->graph) cudaGraphDestroy(h->graph);
   if (h->batch) o3g_batch_destroy(h->batch);
+  if (h->body) {
+    cudaFree(h->body->buf);
+    delete h->body;
+  }
   cudaFree(h->buf);
   delete h;
   return O3G_OK;
@@ -397,6 +467,10 @@ extern "C" int32_t o3g_rk2_step(o3g_rk2_t* h, double dt, const double* fs, int32
   }
   cudaStream_t st = (cudaStream_t)stream;
   int done = 0;
+  if (h->body) {
+    for (; done < nsteps; ++done) O3G_TRY(rk2_one_step(h, dt, fs, st));
+    return O3G_OK;
+  }
   if (!h->warmed || !h->use_graph || h->warm_stream != st) {
     // direct steps; with graphs, one direct step on this stream sizes its workspace so the
     // capture below never allocates
@@ -433,5 +507,78 @@ extern "C" int32_t o3g_rk2_velocities(o3g_rk2_t* h, float** u, float** ug) {
   if (!h || !u) return O3G_ERR_INVALID_ARG;
   for (int d = 0; d < 3; ++d) u[d] = h->u1[d];
   if (ug) for (int d = 0; d < 9; ++d) ug[d] = h->ug1[d];
+  return O3G_OK;
+}
+
+extern "C" int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, int32_t nunk, int32_t maxlev,
+                                       o3g_bem_t* bem, double tol, int32_t max_iter, void* stream) {
+  if (!h || !surf || !bem || (nunk != 2 && nunk != 3) || maxlev < 0 || maxlev > 4 || surf->np < 1 ||
+      !(tol >= 0.0) || max_iter < 1) {
+    set_error("o3g_rk2_attach_body: bad arguments (nunk 2 or 3, maxlev 0..4, np >= 1)");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (h->batch || h->body) {
+    set_error("o3g_rk2_attach_body: the handle is batched or has a body already");
+    return O3G_ERR_STATE;
+  }
+  int64_t n = 0;
+  O3G_TRY(o3g_bem_size(bem, &n));
+  if (n != (int64_t)surf->np * nunk) {
+    set_error("o3g_rk2_attach_body: the BEM system must have np * nunk unknowns");
+    return O3G_ERR_INVALID_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  float* A = nullptr;
+  int64_t ld = 0;
+  O3G_TRY(o3g_bem_matrix(bem, &A, &ld));
+  O3G_TRY(o3g_panels_on_panels_coeff(maxlev, nunk, 1, surf, surf, A, ld, st));
+  O3G_TRY(o3g_bem_factor(bem, st));
+  o3g_rk2::Body* b = new o3g_rk2::Body();
+  b->surf = *surf;
+  b->nunk = nunk;
+  b->maxlev = maxlev;
+  b->bem = bem;
+  b->tol = tol;
+  b->max_iter = max_iter;
+  const size_t pa = align_up((size_t)surf->np * sizeof(float));
+  const size_t ua = align_up((size_t)surf->np * nunk * sizeof(float));
+  cudaError_t e = cudaMalloc((void**)&b->buf, 7 * pa + 2 * ua);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    delete b;
+    set_error_cuda("o3g_rk2_attach_body: cudaMalloc", e);
+    return O3G_ERR_ALLOC;
+  }
+  char* p = (char*)b->buf;
+  for (int d = 0; d < 3; ++d) { b->pu[d] = (float*)p; p += pa; }
+  b->rhs = (float*)p; p += ua;
+  b->sol = (float*)p; p += ua;
+  for (int d = 0; d < 3; ++d) { b->ts[d] = (float*)p; p += pa; }
+  b->sss = (float*)p;
+  h->body = b;
+  h->use_graph = false;
+  return O3G_OK;
+}
+
+extern "C" int32_t o3g_rk2_body_stats(const o3g_rk2_t* h, int64_t* solves, int32_t* last_iters, double* last_relres,
+                                      double* max_relres) {
+  if (!h || !h->body) return O3G_ERR_STATE;
+  if (solves) *solves = h->body->solves;
+  if (last_iters) *last_iters = h->body->last_iters;
+  if (last_relres) *last_relres = h->body->last_relres;
+  if (max_relres) *max_relres = h->body->max_relres;
+  return O3G_OK;
+}
+
+extern "C" int32_t o3g_rk2_body_strengths(const o3g_rk2_t* h, float* const* ts, float* solution, void* stream) {
+  if (!h || !h->body) return O3G_ERR_STATE;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t np = (size_t)h->body->surf.np;
+  if (ts)
+    for (int d = 0; d < 3; ++d)
+      if (ts[d]) O3G_CUDA_TRY(cudaMemcpyAsync(ts[d], h->body->ts[d], np * sizeof(float), cudaMemcpyDefault, st));
+  if (solution)
+    O3G_CUDA_TRY(cudaMemcpyAsync(solution, h->body->sol, np * h->body->nunk * sizeof(float), cudaMemcpyDefault, st));
+  O3G_CUDA_TRY(cudaStreamSynchronize(st));
   return O3G_OK;
 }

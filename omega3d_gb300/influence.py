@@ -257,6 +257,12 @@ def surface_struct(arr, nunk=3):
     return s
 
 
+def _panel_prec(env):
+    if env.precision not in ("plain", "compensated"):
+        raise ValueError("panel influence runs in 'plain' or 'compensated' precision")
+    return L.PRECS[env.precision]
+
+
 def panels_affect_points(src, targ, restype=None, env=None, maxlev=3, arrays=None):
     """Influence.h:557: accumulate the velocity (and gradients) of the panels of `src` at the
     points of `targ`.  `arrays` (from src.device_arrays) selects device memory; otherwise
@@ -270,7 +276,8 @@ def panels_affect_points(src, targ, restype=None, env=None, maxlev=3, arrays=Non
         raise ValueError("surface and targets must live in the same memory")
     tug = (ctypes.c_void_p * 9)(*_rows(targ.ug, 9)) if grads else None
     sss = _rows(a["ps"], 3)[2] if src.nunk == 3 else None
-    st = L.lib().o3g_panels_affect_points(L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev, a["x"].shape[1],
+    st = L.lib().o3g_panels_affect_points(_panel_prec(env), L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev,
+                                          a["x"].shape[1],
                                           *_rows(a["x"], 3), a["area"].shape[0], _base(a["idx"]), _base(a["area"]),
                                           *_rows(a["ts"], 3), sss, targ.n, *_rows(targ.x, 3), *_rows(targ.u, 3),
                                           tug, env.stream_handle(on_dev))
@@ -284,7 +291,8 @@ def points_affect_panels(src, targ, env=None, maxlev=3, arrays=None, pu=None):
     a = arrays or {"x": targ.x, "idx": targ.idx, "area": targ.area}
     pu = targ.pu if pu is None else pu
     on_dev = _is_dev(a["x"])
-    st = L.lib().o3g_points_affect_panels(L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev, src.n, *_rows(src.x, 3),
+    st = L.lib().o3g_points_affect_panels(_panel_prec(env), L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev, src.n,
+                                          *_rows(src.x, 3),
                                           *_rows(src.s, 3), a["x"].shape[1], *_rows(a["x"], 3), a["area"].shape[0],
                                           _base(a["idx"]), _base(a["area"]), *_rows(pu, 3),
                                           env.stream_handle(on_dev))
@@ -459,6 +467,31 @@ class Ralston:
         self.stream.wait_stream(torch.cuda.current_stream(self.x.device))
         L.check(L.lib().o3g_rk2_step(self.h, dt, fsd, nsteps, self.stream.cuda_stream), "o3g_rk2_step")
         torch.cuda.current_stream(self.x.device).wait_stream(self.stream)
+
+    def attach_body(self, surfaces, bem, maxlev=3, tol=1e-10, max_iter=30, arrays=None):
+        """Adds a fixed body (Surfaces) whose BEM system (`bem`, np * nunk unknowns) is solved
+        at every stage for that stage's particles (solve_bem inside find_derivs,
+        Convection.h:188-202); steps then run directly, not from a graph."""
+        self.body_arrays = arrays or surfaces.device_arrays(self.x.device)
+        self.body_struct = surface_struct(self.body_arrays)
+        self.body_bem = bem
+        L.check(L.lib().o3g_rk2_attach_body(self.h, ctypes.byref(self.body_struct), surfaces.nunk, maxlev, bem.h,
+                                            tol, max_iter, self.stream.cuda_stream), "o3g_rk2_attach_body")
+
+    def body_stats(self):
+        n, it, rr, mx = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_double(), ctypes.c_double()
+        L.check(L.lib().o3g_rk2_body_stats(self.h, ctypes.byref(n), ctypes.byref(it), ctypes.byref(rr),
+                                           ctypes.byref(mx)), "o3g_rk2_body_stats")
+        return {"solves": n.value, "last_refinements": it.value, "last_relres": rr.value, "max_relres": mx.value}
+
+    def body_strengths(self):
+        """(ts[3, np], solution[np * nunk]) of the last stage solved, as numpy arrays."""
+        npan = self.body_struct.np
+        ts = np.zeros((3, npan), np.float32)
+        sol = np.zeros(self.body_bem.n, np.float32)
+        L.check(L.lib().o3g_rk2_body_strengths(self.h, (ctypes.c_void_p * 3)(*_rows(ts, 3)), sol.ctypes.data,
+                                               self.stream.cuda_stream), "o3g_rk2_body_strengths")
+        return ts, sol
 
     def velocities(self):
         """Stage-1 velocity and gradient device pointers of the last step (u[3], ug[9])."""

@@ -257,3 +257,47 @@ def ralston_step(x, s, r, elong, dt, core="rm", prec=1, fs=(0.0, 0.0, 0.0), nthr
     uc = u1.copy()
     points_move_rk2(x0, s0, e0, uc, ug1, u2, ug2, dt, 0.25, 0.75)
     return x0, s0, e0, u1, ug1
+
+
+def solve_bem_body(x, s, body, A64, nunk, fs, core="rm", prec=1, maxlev=3):
+    """solve_bem (BEMHelper.h:43-265) for one fixed body and one particle set: panel velocities
+    from the particles (points_affect_panels, Influence.h:1107-1221, velocity only), freestream
+    (finalize_vels, ElementBase.h:187-193), vels_to_rhs_panels (RHS.h:92-110), the system
+    solved in FP64 with the matrix A64 (rows = targets), and Surfaces::set_str
+    (Surfaces.h:267-335).  body: dict with nodes, idx, area, x1, x2, norm.
+    Returns (ts[3, np], sss[np] or None, solution)."""
+    pu = points_affect_panels(x, s, body["nodes"], body["idx"], body["area"], core, prec, maxlev)
+    pu = pu.astype(np.float32)
+    finalize_vels(pu, None, fs)
+    rhs = vels_to_rhs_panels(pu, body["x1"], body["x2"], body["norm"], nunk)
+    sol = np.linalg.solve(A64, rhs.astype(np.float64)).astype(np.float32)
+    ts = sheet_to_panel_strength(sol[0::nunk], sol[1::nunk], body["x1"], body["x2"], body["area"])
+    sss = np.ascontiguousarray(sol[2::nunk]) if nunk == 3 else None
+    return ts, sss, sol
+
+
+def coupled_ralston_step(x, s, r, elong, body, A64, nunk, dt, fs=(1.0, 0.0, 0.0), core="rm", prec=1, maxlev=3):
+    """One Ralston RK2 step of vortex particles around one fixed body (Convection.h:349-425
+    with find_derivs, Convection.h:188-202): at each stage the BEM is solved for the stage's
+    particles, then velocity + gradient = particles (points_affect_points) + panels
+    (panels_affect_points), each summed into float like the reference's += of per-call
+    accumulators, then finalize_vels.  clear_inner_layer is not applied.
+    Returns new (x, s, elong) and the stage-2 solution."""
+    def derivs(xs, ss):
+        ts, sss, sol = solve_bem_body(xs, ss, body, A64, nunk, fs, core, prec, maxlev)
+        u, ug = points_affect_points(xs, r, ss, xs, r, True, core, prec)
+        u, ug = u.astype(np.float32), ug.astype(np.float32)
+        up, gp = panels_affect_points(body["nodes"], body["idx"], body["area"], ts, xs, sss, True, core, prec,
+                                      maxlev)
+        u = (u + up.astype(np.float32)).astype(np.float32)
+        ug = (ug + gp.astype(np.float32)).astype(np.float32)
+        finalize_vels(u, ug, fs)
+        return u, ug, sol
+    x0, s0, e0 = x.copy(), s.copy(), elong.copy()
+    u1, ug1, _ = derivs(x0, s0)
+    xi, si, ei = x0.copy(), s0.copy(), e0.copy()
+    points_move_euler(xi, si, ei, u1, ug1, 2.0 / 3.0 * dt, 1.0)
+    u2, ug2, sol2 = derivs(xi, si)
+    uc = u1.copy()
+    points_move_rk2(x0, s0, e0, uc, ug1, u2, ug2, dt, 0.25, 0.75)
+    return x0, s0, e0, sol2
