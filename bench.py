@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--skip-bem-fp64", action="store_true", help="skip the FP64 LU comparator (~50 s)")
     ap.add_argument("--skip-ring", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--only", choices=["bem", "ring", "batch", "coupled"], default=None,
+                    help="run one workload section alone and print its results (profiling)")
+    ap.add_argument("--coupled-steps", type=int, default=2,
+                    help="coupled sphere + 1M-particle Ralston steps to time (0 skips; 20 = the full run)")
     return ap.parse_args()
 
 
@@ -404,6 +408,103 @@ def bench_batch(args, G, torch, W, flush):
     return out
 
 
+def bench_coupled(args, G, torch, W):
+    """Full coupled step at scale: unit sphere of 5,120 panels (4 icosahedral refinements,
+    2 unknowns per panel), 1,048,576 particles uniform in the wake box x in [1, 6],
+    |y|, |z| < 1.5 (seed 5, N(0, 1e-3^2) strengths, core radius 0.015), Rosenhead-Moore core,
+    compensated FP32.  Each Ralston step (dt = 0.005, freestream (1, 0, 0)) solves the BEM at
+    both stages for the stage's particles (RHS from 1,048,576 particles, the factorisation of
+    the fixed body reused) and sums particle->particle and panel->particle vel+grad.
+    Timed: the assembly + factorisation once, `--coupled-steps` steps, and the parts of one
+    stage separately; the particle-particle sums' error against the FP64 path on the same
+    GPU at 2,048 sampled particles (the panel sums are checked against FP64 by the tests)."""
+    from omega3d_gb300.metrics import linf_err, rel_err
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    n = 1048576
+    xs, idx = G.generate_ovoid(4, 2.0, 2.0, 2.0)
+    surf = G.Surfaces(xs, idx, nunk=2)
+    px, ps, pr = W.wake_particles(n, seed=5)
+    X, S, R, E = t(px), t(ps), t(pr), torch.ones(n, device="cuda")
+    env = G.ExecEnv("rm", "compensated")
+    out = {"panels": surf.npanels, "unknowns": surf.npanels * 2, "particles": n, "core": "rm",
+           "precision": "compensated", "dt": 0.005}
+    rk = G.Ralston(X, S, R, E, env=env, use_graph=False)
+    bem = G.BEM(surf.npanels * 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rk.attach_body(surf, bem)
+    torch.cuda.synchronize()
+    out["assemble_factor_ms"] = (time.perf_counter() - t0) * 1e3
+
+    # the parts of one stage on the initial state
+    arr = rk.body_arrays
+    P = G.Points(X, S, R)
+    e = [ev() for _ in range(4)]
+    P.zero_vels()
+    G.points_affect_points(P, P, G.ResultsType(), env)                  # warm-up
+    torch.cuda.synchronize()
+    pu = torch.zeros(3, surf.npanels, device="cuda")
+    e[0].record()
+    G.points_affect_panels(P, surf, env, arrays=arr, pu=pu)
+    e[1].record()
+    rng = np.random.default_rng(6)
+    surf.set_sheet_strengths(rng.normal(size=surf.npanels).astype(np.float32) * 0.1,
+                             rng.normal(size=surf.npanels).astype(np.float32) * 0.1)
+    arr2 = surf.device_arrays("cuda")
+    torch.cuda.synchronize()
+    e[2].record()
+    G.panels_affect_points(surf, P, G.ResultsType(), env, arrays=arr2)
+    e[3].record()
+    torch.cuda.synchronize()
+    pairs = float(n) * n
+    rhs_ms, pair_ms, pan_ms = e[0].elapsed_time(e[1]), None, e[2].elapsed_time(e[3])
+    e0, e1 = ev(), ev()
+    P.zero_vels()
+    e0.record()
+    G.points_affect_points(P, P, G.ResultsType(), env)
+    e1.record()
+    torch.cuda.synchronize()
+    pair_ms = e0.elapsed_time(e1)
+    out["stage_parts_ms"] = {"rhs_points_affect_panels": rhs_ms, "particle_particle": pair_ms,
+                             "panel_particle": pan_ms}
+    out["particle_particle_interactions_per_s"] = pairs / (pair_ms * 1e-3)
+    out["panel_particle_pairs_per_s"] = float(surf.npanels) * n / (pan_ms * 1e-3)
+
+    # error of the compensated particle-particle sums at sampled particles vs the FP64 path
+    # (P holds the particle sums plus the panel sums of the last call: evaluate again)
+    P.zero_vels()
+    G.points_affect_points(P, P, G.ResultsType(), env)
+    sub = np.linspace(0, n - 1, 2048).astype(np.int64)
+    tq = G.Points(t(px[:, sub].astype(np.float64)), None, t(pr[sub].astype(np.float64)))
+    G.points_affect_points(G.Points(t(px.astype(np.float64)), t(ps.astype(np.float64)), t(pr.astype(np.float64))),
+                           tq, G.ResultsType(), G.ExecEnv("rm", "fp64"))
+    u, g = P.u.cpu().numpy()[:, sub], P.ug.cpu().numpy()[:, sub]
+    u64, g64 = tq.u.cpu().numpy(), tq.ug.cpu().numpy()
+    out["particle_particle_errors_vs_fp64"] = {
+        "u_max": rel_err(u, u64)[0], "u_rms": rel_err(u, u64)[1], "grad_max": rel_err(g, g64)[0],
+        "u_linf": linf_err(u, u64), "grad_linf": linf_err(g, g64), "samples": 2048}
+    del P, tq
+
+    steps = args.coupled_steps
+    e0, e1 = ev(), ev()
+    torch.cuda.synchronize()
+    e0.record(rk.stream)
+    rk.step(0.005, (1.0, 0.0, 0.0), steps)
+    e1.record(rk.stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = rk.body_stats()
+    out["steps"] = steps
+    out["step_ms"] = ms / steps
+    out["interactions_per_step"] = 2 * (pairs + float(surf.npanels) * n * 2)
+    out["bem"] = st
+    out["finite"] = bool(torch.isfinite(X).all().item())
+    del rk, bem
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -420,9 +521,21 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     lib = L.lib()
 
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    if args.only:
+        # one workload section alone (for profiling it); prints that section's results only
+        fn = {"bem": lambda: bench_bem(args, G, torch, W, fp64=not args.skip_bem_fp64),
+              "ring": lambda: bench_ring(args, G, torch, W),
+              "batch": lambda: bench_batch(args, G, torch, W, flush),
+              "coupled": lambda: bench_coupled(args, G, torch, W)}[args.only]
+        res = fn()
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"section": args.only, "result": res}))
+        return
+
     x, s, r = W.gaussian_cloud(args.n, seed=2)
     X, S, R = (torch.from_numpy(a).to(dev) for a in (x, s, r))
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
 
     nsm = int(torch.cuda.get_device_properties(dev).multi_processor_count)
@@ -561,6 +674,9 @@ def run_ours(args):
     batch = None
     if not args.skip_batch:
         batch = bench_batch(args, G, torch, W, flush)
+    coupled = None
+    if args.coupled_steps > 0:
+        coupled = bench_coupled(args, G, torch, W)
 
     if rank == 0:
         cpu_v, cpu_cores, cpu_sample, _ = cpu_reference(args)
@@ -588,7 +704,7 @@ def run_ours(args):
             "fp64_same_gpu": fp64 and {"value": fp64["value"], "unit": UNIT, "targets": fp64["targets"],
                                        "compensated_speedup": local_rate / fp64["value"]},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_sample},
-            "bem_solve": bem, "ring_rk2": ring, "batch": batch,
+            "bem_solve": bem, "ring_rk2": ring, "batch": batch, "coupled": coupled,
             "clocks": clk, "gpu_launches": comp_launches, "num_sms": nsm,
             "wall_s_timed_region": comp_wall,
         }
