@@ -246,14 +246,17 @@ int32_t o3g_rk2_destroy(o3g_rk2_t* h);
  * points' sums before finalize_vels, as Convection::find_vels does (Convection.h:131-182).
  * The matrix (nunk unknowns per panel, subdivision maxlev) is assembled into `bem` and
  * factorised here, once: the body does not move.  The pair and panel sums use the handle's
- * precision.  Steps with a body run directly (the solves' convergence checks read the
- * residual on the host), not from a graph.  clear_inner_layer (Reflect.h) is not applied. */
+ * precision.  With ips > 0, particles and field points are pushed out of the body after the
+ * interim move and after the combine (clear_inner_layer method 1 with cutoff 0.5/sqrt(2 pi)
+ * * ips, Convection.h:372,381,423-424); ips = 0 skips that.  Steps with a body run
+ * directly (the solves' convergence checks read the residual on the host), not from a graph. */
 int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, int32_t nunk, int32_t maxlev, o3g_bem_t* bem,
-                            double tol, int32_t max_iter, void* stream);
+                            double tol, int32_t max_iter, float ips, void* stream);
 /* Solve statistics of the attached body: number of solves, refinements and relative residual
- * of the last one, the largest final residual over all solves. */
+ * of the last one, the largest final residual over all solves, and the number of points
+ * pushed out of the body so far (synchronises the device when `pushed` is given). */
 int32_t o3g_rk2_body_stats(const o3g_rk2_t* h, int64_t* solves, int32_t* last_iters, double* last_relres,
-                           double* max_relres);
+                           double* max_relres, int64_t* pushed);
 /* Copies the body's panel strengths ts[3] (np each) and BEM solution (np * nunk) of the last
  * stage solved into the caller's arrays (host or device; either may be NULL) and waits. */
 int32_t o3g_rk2_body_strengths(const o3g_rk2_t* h, float* const* ts, float* solution, void* stream);
@@ -320,6 +323,17 @@ int32_t o3g_batch_plan(int32_t nsys, const int32_t* np, const int32_t* nf, int32
 int32_t o3g_batch_rk2_create(int32_t core, int32_t prec, int32_t nsys, const int32_t* np, const int32_t* nf,
                              float* const* x, float* const* s, float* r, float* elong, float* const* fx,
                              int32_t use_graph, o3g_rk2_t** h);
+
+/* ---- clear_inner_layer ------------------------------------------------------------------
+ * Replaces clear_inner_panp2 method 1 (Reflect.h:446-656): every one of the n points (device
+ * arrays x, y, z, moved in place) whose height above its closest panels -- the mean normal
+ * and mean contact point of every panel within 10 float epsilon of the closest squared
+ * distance (Reflect.h:56-183 per panel) -- is below cutoff_mult * ips is pushed out to that
+ * height along the mean normal.  surf: device arrays with nodes, idx and normals.  The
+ * positions are bit-identical to the reference's float arithmetic.  With npushed given the
+ * call waits and returns the number pushed; otherwise it is asynchronous. */
+int32_t o3g_clear_inner_layer(int32_t n, float* x, float* y, float* z, const o3g_surface_t* surf, float cutoff_mult,
+                              float ips, int32_t* npushed, void* stream);
 
 /* ---- points_affect_points without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory

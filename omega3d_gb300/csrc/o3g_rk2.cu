@@ -11,10 +11,14 @@
 // and is captured once into a CUDA graph that later steps replay (o3g_rk2_step).
 #include "o3g_batch.cuh"
 
+#include <cmath>
 #include <cstring>
 #include <vector>
 
 namespace o3g {
+
+int32_t clear_inner_layer_dev(int n, float* x, float* y, float* z, const o3g_surface_t& surf, float cut,
+                              int* dev_count, cudaStream_t st);
 
 template <int C>
 int32_t ptpt_core_f(const PtPtCall& c, const float* sx, const float* sy, const float* sz, const float* sr,
@@ -220,6 +224,8 @@ struct o3g_rk2 {
     int max_iter = 30;
     float* buf = nullptr;
     float *pu[3], *rhs, *sol, *ts[3], *sss;
+    float cut = 0.0f;                   // cutoff height of clear_inner_layer (0: not applied)
+    int* pushed = nullptr;              // device count of points pushed
     long long solves = 0;
     int last_iters = 0;
     double last_relres = 0.0, max_relres = 0.0;
@@ -319,6 +325,13 @@ static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStrea
       note_launch();
     }
   }
+  // push interim particles and field points out of the body (Convection.h:372,381)
+  if (h->body && h->body->cut > 0.0f) {
+    O3G_TRY(clear_inner_layer_dev(n, h->xi[0], h->xi[1], h->xi[2], h->body->surf, h->body->cut, h->body->pushed, st));
+    if (nf > 0)
+      O3G_TRY(clear_inner_layer_dev(nf, h->fxi[0], h->fxi[1], h->fxi[2], h->body->surf, h->body->cut, h->body->pushed,
+                                    st));
+  }
   O3G_TRY(rk2_eval(h, 1, fs, st));
   O3G_TRY(o3g_points_finalize(n, fs, h->u2, h->ug2, st));
   if (nf > 0) O3G_TRY(o3g_points_finalize(nf, fs, h->fu2, h->fug2, st));
@@ -326,6 +339,12 @@ static int32_t rk2_one_step(o3g_rk2_t* h, double dt, const double* fs, cudaStrea
   O3G_TRY(o3g_points_move_rk2(n, dt, 0.25, h->u1, h->ug1, 0.75, h->u2, h->ug2, h->x, h->s, h->elong, st));
   if (nf > 0) O3G_TRY(o3g_points_move_rk2(nf, dt, 0.25, h->fu1, nullptr, 0.75, h->fu2, nullptr, h->f, nullptr,
                                           nullptr, st));
+  // and the final positions (Convection.h:423-424)
+  if (h->body && h->body->cut > 0.0f) {
+    O3G_TRY(clear_inner_layer_dev(n, h->x[0], h->x[1], h->x[2], h->body->surf, h->body->cut, h->body->pushed, st));
+    if (nf > 0)
+      O3G_TRY(clear_inner_layer_dev(nf, h->f[0], h->f[1], h->f[2], h->body->surf, h->body->cut, h->body->pushed, st));
+  }
   return O3G_OK;
 }
 
@@ -511,10 +530,10 @@ extern "C" int32_t o3g_rk2_velocities(o3g_rk2_t* h, float** u, float** ug) {
 }
 
 extern "C" int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, int32_t nunk, int32_t maxlev,
-                                       o3g_bem_t* bem, double tol, int32_t max_iter, void* stream) {
+                                       o3g_bem_t* bem, double tol, int32_t max_iter, float ips, void* stream) {
   if (!h || !surf || !bem || (nunk != 2 && nunk != 3) || maxlev < 0 || maxlev > 4 || surf->np < 1 ||
-      !(tol >= 0.0) || max_iter < 1) {
-    set_error("o3g_rk2_attach_body: bad arguments (nunk 2 or 3, maxlev 0..4, np >= 1)");
+      !(tol >= 0.0) || max_iter < 1 || !(ips >= 0.0f) || (ips > 0.0f && (!surf->nx || !surf->ny || !surf->nz))) {
+    set_error("o3g_rk2_attach_body: bad arguments (nunk 2 or 3, maxlev 0..4, np >= 1, ips >= 0, normals)");
     return O3G_ERR_INVALID_ARG;
   }
   if (h->batch || h->body) {
@@ -542,7 +561,7 @@ extern "C" int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, 
   b->max_iter = max_iter;
   const size_t pa = align_up((size_t)surf->np * sizeof(float));
   const size_t ua = align_up((size_t)surf->np * nunk * sizeof(float));
-  cudaError_t e = cudaMalloc((void**)&b->buf, 7 * pa + 2 * ua);
+  cudaError_t e = cudaMalloc((void**)&b->buf, 7 * pa + 2 * ua + 256);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     delete b;
@@ -555,14 +574,31 @@ extern "C" int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, 
   b->sol = (float*)p; p += ua;
   for (int d = 0; d < 3; ++d) { b->ts[d] = (float*)p; p += pa; }
   b->sss = (float*)p;
+  p += pa;
+  b->pushed = (int*)p;
+  // the reference passes 0.5/sqrt(2 pi) as S and multiplies by _ips in S (Convection.h:372)
+  b->cut = ips > 0.0f ? (float)(0.5 / std::sqrt(2.0 * 3.14159265358979323846)) * ips : 0.0f;
+  e = cudaMemset(b->pushed, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    cudaFree(b->buf);
+    delete b;
+    set_error_cuda("o3g_rk2_attach_body: cudaMemset", e);
+    return O3G_ERR_CUDA;
+  }
   h->body = b;
   h->use_graph = false;
   return O3G_OK;
 }
 
 extern "C" int32_t o3g_rk2_body_stats(const o3g_rk2_t* h, int64_t* solves, int32_t* last_iters, double* last_relres,
-                                      double* max_relres) {
+                                      double* max_relres, int64_t* pushed) {
   if (!h || !h->body) return O3G_ERR_STATE;
+  if (pushed) {
+    int v = 0;
+    O3G_CUDA_TRY(cudaDeviceSynchronize());
+    O3G_CUDA_TRY(cudaMemcpy(&v, h->body->pushed, sizeof(int), cudaMemcpyDeviceToHost));
+    *pushed = v;
+  }
   if (solves) *solves = h->body->solves;
   if (last_iters) *last_iters = h->body->last_iters;
   if (last_relres) *last_relres = h->body->last_relres;

@@ -299,6 +299,19 @@ def points_affect_panels(src, targ, env=None, maxlev=3, arrays=None, pu=None):
     L.check(st, "o3g_points_affect_panels")
 
 
+def clear_inner_layer(bdry, targ, cutoff_mult=0.5 / np.sqrt(2.0 * np.pi), ips=0.01, arrays=None, stream=None):
+    """clear_inner_layer method 1 (Reflect.h:446-656): push the points of `targ` (torch CUDA
+    [3, n] positions) that lie below the cutoff layer of `bdry` out along the mean normal.
+    Returns the number of points pushed."""
+    a = arrays or bdry.device_arrays(targ.x.device)
+    s = surface_struct(a)
+    n = ctypes.c_int32()
+    h = stream if stream is not None else ExecEnv().stream_handle(True)
+    L.check(L.lib().o3g_clear_inner_layer(targ.n, *_rows(targ.x, 3), ctypes.byref(s), cutoff_mult, ips,
+                                          ctypes.byref(n), h), "o3g_clear_inner_layer")
+    return n.value
+
+
 def panels_on_panels_coeff(src_arrays, targ_arrays, nunk, is_self, out, ld=None, maxlev=3, stream=None):
     """Coefficients.h:169: write the column-major (ntarg*nunk) x (nsrc*nunk) block into the
     device tensor `out` (viewed with leading dimension ld, default ntarg*nunk)."""
@@ -468,21 +481,23 @@ class Ralston:
         L.check(L.lib().o3g_rk2_step(self.h, dt, fsd, nsteps, self.stream.cuda_stream), "o3g_rk2_step")
         torch.cuda.current_stream(self.x.device).wait_stream(self.stream)
 
-    def attach_body(self, surfaces, bem, maxlev=3, tol=1e-10, max_iter=30, arrays=None):
+    def attach_body(self, surfaces, bem, maxlev=3, tol=1e-10, max_iter=30, ips=0.0, arrays=None):
         """Adds a fixed body (Surfaces) whose BEM system (`bem`, np * nunk unknowns) is solved
         at every stage for that stage's particles (solve_bem inside find_derivs,
-        Convection.h:188-202); steps then run directly, not from a graph."""
+        Convection.h:188-202); with ips > 0 points are pushed out of the body after each move
+        (clear_inner_layer, Convection.h:372,381,423-424).  Steps then run directly."""
         self.body_arrays = arrays or surfaces.device_arrays(self.x.device)
         self.body_struct = surface_struct(self.body_arrays)
         self.body_bem = bem
         L.check(L.lib().o3g_rk2_attach_body(self.h, ctypes.byref(self.body_struct), surfaces.nunk, maxlev, bem.h,
-                                            tol, max_iter, self.stream.cuda_stream), "o3g_rk2_attach_body")
+                                            tol, max_iter, ips, self.stream.cuda_stream), "o3g_rk2_attach_body")
 
     def body_stats(self):
-        n, it, rr, mx = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_double(), ctypes.c_double()
+        n, it, rr, mx, pu = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
         L.check(L.lib().o3g_rk2_body_stats(self.h, ctypes.byref(n), ctypes.byref(it), ctypes.byref(rr),
-                                           ctypes.byref(mx)), "o3g_rk2_body_stats")
-        return {"solves": n.value, "last_refinements": it.value, "last_relres": rr.value, "max_relres": mx.value}
+                                           ctypes.byref(mx), ctypes.byref(pu)), "o3g_rk2_body_stats")
+        return {"solves": n.value, "last_refinements": it.value, "last_relres": rr.value, "max_relres": mx.value,
+                "pushed": pu.value}
 
     def body_strengths(self):
         """(ts[3, np], solution[np * nunk]) of the last stage solved, as numpy arrays."""

@@ -10,6 +10,9 @@
 #   src/Kernels.h     (streamed; its `#include "CoreFunc.h"` is dropped because the
 #                      switched CoreFunc.h precedes it in the same stream)
 #   oracle/ref_driver.cpp (this project's restatement of the loops around them)
+# and oracle/_ref/libo3dref_reflect.so from the reference's Reflect.h (streamed without
+# its includes of Omega3D.h / Points.h / Surfaces.h, which need Eigen and Vc; the
+# declarations it uses come from oracle/reflect_prelude.h) with oracle/ref_reflect_driver.cpp.
 #
 # The reference location defaults to /root/reference/src; set O3D_REFERENCE_SRC to
 # override.  When the sources are absent (e.g. on a machine without the reference) the
@@ -41,3 +44,14 @@ for core in RM WL EXP V2; do
         -o "$OUT/libo3dref_$lc.so"
   echo "build_ref: built $OUT/libo3dref_$lc.so"
 done
+if [ -f "$REF/Reflect.h" ]; then
+  {
+    cat "$HERE/reflect_prelude.h"
+    sed -e 's|^#include "Omega3D.h"|/* declared in reflect_prelude.h */|' \
+        -e 's|^#include "Points.h"|/* declared in reflect_prelude.h */|' \
+        -e 's|^#include "Surfaces.h"|/* declared in reflect_prelude.h */|' "$REF/Reflect.h"
+    cat "$HERE/ref_reflect_driver.cpp"
+  } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w -I"$REF" -x c++ - \
+        -o "$OUT/libo3dref_reflect.so"
+  echo "build_ref: built $OUT/libo3dref_reflect.so"
+fi

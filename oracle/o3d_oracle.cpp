@@ -27,6 +27,7 @@
 #include <vector>
 #include <unordered_map>
 #include <algorithm>
+#include <limits>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -997,3 +998,123 @@ extern "C" int o3o_flops_per_pair(int core, int grads, int have_tr) {
   return 23 + (have_tr ? tv[core] : tp[core]);
 }
 
+
+// ---------------------------------------------------------------------------------------
+// clear_inner_layer, method 1 (Reflect.h:446-656): push every point that lies below the
+// cutoff layer of the closest panels out along their mean normal.  Called by
+// Convection::advect_2nd_ralston after the interim move and after the combine
+// (Convection.h:372,381,423-424) with cutoff_mult = 0.5/sqrt(2 pi).
+namespace {
+
+template <class S> S rdot(S a0, S a1, S a2, S b0, S b1, S b2) { return a0 * b0 + a1 * b1 + a2 * b2; }
+
+// closest point of triangle (0,1,2) with unit normal n to t: Reflect.h:56-183
+// (corners, then edges, then the interior prism; later tests overwrite earlier ones)
+template <class S>
+void closest_on_panel(S x0, S y0, S z0, S x1, S y1, S z1, S x2, S y2, S z2, S nx, S ny, S nz, S tx, S ty, S tz,
+                      S* distsq, S* cx, S* cy, S* cz) {
+  S best = (S)9.9e+9, px = 0, py = 0, pz = 0;
+  const S a0 = tx - x0, a1 = ty - y0, a2 = tz - z0;
+  const S b0 = tx - x1, b1 = ty - y1, b2 = tz - z1;
+  const S c0 = tx - x2, c1 = ty - y2, c2 = tz - z2;
+  const S da = rdot(a0, a1, a2, a0, a1, a2);
+  if (da < best) { best = da; px = x0; py = y0; pz = z0; }
+  const S db = rdot(b0, b1, b2, b0, b1, b2);
+  if (db < best) { best = db; px = x1; py = y1; pz = z1; }
+  const S dc = rdot(c0, c1, c2, c0, c1, c2);
+  if (dc < best) { best = dc; px = x2; py = y2; pz = z2; }
+  // edges: squared distance to the line |e x d|^2 / |e|^2, kept when the foot lies inside
+  auto edge = [&](S e0, S e1, S e2, S d0, S d1, S d2, S ox, S oy, S oz) {
+    const S inv = (S)(1.0 / rdot(e0, e1, e2, e0, e1, e2));
+    const S r0 = e1 * d2 - e2 * d1, r1 = e2 * d0 - e0 * d2, r2 = e0 * d1 - e1 * d0;
+    const S dl = rdot(r0, r1, r2, r0, r1, r2) * inv;
+    if (dl < best) {
+      const S t = rdot(e0, e1, e2, d0, d1, d2) * inv;
+      if (0.0 < t && t < 1.0) {
+        best = dl;
+        px = ox + t * e0; py = oy + t * e1; pz = oz + t * e2;
+      }
+    }
+  };
+  const S e01x = x1 - x0, e01y = y1 - y0, e01z = z1 - z0;
+  edge(e01x, e01y, e01z, a0, a1, a2, x0, y0, z0);
+  const S e12x = x2 - x1, e12y = y2 - y1, e12z = z2 - z1;
+  edge(e12x, e12y, e12z, b0, b1, b2, x1, y1, z1);
+  const S e20x = x0 - x2, e20y = y0 - y2, e20z = z0 - z2;
+  edge(e20x, e20y, e20z, c0, c1, c2, x2, y2, z2);
+  // inside all three edge half-spaces: the foot of the normal
+  auto side = [&](S e0, S e1, S e2, S d0, S d1, S d2) {
+    const S i0 = ny * e2 - nz * e1, i1 = nz * e0 - nx * e2, i2 = nx * e1 - ny * e0;
+    return rdot(d0, d1, d2, i0, i1, i2);
+  };
+  const S s01 = side(e01x, e01y, e01z, a0, a1, a2);
+  const S s12 = side(e12x, e12y, e12z, b0, b1, b2);
+  const S s20 = side(e20x, e20y, e20z, c0, c1, c2);
+  if (s01 > 0.0 && s12 > 0.0 && s20 > 0.0) {
+    const S h = rdot(a0, a1, a2, nx, ny, nz);
+    best = h * h;
+    px = tx - nx * h; py = ty - ny * h; pz = tz - nz * h;
+  }
+  *distsq = best; *cx = px; *cy = py; *cz = pz;
+}
+
+template <class S>
+int clear_inner(int n, S* x, int nn, const S* nodes, int np, const uint32_t* idx, const S* norm, S cutoff_mult, S ips,
+                int nthreads) {
+  const S* nx = nodes; const S* ny = nodes + nn; const S* nz = nodes + 2 * (size_t)nn;
+  const S* snx = norm; const S* sny = norm + np; const S* snz = norm + 2 * (size_t)np;
+  S* tx = x; S* ty = x + n; S* tz = x + 2 * (size_t)n;
+  const S eps = (S)(10.0 * std::numeric_limits<S>::epsilon());
+  const S cut = cutoff_mult * ips;
+  int pushed = 0;
+#pragma omp parallel for num_threads(nthreads) reduction(+:pushed) schedule(dynamic, 64)
+  for (int i = 0; i < n; ++i) {
+    S mind = std::numeric_limits<S>::max();
+    S mn[3] = {0, 0, 0}, mc[3] = {0, 0, 0};
+    int nh = 0;
+    for (int j = 0; j < np; ++j) {
+      const uint32_t p0 = idx[3 * (size_t)j], p1 = idx[3 * (size_t)j + 1], p2 = idx[3 * (size_t)j + 2];
+      S d2, cx, cy, cz;
+      closest_on_panel<S>(nx[p0], ny[p0], nz[p0], nx[p1], ny[p1], nz[p1], nx[p2], ny[p2], nz[p2], snx[j], sny[j],
+                          snz[j], tx[i], ty[i], tz[i], &d2, &cx, &cy, &cz);
+      if (d2 < mind - eps) {
+        // a new closest set: the running sums restart from this panel
+        mind = d2;
+        mn[0] = (S)0 + snx[j]; mn[1] = (S)0 + sny[j]; mn[2] = (S)0 + snz[j];
+        mc[0] = (S)0 + cx; mc[1] = (S)0 + cy; mc[2] = (S)0 + cz;
+        nh = 1;
+      } else if (d2 < mind + eps) {
+        mn[0] += snx[j]; mn[1] += sny[j]; mn[2] += snz[j];
+        mc[0] += cx; mc[1] += cy; mc[2] += cz;
+        ++nh;
+      }
+    }
+    if (nh == 0) continue;
+    // normalizeVec (MathHelper.h:186-192): 1/sqrt in double, rounded to S
+    const S len = (S)(1.0 / std::sqrt(mn[0] * mn[0] + mn[1] * mn[1] + mn[2] * mn[2]));
+    for (int d = 0; d < 3; ++d) mn[d] *= len;
+    for (int d = 0; d < 3; ++d) mc[d] /= (S)nh;
+    const S dx0 = tx[i] - mc[0], dx1 = ty[i] - mc[1], dx2 = tz[i] - mc[2];
+    const S dotp = rdot(mn[0], mn[1], mn[2], dx0, dx1, dx2) - cut;
+    if (dotp < 0.0) {
+      tx[i] -= dotp * mn[0];
+      ty[i] -= dotp * mn[1];
+      tz[i] -= dotp * mn[2];
+      ++pushed;
+    }
+  }
+  return pushed;
+}
+
+}  // namespace
+
+// x: [3][n] points (moved in place); returns the number pushed, or -1 on bad arguments
+extern "C" int o3o_clear_inner_layer(int prec, int n, void* x, int nn, const void* nodes, int np, const uint32_t* idx,
+                                     const void* norm, double cutoff_mult, double ips, int nthreads) {
+  if (n < 0 || np < 1 || nn < 3) return -1;
+  if (prec == 2)
+    return clear_inner<double>(n, (double*)x, nn, (const double*)nodes, np, idx, (const double*)norm, cutoff_mult, ips,
+                               nthreads);
+  return clear_inner<float>(n, (float*)x, nn, (const float*)nodes, np, idx, (const float*)norm, (float)cutoff_mult,
+                            (float)ips, nthreads);
+}

@@ -276,13 +276,16 @@ def solve_bem_body(x, s, body, A64, nunk, fs, core="rm", prec=1, maxlev=3):
     return ts, sss, sol
 
 
-def coupled_ralston_step(x, s, r, elong, body, A64, nunk, dt, fs=(1.0, 0.0, 0.0), core="rm", prec=1, maxlev=3):
+def coupled_ralston_step(x, s, r, elong, body, A64, nunk, dt, fs=(1.0, 0.0, 0.0), core="rm", prec=1, maxlev=3,
+                         ips=0.0):
     """One Ralston RK2 step of vortex particles around one fixed body (Convection.h:349-425
     with find_derivs, Convection.h:188-202): at each stage the BEM is solved for the stage's
     particles, then velocity + gradient = particles (points_affect_points) + panels
     (panels_affect_points), each summed into float like the reference's += of per-call
-    accumulators, then finalize_vels.  clear_inner_layer is not applied.
-    Returns new (x, s, elong) and the stage-2 solution."""
+    accumulators, then finalize_vels.  With ips > 0 the interim and the final positions are
+    pushed out of the body (clear_inner_layer method 1, cutoff 0.5/sqrt(2 pi) * ips,
+    Convection.h:372,423).  Returns new (x, s, elong) and the stage-2 solution."""
+    cut = float(np.float32(0.5 / np.sqrt(2.0 * np.pi)))
     def derivs(xs, ss):
         ts, sss, sol = solve_bem_body(xs, ss, body, A64, nunk, fs, core, prec, maxlev)
         u, ug = points_affect_points(xs, r, ss, xs, r, True, core, prec)
@@ -297,7 +300,41 @@ def coupled_ralston_step(x, s, r, elong, body, A64, nunk, dt, fs=(1.0, 0.0, 0.0)
     u1, ug1, _ = derivs(x0, s0)
     xi, si, ei = x0.copy(), s0.copy(), e0.copy()
     points_move_euler(xi, si, ei, u1, ug1, 2.0 / 3.0 * dt, 1.0)
+    if ips > 0:
+        clear_inner_layer(xi, body["nodes"], body["idx"], body["norm"], cut, ips)
     u2, ug2, sol2 = derivs(xi, si)
     uc = u1.copy()
     points_move_rk2(x0, s0, e0, uc, ug1, u2, ug2, dt, 0.25, 0.75)
+    if ips > 0:
+        clear_inner_layer(x0, body["nodes"], body["idx"], body["norm"], cut, ips)
     return x0, s0, e0, sol2
+
+
+def clear_inner_layer(x, nodes, idx, norm, cutoff_mult=0.5 / np.sqrt(2.0 * np.pi), ips=0.01, prec=0, nthreads=0,
+                      use_ref=False):
+    """clear_inner_layer method 1 (Reflect.h:446-656) in place on x[3, n]: points below the
+    cutoff layer (cutoff_mult * ips above the closest panels) are pushed out along the mean
+    normal of the closest panels.  Returns the number of points pushed."""
+    dt = np.float64 if prec == 2 else np.float32
+    assert x.dtype == dt and x.flags["C_CONTIGUOUS"]
+    nx, nm = _as(nodes, dt), _as(norm, dt)
+    idx = np.ascontiguousarray(idx, np.uint32)
+    n, nn, np_ = x.shape[1], nx.shape[1], nm.shape[1]
+    if use_ref:
+        path = os.path.join(REF_DIR, "libo3dref_reflect.so")
+        if "reflect" not in _ref:
+            _ref["reflect"] = ctypes.CDLL(path)
+        rc = _ref["reflect"].ref_clear_inner_layer(ctypes.c_int(prec), ctypes.c_int(n), _p(x), ctypes.c_int(nn),
+                                                   _p(nx), ctypes.c_int(np_), _p(idx), _p(nm),
+                                                   ctypes.c_double(cutoff_mult), ctypes.c_double(ips))
+    else:
+        rc = lib().o3o_clear_inner_layer(ctypes.c_int(prec), ctypes.c_int(n), _p(x), ctypes.c_int(nn), _p(nx),
+                                         ctypes.c_int(np_), _p(idx), _p(nm), ctypes.c_double(cutoff_mult),
+                                         ctypes.c_double(ips), ctypes.c_int(_nthreads(nthreads)))
+    if rc < 0:
+        raise RuntimeError("oracle clear_inner_layer failed")
+    return int(rc)
+
+
+def ref_reflect_available():
+    return os.path.exists(os.path.join(REF_DIR, "libo3dref_reflect.so"))

@@ -2,9 +2,11 @@
 
 Run in a checkout that has the reference sources (oracle/build_ref.sh compiles
 src/Kernels.h, src/CoreFunc.h and src/MathHelper.h of the reference into
-oracle/_ref/libo3dref_<core>.so; the loops around them are oracle/ref_driver.cpp):
+oracle/_ref/libo3dref_<core>.so, and src/Reflect.h into oracle/_ref/libo3dref_reflect.so;
+the loops around them are oracle/ref_driver.cpp and oracle/ref_reflect_driver.cpp):
 
-    sh oracle/build_ref.sh && python tests/golden/make_golden.py
+    sh oracle/build_ref.sh && python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py --only reflect                       # reflect.npz alone
 
 Every fixture holds its seeded inputs and the outputs of the reference build for the
 precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
@@ -54,7 +56,37 @@ def sphere_inputs(levels=1, scale=2.0, seed=13):
     return dict(nodes=nodes, idx=idx, x1=x1, x2=x2, norm=nm, area=area, ps0=ps0, ps1=ps1, sss=sss, ts=ts)
 
 
+def reflect_inputs(levels=2, scale=2.0, seed=15, n=1500):
+    """Points around and inside a sphere, on its nodes and just inside them."""
+    nodes, idx = O.generate_ovoid(levels, scale, scale, scale)
+    x1, x2, nm, area = O.compute_bases(nodes, idx)
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(3, n))
+    d /= np.linalg.norm(d, axis=0)
+    pts = (d * rng.uniform(0.85, 1.06, n)).astype(np.float32)
+    k = min(100, nodes.shape[1])
+    pts = np.concatenate([pts, nodes[:, :k].copy(), (nodes[:, :k] * np.float32(0.995)).astype(np.float32)], axis=1)
+    return dict(nodes=nodes, idx=idx, norm=nm), np.ascontiguousarray(pts)
+
+
+def write_reflect():
+    if not O.ref_reflect_available():
+        raise SystemExit("oracle/_ref/libo3dref_reflect.so missing: run sh oracle/build_ref.sh")
+    geo, pts = reflect_inputs()
+    out = {}
+    for prec in (0, 2):
+        x = pts.astype(np.float64 if prec == 2 else np.float32).copy()
+        out["npushed_p%d" % prec] = np.array(O.clear_inner_layer(x, geo["nodes"], geo["idx"], geo["norm"],
+                                                                  ips=0.05, prec=prec, use_ref=True))
+        out["x_p%d" % prec] = x
+    _save("reflect.npz", {"pinned": True, "method": 1, "ips": 0.05, "cutoff_mult": "0.5/sqrt(2 pi)",
+                          "source": "reference Reflect.h"}, x_in=pts, **geo, **out)
+
+
 def main():
+    if "--only" in sys.argv and sys.argv[-1] == "reflect":
+        write_reflect()
+        return
     for core in O.REF_CORES:
         if not O.ref_available(core):
             raise SystemExit("oracle/_ref/libo3dref_%s.so missing: run sh oracle/build_ref.sh" % core)
@@ -105,6 +137,7 @@ def main():
         arrays["nodes_L%d" % lev], arrays["idx_L%d" % lev] = n, i
     _save("sphere.npz", {"pinned": False, "scale": 2.0, "source": "oracle restatement of generate_ovoid"},
           **arrays)
+    write_reflect()
 
 
 if __name__ == "__main__":

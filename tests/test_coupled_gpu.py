@@ -11,6 +11,8 @@ Tolerances:
     particle displacements per particle <= 1e-4 relative, strength changes L-infinity
     <= 1e-4, the stage-2 BEM solution <= 1e-4 relative to its largest entry (the GPU matrix
     differs from the oracle's FP32 one by summation order, <= 1e-5 elementwise).
+  * clear_inner_layer: bit-identical to the reference's Reflect.h (golden) and the oracle.
+  * with ips > 0 the coupled step also pushes particles out of the body after both moves.
   * potential flow around the sphere from tracer particles (zero strength): RMS error of
     the velocity <= 2e-2 of the freestream at radius 1.3-1.6 (discretisation of 1,280 panels).
 """
@@ -91,25 +93,53 @@ def _particles(n, seed):
     return x, s.astype(np.float32), r, rng
 
 
-@pytest.mark.parametrize("nunk", [2, 3])
-def test_coupled_ralston_step_vs_oracle(cuda, nunk):
+def test_clear_inner_layer_bit_exact(cuda):
+    import json
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reflect.npz"))
+    ips = json.loads(str(d["meta"]))["ips"]
+    x1, x2, nm, area = O.compute_bases(d["nodes"], d["idx"])
+    s = G.Surfaces(d["nodes"], d["idx"], nunk=2)
+    arr = s.device_arrays("cuda")
+    X = _t(d["x_in"])
+    n = G.clear_inner_layer(s, G.Points(X, None, None, inert=True), ips=ips, arrays=arr)
+    assert n == int(d["npushed_p0"])
+    assert np.array_equal(X.cpu().numpy(), d["x_p0"])
+    # a larger case against the oracle
+    s3 = _sphere(3, 2)
+    rng = np.random.default_rng(12)
+    v = rng.normal(size=(3, 50000))
+    v /= np.linalg.norm(v, axis=0)
+    pts = (v * rng.uniform(0.9, 1.1, 50000)).astype(np.float32)
+    ref = pts.copy()
+    no = O.clear_inner_layer(ref, s3.x, s3.idx, s3.norm, ips=0.02)
+    X = _t(pts)
+    ng = G.clear_inner_layer(s3, G.Points(X, None, None, inert=True), ips=0.02)
+    assert ng == no and np.array_equal(X.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("nunk,ips", [(2, 0.0), (3, 0.0), (2, 0.03)])
+def test_coupled_ralston_step_vs_oracle(cuda, nunk, ips):
     import torch
     s = _sphere(2, nunk)
     x, sv, r, _ = _particles(2400, 31)
+    if ips > 0:
+        x[:, :200] *= np.float32(0.97)      # some particles inside the body: pushed out
     e = np.ones(x.shape[1], np.float32)
     dt, fs = 0.005, (1.0, 0.0, 0.0)
     X, S, R, E = _t(x), _t(sv), _t(r), _t(e)
     rk = G.Ralston(X, S, R, E, env=G.ExecEnv("rm", "compensated"))
     bem = G.BEM(s.npanels * nunk)
-    rk.attach_body(s, bem)
+    rk.attach_body(s, bem, ips=ips)
     rk.step(dt, fs, 1)
     torch.cuda.synchronize()
     st = rk.body_stats()
     assert st["solves"] == 2 and st["max_relres"] <= 1e-10
+    assert (st["pushed"] > 0) == (ips > 0)
     _, sol_gpu = rk.body_strengths()
     geo = _body(s)
     A = O.panels_on_panels_coeff(geo, geo, nunk, True, "rm", 0).T.astype(np.float64)
-    xo, so, eo, sol_o = O.coupled_ralston_step(x, sv, r, e, geo, A, nunk, dt, fs, "rm", 1)
+    xo, so, eo, sol_o = O.coupled_ralston_step(x, sv, r, e, geo, A, nunk, dt, fs, "rm", 1, ips=ips)
     Xg, Sg, Eg = X.cpu().numpy(), S.cpu().numpy(), E.cpu().numpy()
     assert rel_err(Xg - x, xo - x)[0] <= 1e-4
     assert linf_err(Sg - sv, so - sv) <= 1e-4
@@ -163,10 +193,11 @@ def test_attach_body_rejects_bad_arguments(cuda):
     st = G.influence.surface_struct(arr)
     lib = L.lib()
     wrong = G.BEM(s.npanels * 3)
-    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, wrong.h, 1e-10, 30, None) == 1
+    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, wrong.h, 1e-10, 30, 0.0, None) == 1
     right = G.BEM(s.npanels * 2)
-    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 5, right.h, 1e-10, 30, None) == 1
-    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 4, 3, right.h, 1e-10, 30, None) == 1
-    assert lib.o3g_rk2_body_stats(rk.h, None, None, None, None) == 9
-    L.check(lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, None), "attach")
-    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, None) == 9
+    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 5, right.h, 1e-10, 30, 0.0, None) == 1
+    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 4, 3, right.h, 1e-10, 30, 0.0, None) == 1
+    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, -1.0, None) == 1
+    assert lib.o3g_rk2_body_stats(rk.h, None, None, None, None, None) == 9
+    L.check(lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, 0.0, None), "attach")
+    assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, 0.0, None) == 9

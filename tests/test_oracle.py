@@ -205,3 +205,57 @@ def test_flop_counts_match_reference_accounting():
     assert O.flops_per_pair("wl", True, True) == 70
     assert O.flops_per_pair("exp", True, True) == 68
     assert O.flops_per_pair("rm", False, True) == 30
+
+
+# ---- clear_inner_layer (Reflect.h) ---------------------------------------------------
+def test_oracle_clear_inner_layer_matches_golden():
+    d, meta = _gold("reflect.npz")
+    assert meta["pinned"] and meta["method"] == 1
+    for prec in (0, 2):
+        x = d["x_in"].astype(np.float64 if prec == 2 else np.float32).copy()
+        n = O.clear_inner_layer(x, d["nodes"], d["idx"], d["norm"], ips=meta["ips"], prec=prec)
+        assert n == int(d["npushed_p%d" % prec]) and n > 0
+        assert _exact(x, d["x_p%d" % prec])
+
+
+def test_oracle_clear_inner_layer_bit_exact_vs_reference():
+    if not O.ref_reflect_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    nodes, idx = O.generate_ovoid(3, 2.0, 2.0, 2.0)
+    _, _, nm, _ = O.compute_bases(nodes, idx)
+    rng = np.random.default_rng(8)
+    d = rng.normal(size=(3, 4000))
+    d /= np.linalg.norm(d, axis=0)
+    pts = (d * rng.uniform(0.95, 1.02, 4000)).astype(np.float32)
+    # points on node-edge-face boundaries: node positions and edge midpoints
+    mid = (0.5 * (nodes[:, idx[0::3]] + nodes[:, idx[1::3]])).astype(np.float32)
+    pts = np.ascontiguousarray(np.concatenate([pts, nodes, mid], axis=1))
+    for prec in (0, 2):
+        for ips in (0.0, 0.02, 0.1):
+            a = pts.astype(np.float64 if prec == 2 else np.float32).copy()
+            b = a.copy()
+            na = O.clear_inner_layer(a, nodes, idx, nm, ips=ips, prec=prec)
+            nb = O.clear_inner_layer(b, nodes, idx, nm, ips=ips, prec=prec, use_ref=True)
+            assert na == nb and _exact(a, b)
+
+
+def test_clear_inner_layer_leaves_points_at_the_cutoff():
+    nodes, idx = O.generate_ovoid(2, 2.0, 2.0, 2.0)
+    _, _, nm, _ = O.compute_bases(nodes, idx)
+    rng = np.random.default_rng(9)
+    d = rng.normal(size=(3, 3000))
+    d /= np.linalg.norm(d, axis=0)
+    x = (d * rng.uniform(0.5, 1.5, 3000)).astype(np.float32)
+    x0 = x.copy()
+    ips = 0.04
+    n = O.clear_inner_layer(x, nodes, idx, nm, ips=ips)
+    moved = np.any(x != x0, axis=0)
+    assert n == moved.sum() and n > 0
+    # pushed points end up near the cutoff layer outside the body, untouched ones were outside
+    cut = 0.5 / np.sqrt(2 * np.pi) * ips
+    assert np.linalg.norm(x0[:, ~moved], axis=0).min() > 0.95
+    # a second pass only nudges points left a rounding error below the layer (1 ulp), or
+    # near an edge whose closest-panel set changed, by far less than the cutoff height
+    y = x.copy()
+    O.clear_inner_layer(y, nodes, idx, nm, ips=ips)
+    assert np.abs(y - x).max() <= 0.01 * cut
