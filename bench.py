@@ -204,6 +204,14 @@ def bench_bem(args, G, torch, W, fp64=True):
                    "assemble_ms": e[1].elapsed_time(e[2]), "factor_ms": e[2].elapsed_time(e[3]),
                    "solve_ms": e[3].elapsed_time(e[4]), "refinements": bem.iters, "relres": bem.relres,
                    "total_ms": e[0].elapsed_time(e[4])}
+            # the reference's own method on the same assembled matrix: GMRES, no factorisation
+            e[5].record()
+            xg = bem.solve(rhs, tol=1e-10, max_iter=300, method="gmres")
+            e[6].record()
+            torch.cuda.synchronize()
+            res["gmres"] = {"solve_ms": e[5].elapsed_time(e[6]), "iterations": bem.iters, "relres": bem.relres,
+                            "total_ms_with_rhs_and_assembly": e[0].elapsed_time(e[2]) + e[5].elapsed_time(e[6]),
+                            "strengths_vs_lu_max_rel": float(((xg - xs).abs().max() / xs.abs().max()).item())}
         if fp64 and nunk == 2:
             A = torch.empty((n, n), device="cuda")
             G.panels_on_panels_coeff(arr, arr, nunk, True, A)
@@ -221,6 +229,9 @@ def bench_bem(args, G, torch, W, fp64=True):
             res["fp64_lu_relres"] = float((torch.linalg.norm(bd - Ad @ xd) / torch.linalg.norm(bd)).item())
             res["strengths_vs_fp64_lu_max_rel"] = float(((xs.double() - xd).abs().max() / xd.abs().max()).item())
             res["speedup_vs_fp64_lu"] = res["fp64_lu_solve_ms"] / (res["factor_ms"] + res["solve_ms"])
+            res["gmres"]["speedup_vs_fp64_lu"] = res["fp64_lu_solve_ms"] / res["gmres"]["solve_ms"]
+            res["gmres"]["strengths_vs_fp64_lu_max_rel"] = float(((xg.double() - xd).abs().max() /
+                                                                  xd.abs().max()).item())
             del Ad, LU, piv
         out["nunk%d" % nunk] = res
         del bem

@@ -182,10 +182,11 @@ int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int32_t is_self
 /* ---- BEM system ------------------------------------------------------------------------
  * Replaces BEM<S,I> (BEM.h:44-234).  The handle owns the device-resident n x n FP32 matrix
  * (column-major, leading dimension from o3g_bem_matrix), its LU factors and scratch.
- * The reference solves with Eigen GMRES (BEM.h:182-202); here the matrix is factorised
- * in FP32 with partial pivoting and TF32 tensor-core trailing updates, and solutions are
- * refined with residuals b - A x formed in FP64 until ||r||/||b|| <= tol (the residual
- * the reference prints, BEM.h:227-230). */
+ * The reference solves with Eigen GMRES (BEM.h:182-202).  Here either the matrix is
+ * factorised in FP32 with partial pivoting and TF32 tensor-core trailing updates and
+ * solutions are refined with FP64-accurate residuals b - A x (o3g_bem_factor +
+ * o3g_bem_solve), or GMRES runs on the unfactored matrix (o3g_bem_solve_gmres); both stop
+ * at ||r||/||b|| <= tol, the residual the reference prints (BEM.h:227-230). */
 typedef struct o3g_bem o3g_bem_t;
 /* number of unknowns of the system */
 int32_t o3g_bem_size(const o3g_bem_t* h, int64_t* n);
@@ -206,6 +207,13 @@ int32_t o3g_bem_factor(o3g_bem_t* h, void* stream);
  * when tol is not reached within max_iter refinements (x still holds the best iterate) */
 int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
                       int32_t max_iter, int32_t* iters, double* relres, void* stream);
+/* solve A x = b without factorising: restarted GMRES(restart), the reference's own method
+ * (Eigen GMRES, BEM.h:182-202), with FP64 Krylov vectors and FP64-accurate products of the
+ * FP32 matrix, until ||b - A x|| / ||b|| <= tol (checked on the true residual at every
+ * restart) or max_iter iterations; arguments otherwise as o3g_bem_solve.  Needs only the
+ * assembled matrix (o3g_bem_matrix / o3g_bem_set_block). */
+int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
+                            int32_t max_iter, int32_t restart, int32_t* iters, double* relres, void* stream);
 /* finalize_vels of panel velocities (u = fs + u/(4 pi), ElementBase.h:187-193) and
  * vels_to_rhs_panels (RHS.h:92-110) in one pass; device arrays; rhs has np*nunk entries */
 int32_t o3g_panel_vels_to_rhs(int32_t np, int32_t nunk, const double* fs, float* pu, float* pv, float* pw,

@@ -108,6 +108,8 @@ def _declare(l):
     l.o3g_bem_factor.argtypes = [P, P]
     l.o3g_bem_solve.restype = c_i32
     l.o3g_bem_solve.argtypes = [P, P, P, P, c_i32, c_d, c_i32, P, P, P]
+    l.o3g_bem_solve_gmres.restype = c_i32
+    l.o3g_bem_solve_gmres.argtypes = [P, P, P, P, c_i32, c_d, c_i32, c_i32, P, P, P]
     l.o3g_panel_vels_to_rhs.restype = c_i32
     l.o3g_panel_vels_to_rhs.argtypes = [c_i32, c_i32, P, P, P, P, P, P, P]
     l.o3g_points_finalize.restype = c_i32

@@ -13,9 +13,13 @@
 //       - k_laswp: the panel's row interchanges applied to the other columns;
 //       - k_trsm_unit_lower: U12 = L11^-1 A12, one warp per column, L11 in shared memory;
 //       - trailing update A22 -= L21 U12 as a TF32 tensor-core GEMM (cuBLAS, a plain GEMM);
-//   * iterative refinement: residuals r = b - A x formed in FP64 from the unfactored FP32
-//     matrix and the FP64 iterate, corrections from the FP32 factors (forward/back
-//     substitution in one cooperative kernel each), until ||r||/||b|| <= tol.
+//   * iterative refinement: residuals r = b - A x formed FP64-accurately (double-single
+//     FP32 arithmetic, k_matvec_ds) from the unfactored FP32 matrix and the FP64 iterate,
+//     corrections from the FP32 factors (forward/back substitution in one cooperative kernel
+//     each), until ||r||/||b|| <= tol;
+//   * or, without any factorisation, restarted GMRES -- the reference's own solver
+//     (BEM.h:182-202) -- with FP64 Krylov vectors, classical Gram-Schmidt with one
+//     reorthogonalisation, and the same FP64-accurate products (o3g_bem_solve_gmres).
 // Every grid barrier here spins at most kSpinLimit rounds, then sets an error flag that all
 // blocks check, so a fault in the barrier logic ends the kernel instead of hanging.
 #include "o3g_common.cuh"
@@ -463,52 +467,6 @@ __global__ void __launch_bounds__(kSolveThreads) k_trsv_upper(TrsvArgs a) {
   }
 }
 
-// FP64 residual partials: part[cb][i] = sum_{j in chunk cb} A(i,j) x(j)
-__global__ void k_resid_part(const float* __restrict__ A, long long ld, int n, const double* __restrict__ x,
-                             int cchunk, double* __restrict__ part) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cb = blockIdx.y;
-  if (i >= n) return;
-  const int j0 = cb * cchunk, j1 = min(n, j0 + cchunk);
-  double s[4] = {0.0, 0.0, 0.0, 0.0};
-  int j = j0;
-  for (; j + 8 <= j1; j += 8) {
-    float av[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) av[q] = __ldg(A + (size_t)(j + q) * ld + i);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) s[q & 3] = fma((double)av[q], x[j + q], s[q & 3]);
-  }
-  for (; j < j1; ++j) s[0] = fma((double)A[(size_t)j * ld + i], x[j], s[0]);
-  part[(size_t)cb * n + i] = (s[0] + s[1]) + (s[2] + s[3]);
-}
-// r = b - sum_cb part[cb]; also accumulates ||r||^2 and ||b||^2 per block into nrm[2*blockIdx]
-__global__ void k_resid_finish(const double* __restrict__ part, int ncb, int n, const double* __restrict__ b,
-                               double* __restrict__ r, double* __restrict__ nrm) {
-  __shared__ double s1[8], s2[8];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double rr = 0.0, bb = 0.0;
-  if (i < n) {
-    double s = 0.0;
-    for (int k = 0; k < ncb; ++k) s += part[(size_t)k * n + i];
-    const double ri = b[i] - s;
-    r[i] = ri;
-    rr = ri * ri;
-    bb = b[i] * b[i];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    rr += __shfl_xor_sync(0xffffffffu, rr, o);
-    bb += __shfl_xor_sync(0xffffffffu, bb, o);
-  }
-  if ((threadIdx.x & 31) == 0) { s1[threadIdx.x >> 5] = rr; s2[threadIdx.x >> 5] = bb; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a1 = 0.0, a2 = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a1 += s1[w]; a2 += s2[w]; }
-    nrm[2 * blockIdx.x] = a1;
-    nrm[2 * blockIdx.x + 1] = a2;
-  }
-}
 __global__ void k_axpy_f2d(double* x, const float* d, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] += (double)d[i];
@@ -520,6 +478,85 @@ __global__ void k_f2d(const float* s, double* d, int n) {
 __global__ void k_d2f(const double* s, float* d, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) d[i] = (float)s[i];
+}
+
+// ---- FP64-accurate products of the FP32 matrix without the FP64 pipe --------------------
+// x (double) is split into xh + xl (floats, ~48 significant bits together).  Each product
+// a * xh is formed error-free (p + e, e = fma(a, xh, -p)), a * xl in one fma, and the row
+// sum is carried as a double-single pair (hi, lo) with Knuth's two-sum, renormalised every
+// 8 columns.  About 10 FP32 instructions per matrix element: the kernel streams the matrix
+// at HBM speed, where the same sum on the FP64 pipe is limited by its rate.
+constexpr int kMvChunk = 1024;   // columns per block (blockIdx.y)
+
+__global__ void k_split_f64(const double* __restrict__ x, float* xh, float* xl, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  const float h = (float)v;
+  xh[i] = h;
+  xl[i] = (float)(v - (double)h);
+}
+
+__device__ __forceinline__ void ds_add_product(float a, float h, float l, float& hi, float& lo) {
+  const float p = __fmul_rn(a, h);
+  const float e = fmaf(a, h, -p);
+  const float s = __fadd_rn(hi, p);
+  const float bb = __fsub_rn(s, hi);
+  const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  hi = s;
+  lo = fmaf(a, l, __fadd_rn(lo, __fadd_rn(t, e)));
+}
+
+// part[cb][i] = sum over the columns of chunk cb of A[i, j] x[j]
+__global__ void __launch_bounds__(256) k_matvec_ds(const float* __restrict__ A, long long ld, int n,
+                                                   const float* __restrict__ xh, const float* __restrict__ xl,
+                                                   double* __restrict__ part) {
+  __shared__ float sh[kMvChunk], sl[kMvChunk];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cb = blockIdx.y;
+  const int j0 = cb * kMvChunk, m = min(n - j0, kMvChunk);
+  for (int k = threadIdx.x; k < m; k += blockDim.x) { sh[k] = xh[j0 + k]; sl[k] = xl[j0 + k]; }
+  __syncthreads();
+  if (i >= n) return;
+  const float* a = A + (size_t)j0 * ld + i;
+  float hi = 0.f, lo = 0.f;
+  int k = 0;
+  for (; k + 8 <= m; k += 8) {
+    float av[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) av[q] = __ldg(a + (size_t)(k + q) * ld);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ds_add_product(av[q], sh[k + q], sl[k + q], hi, lo);
+    // renormalise: move the bulk of lo into hi (Dekker's fast two-sum, |hi| >= |lo|)
+    const float s2 = __fadd_rn(hi, lo);
+    lo = __fsub_rn(lo, __fsub_rn(s2, hi));
+    hi = s2;
+  }
+  for (; k < m; ++k) ds_add_product(__ldg(a + (size_t)k * ld), sh[k], sl[k], hi, lo);
+  part[(size_t)cb * n + i] = (double)hi + (double)lo;
+}
+
+// y = b - sum_cb part (b != null) or y = sum_cb part; per-block sums of y^2 into nrm
+__global__ void k_matvec_finish(const double* __restrict__ part, int ncb, int n, const double* __restrict__ b,
+                                double* __restrict__ y, double* __restrict__ nrm) {
+  __shared__ double s1[8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double yy = 0.0;
+  if (i < n) {
+    double s = 0.0;
+    for (int k = 0; k < ncb; ++k) s += part[(size_t)k * n + i];
+    const double v = b ? b[i] - s : s;
+    y[i] = v;
+    yy = v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) yy += __shfl_xor_sync(0xffffffffu, yy, o);
+  if ((threadIdx.x & 31) == 0) s1[threadIdx.x >> 5] = yy;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a1 += s1[w];
+    if (nrm) nrm[blockIdx.x] = a1;
+  }
 }
 
 // finalize_vels of the panel velocities (u = fs + u/(4 pi) in double, ElementBase.h:187-193
@@ -895,10 +932,9 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   const long long ld = h->ld;
   DeviceFacts df;
   O3G_TRY(device_facts(&df));
-  const int cchunk = 1024;
-  const int ncb = (n + cchunk - 1) / cchunk;
+  const int ncb = (n + kMvChunk - 1) / kMvChunk;
   const int nrb = (n + 255) / 256;
-  const size_t need = align_up((size_t)n * 8) * 3 + align_up((size_t)n * 4) * 3 + align_up((size_t)ncb * n * 8) +
+  const size_t need = align_up((size_t)n * 8) * 3 + align_up((size_t)n * 4) * 5 + align_up((size_t)ncb * n * 8) +
                       align_up((size_t)nrb * 16);
   O3G_TRY(bem_scratch(h, need));
   Carve cv(h->scratch);
@@ -908,6 +944,8 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   float* bf = cv.take<float>(n);
   float* y = cv.take<float>(n);
   float* xf = cv.take<float>(n);
+  float* xh = cv.take<float>(n);
+  float* xl = cv.take<float>(n);
   double* part = cv.take<double>((size_t)ncb * n);
   double* nrm = cv.take<double>(2 * (size_t)nrb);
   O3G_CUDA_TRY(cudaMemcpyAsync(bf, b, (size_t)n * 4, mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice
@@ -926,26 +964,25 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   ta.LU = h->LU; ta.dinv = h->dinv; ta.ld = ld; ta.n = n; ta.y = y;
   ta.bar = Barrier{(unsigned*)(h->flags + 2), (unsigned*)(h->flags + 3), h->flags};
   void* targs[] = {&ta};
-  std::vector<double> hn(2 * (size_t)nrb);
+  std::vector<double> hn((size_t)nrb);
   double rel = 1.0, bnorm = 0.0;
   int it = 0;
   KernelTimer& tm = thread_timer();
   tm.begin(st);
   for (it = 0; it <= max_iter; ++it) {
+    // r = b - A x in FP64-accurate double-single arithmetic (r = b at x = 0)
     if (it > 0) {
-      k_resid_part<<<dim3(nrb, ncb), 256, 0, st>>>(h->A, ld, n, xd, cchunk, part);
-      note_launch();
-    } else {
-      // r = b at x = 0 (part = 0 is implied): reuse the finish kernel with zero partials
-      O3G_CUDA_TRY(cudaMemsetAsync(part, 0, (size_t)n * 8, st));
+      k_split_f64<<<nrb, 256, 0, st>>>(xd, xh, xl, n);
+      k_matvec_ds<<<dim3(nrb, ncb), 256, 0, st>>>(h->A, ld, n, xh, xl, part);
+      note_launch(2);
     }
-    k_resid_finish<<<nrb, 256, 0, st>>>(part, it > 0 ? ncb : 1, n, bd, rd, nrm);
+    k_matvec_finish<<<nrb, 256, 0, st>>>(part, it > 0 ? ncb : 0, n, bd, rd, nrm);
     note_launch();
-    O3G_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, 2 * (size_t)nrb * 8, cudaMemcpyDeviceToHost, st));
+    O3G_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, (size_t)nrb * 8, cudaMemcpyDeviceToHost, st));
     O3G_CUDA_TRY(cudaStreamSynchronize(st));
-    double rr = 0.0, bb = 0.0;
-    for (int k = 0; k < nrb; ++k) { rr += hn[2 * k]; bb += hn[2 * k + 1]; }
-    bnorm = std::sqrt(bb);
+    double rr = 0.0;
+    for (int k = 0; k < nrb; ++k) rr += hn[k];
+    if (it == 0) bnorm = std::sqrt(rr);
     rel = bnorm > 0.0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
     if (rel <= tol || it == max_iter) break;
     k_permute_to_float<<<nrb, 256, 0, st>>>(rd, h->perm, y, n);
@@ -976,6 +1013,174 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
     char msg[160];
     std::snprintf(msg, sizeof(msg), "o3g_bem_solve: relative residual %.3e after %d refinements (tol %.1e)", rel, it,
                   tol);
+    set_error(msg);
+    return O3G_ERR_NOT_CONVERGED;
+  }
+  return O3G_OK;
+}
+
+// ---- GMRES: the reference's solver (Eigen GMRES, BEM.h:182-202) ----------------------------
+// Restarted GMRES(m) on the unfactored FP32 matrix: FP64 Krylov vectors, classical
+// Gram-Schmidt with one reorthogonalisation (cuBLAS DGEMV on the n x (k+1) basis), Givens
+// rotations of the small Hessenberg matrix on the host, FP64-accurate matrix products
+// (k_matvec_ds).  The true residual ||b - A x|| / ||b|| (BEM.h:227-230) is recomputed at
+// every restart and decides convergence.  No preconditioner: the vortex-sheet rows of the
+// matrix have a zero diagonal (Coefficients.h:414-436), where a Jacobi preconditioner is
+// the identity.
+extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
+                                       int32_t max_iter, int32_t restart, int32_t* iters, double* relres,
+                                       void* stream) {
+  O3G_TRY(bem_check(h));
+  if (!b || (mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || max_iter < 1 || restart < 1 || restart > 500 ||
+      !(tol >= 0.0)) {
+    set_error("o3g_bem_solve_gmres: bad arguments (max_iter >= 1, restart 1..500, tol >= 0)");
+    return O3G_ERR_INVALID_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = h->n;
+  const long long ld = h->ld;
+  const int m = std::min(restart, max_iter);
+  const int ncb = (n + kMvChunk - 1) / kMvChunk;
+  const int nrb = (n + 255) / 256;
+  const size_t need = align_up((size_t)(m + 1) * n * 8) + 2 * align_up((size_t)n * 8) + 4 * align_up((size_t)n * 4) +
+                      align_up((size_t)ncb * n * 8) + align_up((size_t)nrb * 8) + align_up((size_t)2 * (m + 1) * 8);
+  O3G_TRY(bem_scratch(h, need));
+  Carve cv(h->scratch);
+  double* V = cv.take<double>((size_t)(m + 1) * n);
+  double* bd = cv.take<double>(n);
+  double* xd = cv.take<double>(n);
+  float* bf = cv.take<float>(n);
+  float* xf = cv.take<float>(n);
+  float* xh = cv.take<float>(n);
+  float* xl = cv.take<float>(n);
+  double* part = cv.take<double>((size_t)ncb * n);
+  double* nrm = cv.take<double>(nrb);
+  double* hd = cv.take<double>(2 * (size_t)(m + 1));
+  if (cublasSetStream(h->cublas, st) != CUBLAS_STATUS_SUCCESS) {
+    set_error("o3g_bem_solve_gmres: cublasSetStream failed");
+    return O3G_ERR_CUDA;
+  }
+  cublasSetPointerMode(h->cublas, CUBLAS_POINTER_MODE_HOST);
+  O3G_CUDA_TRY(cudaMemcpyAsync(bf, b, (size_t)n * 4, mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice
+                                                                           : cudaMemcpyDeviceToDevice, st));
+  k_f2d<<<nrb, 256, 0, st>>>(bf, bd, n);
+  note_launch();
+  O3G_CUDA_TRY(cudaMemsetAsync(xd, 0, (size_t)n * 8, st));
+  std::vector<double> hn((size_t)nrb);
+  // y = b - A xin (bin given) or y = A xin; the squared norm of y when asked (synchronises)
+  auto matvec = [&](const double* xin, const double* bin, double* yout, double* norm2) -> int32_t {
+    int nc = 0;
+    if (xin) {
+      k_split_f64<<<nrb, 256, 0, st>>>(xin, xh, xl, n);
+      k_matvec_ds<<<dim3(nrb, ncb), 256, 0, st>>>(h->A, ld, n, xh, xl, part);
+      note_launch(2);
+      nc = ncb;
+    }
+    k_matvec_finish<<<nrb, 256, 0, st>>>(part, nc, n, bin, yout, nrm);
+    note_launch();
+    O3G_CUDA_TRY(cudaGetLastError());
+    if (norm2) {
+      O3G_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, (size_t)nrb * 8, cudaMemcpyDeviceToHost, st));
+      O3G_CUDA_TRY(cudaStreamSynchronize(st));
+      double s2 = 0.0;
+      for (int k = 0; k < nrb; ++k) s2 += hn[k];
+      *norm2 = s2;
+    }
+    return O3G_OK;
+  };
+  auto cublas_ok = [&](cublasStatus_t cs, const char* what) -> int32_t {
+    if (cs == CUBLAS_STATUS_SUCCESS) return O3G_OK;
+    set_error(what);
+    return O3G_ERR_CUDA;
+  };
+  double bb = 0.0;
+  O3G_TRY(matvec(nullptr, bd, V, &bb));           // V0 = b, ||b||^2
+  const double bnorm = std::sqrt(bb);
+  int total = 0;
+  double rel = 0.0;
+  KernelTimer& tm = thread_timer();
+  tm.begin(st);
+  if (bnorm > 0.0) {
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), hc(2 * (size_t)(m + 1));
+    auto Hat = [&](int i, int k) -> double& { return H[(size_t)k * (m + 1) + i]; };
+    const double one = 1.0, zero = 0.0, minus1 = -1.0;
+    for (;;) {
+      double rr = 0.0;
+      O3G_TRY(matvec(total > 0 ? xd : nullptr, bd, V, &rr));   // V0 = r = b - A x
+      rel = std::sqrt(rr) / bnorm;
+      if (rel <= tol || total >= max_iter) break;
+      const double beta = std::sqrt(rr);
+      const double ib = 1.0 / beta;
+      O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &ib, V, 1), "o3g_bem_solve_gmres: cublasDscal"));
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0] = beta;
+      int k = 0;
+      for (; k < m && total < max_iter;) {
+        double* vk = V + (size_t)k * n;
+        double* w = V + (size_t)(k + 1) * n;
+        O3G_TRY(matvec(vk, nullptr, w, nullptr));
+        // classical Gram-Schmidt, twice
+        for (int pass = 0; pass < 2; ++pass) {
+          double* hp = hd + (size_t)pass * (m + 1);
+          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_T, n, k + 1, &one, V, n, w, 1, &zero, hp, 1),
+                            "o3g_bem_solve_gmres: cublasDgemv"));
+          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, k + 1, &minus1, V, n, hp, 1, &one, w, 1),
+                            "o3g_bem_solve_gmres: cublasDgemv"));
+        }
+        double wn = 0.0;
+        O3G_TRY(cublas_ok(cublasDnrm2(h->cublas, n, w, 1, &wn), "o3g_bem_solve_gmres: cublasDnrm2"));
+        O3G_CUDA_TRY(cudaMemcpyAsync(hc.data(), hd, 2 * (size_t)(m + 1) * 8, cudaMemcpyDeviceToHost, st));
+        O3G_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int i = 0; i <= k; ++i) Hat(i, k) = hc[i] + hc[(size_t)(m + 1) + i];
+        Hat(k + 1, k) = wn;
+        if (wn > 0.0) {
+          const double iw = 1.0 / wn;
+          O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &iw, w, 1), "o3g_bem_solve_gmres: cublasDscal"));
+        }
+        // previous rotations, then a new one that zeroes H(k+1, k)
+        for (int i = 0; i < k; ++i) {
+          const double a = Hat(i, k), c = Hat(i + 1, k);
+          Hat(i, k) = cs[i] * a + sn[i] * c;
+          Hat(i + 1, k) = -sn[i] * a + cs[i] * c;
+        }
+        const double dd = std::hypot(Hat(k, k), Hat(k + 1, k));
+        cs[k] = dd > 0.0 ? Hat(k, k) / dd : 1.0;
+        sn[k] = dd > 0.0 ? Hat(k + 1, k) / dd : 0.0;
+        Hat(k, k) = dd;
+        Hat(k + 1, k) = 0.0;
+        g[k + 1] = -sn[k] * g[k];
+        g[k] = cs[k] * g[k];
+        ++k;
+        ++total;
+        if (std::fabs(g[k]) <= 0.5 * tol * bnorm || wn == 0.0) break;
+      }
+      // x += V y with H(0:k, 0:k) y = g(0:k)
+      for (int i = k - 1; i >= 0; --i) {
+        double sacc = g[i];
+        for (int j = i + 1; j < k; ++j) sacc -= Hat(i, j) * y[j];
+        y[i] = Hat(i, i) != 0.0 ? sacc / Hat(i, i) : 0.0;
+      }
+      O3G_CUDA_TRY(cudaMemcpyAsync(hd, y.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
+      O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, k, &one, V, n, hd, 1, &one, xd, 1),
+                        "o3g_bem_solve_gmres: cublasDgemv"));
+    }
+  }
+  tm.end(st);
+  k_d2f<<<nrb, 256, 0, st>>>(xd, xf, n);
+  note_launch();
+  if (x)
+    O3G_CUDA_TRY(cudaMemcpyAsync(x, xf, (size_t)n * 4, mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost
+                                                                            : cudaMemcpyDeviceToDevice, st));
+  if (x64)
+    O3G_CUDA_TRY(cudaMemcpyAsync(x64, xd, (size_t)n * 8, mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost
+                                                                              : cudaMemcpyDeviceToDevice, st));
+  O3G_CUDA_TRY(cudaStreamSynchronize(st));
+  if (iters) *iters = total;
+  if (relres) *relres = rel;
+  if (!(rel <= tol)) {
+    char msg[160];
+    std::snprintf(msg, sizeof(msg), "o3g_bem_solve_gmres: relative residual %.3e after %d iterations (tol %.1e)", rel,
+                  total, tol);
     set_error(msg);
     return O3G_ERR_NOT_CONVERGED;
   }

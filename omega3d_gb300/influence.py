@@ -384,9 +384,13 @@ class BEM:
         L.check(L.lib().o3g_bem_factor(self.h, ExecEnv(stream=stream).stream_handle(True)), "o3g_bem_factor")
         self.factored = True
 
-    def solve(self, b=None, tol=1e-10, max_iter=30, stream=None, x64=False):
-        """BEM::solve (BEM.h:169-234); returns the FP32 strengths (and FP64 ones if asked)."""
-        if not self.factored:
+    def solve(self, b=None, tol=1e-10, max_iter=30, stream=None, x64=False, method="lu", restart=60):
+        """BEM::solve (BEM.h:169-234); returns the FP32 strengths (and FP64 ones if asked).
+        method "lu": FP32/TF32 LU (factorised once per matrix) + refinement, max_iter
+        refinements; "gmres": restarted GMRES on the unfactored matrix, max_iter iterations."""
+        if method not in ("lu", "gmres"):
+            raise ValueError("method must be 'lu' or 'gmres'")
+        if method == "lu" and not self.factored:
             self.factor(stream)
         b = self.b if b is None else b
         on = _is_dev(b)
@@ -398,11 +402,15 @@ class BEM:
             b = np.ascontiguousarray(b, np.float32)
             x = np.empty(self.n, np.float32)
             xd = np.empty(self.n, np.float64) if x64 else None
-        st = L.lib().o3g_bem_solve(self.h, _base(b), _base(x), None if xd is None else _base(xd),
-                                   L.MEM_DEVICE if on else L.MEM_HOST, tol, max_iter, ctypes.byref(it),
-                                   ctypes.byref(rr), ExecEnv(stream=stream).stream_handle(on))
+        mem, sh = L.MEM_DEVICE if on else L.MEM_HOST, ExecEnv(stream=stream).stream_handle(on)
+        if method == "lu":
+            st = L.lib().o3g_bem_solve(self.h, _base(b), _base(x), None if xd is None else _base(xd), mem, tol,
+                                       max_iter, ctypes.byref(it), ctypes.byref(rr), sh)
+        else:
+            st = L.lib().o3g_bem_solve_gmres(self.h, _base(b), _base(x), None if xd is None else _base(xd), mem,
+                                             tol, max_iter, restart, ctypes.byref(it), ctypes.byref(rr), sh)
         self.iters, self.relres = it.value, rr.value
-        L.check(st, "o3g_bem_solve")
+        L.check(st, "o3g_bem_solve" if method == "lu" else "o3g_bem_solve_gmres")
         if not on:
             self.strengths = x
         return (x, xd) if x64 else x

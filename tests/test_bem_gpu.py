@@ -1,6 +1,7 @@
 """GPU tests of the BEM system through the C-ABI: FP32 LU with partial pivoting (TF32
-trailing updates) plus FP64-residual refinement, against an FP64 LU oracle (numpy/LAPACK
-on the same matrix) and the potential-flow known answer on a sphere.
+trailing updates) plus FP64-residual refinement, and GMRES on the unfactored matrix (the
+reference's own solver), against an FP64 LU oracle (numpy/LAPACK on the same matrix) and
+the potential-flow known answer on a sphere.
 
 Tolerances: refined solutions reach ||b - A x||/||b|| <= 1e-10 (FP64 residual of the FP32
 matrix) and agree with the FP64 LU solution of the same matrix to 1e-9 relative (the
@@ -18,11 +19,11 @@ from omega3d_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 
-def _solve(A, b, tol=1e-10, max_iter=30):
+def _solve(A, b, tol=1e-10, max_iter=30, method="lu", restart=60):
     n = A.shape[0]
     bem = G.BEM(n)
     bem.set_block(0, 0, np.ascontiguousarray(A.T.astype(np.float32)))   # column-major block
-    x, x64 = bem.solve(b.astype(np.float32), tol=tol, max_iter=max_iter, x64=True)
+    x, x64 = bem.solve(b.astype(np.float32), tol=tol, max_iter=max_iter, x64=True, method=method, restart=restart)
     return bem, x, x64
 
 
@@ -142,3 +143,55 @@ def test_panel_vels_to_rhs_matches_oracle(cuda):
         torch.cuda.synchronize()
         assert np.array_equal(rhs.cpu().numpy(), ref)
         assert np.array_equal(P.cpu().numpy(), pr)
+
+
+@pytest.mark.parametrize("n", [1, 7, 129, 1000, 2500])
+def test_gmres_matches_fp64_lu(cuda, n):
+    rng = np.random.default_rng(100 + n)
+    A = rng.normal(size=(n, n)) / np.sqrt(n) + 2.0 * np.eye(n)
+    b = rng.normal(size=n)
+    bem, x, x64 = _solve(A, b, method="gmres", max_iter=200)
+    A32 = A.astype(np.float32).astype(np.float64)
+    b32 = b.astype(np.float32).astype(np.float64)
+    xref = np.linalg.solve(A32, b32)
+    # the residual is checked independently of the library's own FP64-accurate products
+    assert bem.relres <= 1e-10
+    assert np.linalg.norm(b32 - A32 @ x64) / np.linalg.norm(b32) <= 1e-10
+    assert np.abs(x64 - xref).max() <= 1e-9 * np.abs(xref).max()
+
+
+def test_gmres_restarts_and_reports_non_convergence(cuda):
+    n = 600
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(n, n)) / np.sqrt(n) + 1.2 * np.eye(n)       # slower convergence
+    b = rng.normal(size=n)
+    bem, x, x64 = _solve(A, b, method="gmres", max_iter=400, restart=8)   # many restarts
+    A32 = A.astype(np.float32).astype(np.float64)
+    assert np.linalg.norm(b.astype(np.float32) - A32 @ x64) / np.linalg.norm(b.astype(np.float32)) <= 1e-10
+    assert bem.iters > 8
+    with pytest.raises(G.O3GError) as ei:
+        _solve(A, b, method="gmres", max_iter=3)
+    assert ei.value.status == 5
+
+
+@pytest.mark.parametrize("nunk", [2, 3])
+def test_sphere_gmres_agrees_with_lu_and_fp64(cuda, nunk):
+    import torch
+    x, i = G.generate_ovoid(3, 2.0, 2.0, 2.0)
+    s = G.Surfaces(x, i, nunk=nunk)
+    n = s.npanels * nunk
+    arr = s.device_arrays("cuda")
+    bem = G.BEM(n)
+    bem.assemble(arr, arr, nunk, True)
+    rng = np.random.default_rng(nunk)
+    b = torch.from_numpy(rng.normal(size=n).astype(np.float32)).cuda()
+    xg, xg64 = bem.solve(b, tol=1e-11, max_iter=200, x64=True, method="gmres")
+    it_g = bem.iters
+    xl, xl64 = bem.solve(b, tol=1e-11, x64=True, method="lu")
+    Ac = torch.empty((n, n), device="cuda")
+    G.panels_on_panels_coeff(arr, arr, nunk, True, Ac)
+    A = Ac.cpu().numpy().T.astype(np.float64)
+    xref = np.linalg.solve(A, b.cpu().numpy().astype(np.float64))
+    for v in (xg64, xl64):
+        assert np.abs(v.cpu().numpy() - xref).max() <= 1e-9 * np.abs(xref).max()
+    assert it_g <= 60       # a well-conditioned second-kind system
