@@ -350,7 +350,7 @@ __global__ void k_bpack_src(int total, int nsys, const int* __restrict__ soff, c
     p.x = s.p[0][g]; p.y = s.p[1][g]; p.z = s.p[2][g]; p.w = core_param_rt(core, r);
     w.x = s.p[4][g]; w.y = s.p[5][g]; w.z = s.p[6][g]; w.w = r;
   } else {
-    p.x = 0.f; p.y = 0.f; p.z = 0.f; p.w = 1.f;
+    p.x = 1e9f; p.y = 1e9f; p.z = 1e9f; p.w = 1.f;   // zero strength, finite cores: adds exactly 0
     w.x = 0.f; w.y = 0.f; w.z = 0.f; w.w = 0.f;
   }
   spos[j] = p;
@@ -381,7 +381,7 @@ __global__ void k_bpack_tgt(int total, int nsys, const int* __restrict__ toff, c
   tmap[j] = g;
 }
 
-// per source tile: bounds of its real sources (as k_tile_bounds, tiles of many systems)
+// per half tile: bounds of its real sources (as k_tile_bounds, tiles of many systems)
 __global__ void __launch_bounds__(kBlock) k_btile_bounds(int nsys, const int* __restrict__ soff,
                                                          const BatchSysDev* __restrict__ S,
                                                          const V4<float>* __restrict__ spos, float4* tlo,
@@ -409,15 +409,20 @@ __global__ void __launch_bounds__(kBlock) k_btile_bounds(int nsys, const int* __
 #pragma unroll
     for (int d = 0; d < 7; ++d) red[threadIdx.x >> 5][d] = v[d];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // one box per half tile (kHalf sources, reduced from its two warps); a half without real
+  // sources gets an empty box, which every far-field test accepts
+  if (threadIdx.x < kBlock / kHalf) {
+    const int hf = threadIdx.x;
+    constexpr int W = kHalf / 32;
     float m[7];
     for (int d = 0; d < 7; ++d) {
-      m[d] = red[0][d];
-      for (int wq = 1; wq < kBlock / 32; ++wq) m[d] = fminf(m[d], red[wq][d]);
+      m[d] = red[hf * W][d];
+      for (int wq = 1; wq < W; ++wq) m[d] = fminf(m[d], red[hf * W + wq][d]);
     }
     const float pad = 1e-6f * (fabsf(m[0]) + fabsf(m[1]) + fabsf(m[2]) + fabsf(m[3]) + fabsf(m[4]) + fabsf(m[5]));
-    tlo[tile] = make_float4(m[0] - pad, m[1] - pad, m[2] - pad, -m[6] * 1.000001f);
-    thi[tile] = make_float4(-m[3] + pad, -m[4] + pad, -m[5] + pad, 0.f);
+    const int u = tile * (kBlock / kHalf) + hf;
+    tlo[u] = make_float4(m[0] - pad, m[1] - pad, m[2] - pad, -m[6] * 1.000001f);
+    thi[u] = make_float4(-m[3] + pad, -m[4] + pad, -m[5] + pad, 0.f);
   }
 }
 
@@ -695,7 +700,7 @@ int32_t batch_create(int core, int prec, bool grads, int nsys, const BatchSysDev
   add((size_t)std::max(h->cap_tbs, 1LL) * (sizeof(int4) + sizeof(int)));
   add((size_t)std::max(h->cap_slab_floats, 1LL) * sizeof(float));
   add(sizeof(int));
-  add((size_t)std::max(h->ntiles, 1) * sizeof(float4) * 2);
+  add((size_t)std::max(h->ntiles, 1) * sizeof(float4) * 4);
   add((size_t)nsys * 6 * sizeof(float));
   if (sorted) {
     add((size_t)nkeys * sizeof(unsigned long long) * 2);
@@ -733,8 +738,8 @@ int32_t batch_create(int core, int prec, bool grads, int nsys, const BatchSysDev
   }
   h->partial = cv.take<float>((size_t)std::max(h->cap_slab_floats, 1LL));
   h->head = cv.take<int>(1);
-  h->tile_lo = cv.take<float4>((size_t)std::max(h->ntiles, 1) * 2);
-  h->tile_hi = h->tile_lo + std::max(h->ntiles, 1);
+  h->tile_lo = cv.take<float4>((size_t)std::max(h->ntiles, 1) * 4);     // two halves per tile
+  h->tile_hi = h->tile_lo + 2 * (size_t)std::max(h->ntiles, 1);
   h->bbox = cv.take<float>((size_t)nsys * 6);
   if (sorted) {
     h->kin = cv.take<unsigned long long>((size_t)nkeys * 2);

@@ -41,7 +41,7 @@ struct BatchArgs {
   int nitems;
   const int4* tbs;         // per target block: {system, first target slot, first partial slab or -1, nsplit}
   const BatchSysDev* sys;
-  const float4* tile_lo;   // per source tile bounds (classifying cores only)
+  const float4* tile_lo;   // per half-tile bounds (classifying cores only)
   const float4* tile_hi;
   T* partial;              // slabs of [NP][kBlock * TPT]
   int* arrivals;           // per target block: items finished (reset by the last one)
@@ -61,9 +61,10 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
   constexpr int TB = kBlock * TPT;
   __shared__ V4<T> sp[kBlock];
   __shared__ V4<T> sw[kBlock];
-  __shared__ float sbox[kBlock / 32][7];
   __shared__ int s_item, s_last;
   const int tid = threadIdx.x;
+  // lane l of warp w handles slots wbase + 32 k (k < TPT) of the target block
+  const int wbase = (tid >> 5) * (32 * TPT) + (tid & 31);
 
   for (;;) {
     __syncthreads();
@@ -73,58 +74,21 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
     if (it >= a.nitems) break;
     const int4 item = a.items[it];
     const int4 tb = a.tbs[item.x];
-    const int tbase = tb.y + tid;
+    const int tbase = tb.y + wbase;
 
     V4<T> tp[TPT];
     int tm[TPT];
+    bool real[TPT];
 #pragma unroll
     for (int k = 0; k < TPT; ++k) {
-      tp[k] = a.tpos[tbase + k * kBlock];
-      tm[k] = a.tmap[tbase + k * kBlock];
+      tp[k] = a.tpos[tbase + 32 * k];
+      tm[k] = a.tmap[tbase + 32 * k];
+      real[k] = tm[k] >= 0;
     }
 
-    // bounding box and largest core parameter of the block's real targets
     float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
-    if (CLASSIFY) {
-      float lo3[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi3[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mw = 0.f;
-#pragma unroll
-      for (int k = 0; k < TPT; ++k) {
-        if (tm[k] >= 0) {
-          const float v[3] = {(float)tp[k].x, (float)tp[k].y, (float)tp[k].z};
-#pragma unroll
-          for (int d = 0; d < 3; ++d) { lo3[d] = fminf(lo3[d], v[d]); hi3[d] = fmaxf(hi3[d], v[d]); }
-          mw = fmaxf(mw, (float)tp[k].w);
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          lo3[d] = fminf(lo3[d], __shfl_xor_sync(0xffffffffu, lo3[d], o));
-          hi3[d] = fmaxf(hi3[d], __shfl_xor_sync(0xffffffffu, hi3[d], o));
-        }
-        mw = fmaxf(mw, __shfl_xor_sync(0xffffffffu, mw, o));
-      }
-      if ((tid & 31) == 0) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) { sbox[tid >> 5][d] = lo3[d]; sbox[tid >> 5][3 + d] = hi3[d]; }
-        sbox[tid >> 5][6] = mw;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int d = 0; d < 3; ++d) { blo[d] = 3.0e38f; bhi[d] = -3.0e38f; }
-#pragma unroll
-      for (int wq = 0; wq < kBlock / 32; ++wq) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) { blo[d] = fminf(blo[d], sbox[wq][d]); bhi[d] = fmaxf(bhi[d], sbox[wq][3 + d]); }
-        bw = fmaxf(bw, sbox[wq][6]);
-      }
-      const float pad = 1e-6f * (fabsf(blo[0]) + fabsf(blo[1]) + fabsf(blo[2]) + fabsf(bhi[0]) + fabsf(bhi[1]) +
-                                 fabsf(bhi[2]));
-#pragma unroll
-      for (int d = 0; d < 3; ++d) { blo[d] -= pad; bhi[d] += pad; }
-      bw *= 1.000001f;
-    }
+    bool live = true;
+    if (CLASSIFY) live = warp_box<TPT, T>(tp, real, blo, bhi, bw);
 
     T acc[TPT][NA];
 #pragma unroll
@@ -142,16 +106,21 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
       sp[tid] = a.spos[(size_t)tile * kBlock + tid];
       sw[tid] = a.sstr[(size_t)tile * kBlock + tid];
       __syncthreads();
-      bool far = false;
-      if (CLASSIFY) {
-        const float4 slo = a.tile_lo[tile], shi = a.tile_hi[tile];
-        const float gx = fmaxf(0.f, fmaxf(slo.x - bhi[0], blo[0] - shi.x));
-        const float gy = fmaxf(0.f, fmaxf(slo.y - bhi[1], blo[1] - shi.y));
-        const float gz = fmaxf(0.f, fmaxf(slo.z - bhi[2], blo[2] - shi.z));
-        far = FarRule<C>::far(gx * gx + gy * gy + gz * gz, slo.w + bw);
+      if constexpr (CLASSIFY) {
+        if (!live) continue;
+#pragma unroll 1
+        for (int hf = 0; hf < kBlock / kHalf; ++hf) {
+          const int u = tile * (kBlock / kHalf) + hf;
+          if (half_is_far<C, true>(a.tile_lo[u], a.tile_hi[u], blo, bhi, bw))
+            sweep_tile<CORE_SING, MODE, GRADS, true, TPT, T, NA, NC, NH, kHalf>(sp + hf * kHalf, sw + hf * kHalf, tp,
+                                                                             acc, hi, lo);
+          else
+            sweep_tile<C, MODE, GRADS, true, TPT, T, NA, NC, NH, kHalf>(sp + hf * kHalf, sw + hf * kHalf, tp, acc,
+                                                                     hi, lo);
+        }
+      } else {
+        sweep_tile<C, MODE, GRADS, true, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
       }
-      if (far) sweep_tile<CORE_SING, MODE, GRADS, true, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
-      else     sweep_tile<C, MODE, GRADS, true, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
     }
     if (!ACC && GRADS) {
 #pragma unroll
@@ -165,7 +134,7 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
       for (int k = 0; k < TPT; ++k) {
         const int g = tm[k];
         if (g < 0) continue;
-        const int slot = tbase + k * kBlock;
+        const int slot = tbase + 32 * k;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           if (a.sink) {
@@ -185,7 +154,7 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
       T* base = a.partial + (size_t)(tb.z + item.w) * NP * TB;
 #pragma unroll
       for (int k = 0; k < TPT; ++k) {
-        const int i = tid + k * kBlock;
+        const int i = wbase + 32 * k;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           if (ACC) {
@@ -208,8 +177,8 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
     for (int k = 0; k < TPT; ++k) {
       const int g = tm[k];
       if (g < 0) continue;
-      const int i = tid + k * kBlock;
-      const int slot = tbase + k * kBlock;
+      const int i = wbase + 32 * k;
+      const int slot = tbase + 32 * k;
 #pragma unroll 1
       for (int c = 0; c < NC; ++c) {
         double sd = 0.0;

@@ -7,6 +7,9 @@
 #include <string>
 
 #include "../../include/o3dgpu.h"
+#include "o3g_gauss_poly.h"
+
+#include <type_traits>
 
 namespace o3g {
 
@@ -138,7 +141,39 @@ __device__ __forceinline__ double dev_expm1(double x) { return expm1(x); }
 __device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 
-// Gaussian core with gradient factor (the project's own definition, see o3dgpu.h)
+// G(q) and D(q) = 2 G'(q) of the Gaussian core for q in [0, qfar] in FP32, from the
+// piecewise polynomials of o3g_gauss_poly.h (interval j = number of edges 1, 4, ..., 36 at
+// or below q; Horner's rule in t = q s_j + o_j): branch-free, no erf/exp/division
+__device__ __forceinline__ void gauss_poly(float q, float& G, float& D) {
+  const int j = (q >= 1.f) + (q >= 4.f) + (q >= 9.f) + (q >= 16.f) + (q >= 25.f) + (q >= 36.f);
+  const float* c = kGaussPoly + j * kGaussPolyStride;
+  const float t = fmaf(q, __ldg(c), __ldg(c + 1));
+  const float* cg = c + 2;
+  const float* cd = cg + (kGaussPolyDeg + 1);
+  float g = __ldg(cg + kGaussPolyDeg), d = __ldg(cd + kGaussPolyDeg);
+#pragma unroll
+  for (int k = kGaussPolyDeg - 1; k >= 0; --k) {
+    g = fmaf(g, t, __ldg(cg + k));
+    d = fmaf(d, t, __ldg(cd + k));
+  }
+  G = g;
+  D = d;
+}
+__device__ __forceinline__ float gauss_poly_g(float q) {
+  const int j = (q >= 1.f) + (q >= 4.f) + (q >= 9.f) + (q >= 16.f) + (q >= 25.f) + (q >= 36.f);
+  const float* c = kGaussPoly + j * kGaussPolyStride;
+  const float t = fmaf(q, __ldg(c), __ldg(c + 1));
+  const float* cg = c + 2;
+  float g = __ldg(cg + kGaussPolyDeg);
+#pragma unroll
+  for (int k = kGaussPolyDeg - 1; k >= 0; --k) g = fmaf(g, t, __ldg(cg + k));
+  return g;
+}
+
+// Gaussian core with gradient factor (the project's own definition, see o3dgpu.h):
+// r3 = G(q) / sigma^3, bbb = 2 G'(q) / sigma^5 with q = d^2 / sigma^2; the singular kernel
+// beyond q = qfar.  FP32 evaluates G from the polynomials above; FP64 (the comparator) from
+// the Taylor series for q < 1 and the closed form with erf/exp beyond.
 template <bool ACC, class T>
 __device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb) {
   const T c = T(0.79788456080286535588);  // sqrt(2/pi)
@@ -147,6 +182,16 @@ __device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb) {
     const T rs2 = rs * rs;
     r3 = rs2 * rs;
     bbb = T(-3.0) * r3 * rs2;
+    return;
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    const float rsg = rsq<ACC>(sig2);
+    const float rsg2 = rsg * rsg;
+    float G, D;
+    gauss_poly(distsq * rsg2, G, D);
+    const float isig3 = rsg2 * rsg;
+    r3 = G * isig3;
+    bbb = D * isig3 * rsg2;
     return;
   }
   const T q = distsq / sig2;
@@ -177,6 +222,11 @@ __device__ __forceinline__ T gauss_v(T distsq, T sig2) {
   if (distsq > GaussP<T>::qfar * sig2) {
     const T rs = rsq<ACC>(distsq);
     return rs * rs * rs;
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    const float rsg = rsq<ACC>(sig2);
+    const float rsg2 = rsg * rsg;
+    return gauss_poly_g(distsq * rsg2) * (rsg2 * rsg);
   }
   const T q = distsq / sig2;
   if (q < T(1.0)) {

@@ -73,7 +73,7 @@ static int32_t noalloc_run(int ns, const float* sx, const float* sy, const float
   const int nsp = same ? (pl.ns_pad > pl.nt_pad ? pl.ns_pad : pl.nt_pad) : pl.ns_pad;
   size_t fixed = 2 * align_up((size_t)nsp * sizeof(V4<float>));
   if (!same) fixed += align_up((size_t)pl.nt_pad * sizeof(V4<float>));
-  if (CLASSIFY) fixed += 2 * align_up((size_t)pl.ntiles * sizeof(float4));
+  if (CLASSIFY) fixed += 2 * align_up((size_t)pl.ntiles * 2 * sizeof(float4));
   if (fixed > kNoAllocBytes) {
     char msg[200];
     std::snprintf(msg, sizeof(msg),
@@ -97,8 +97,8 @@ static int32_t noalloc_run(int ns, const float* sx, const float* sy, const float
   V4<float>* spos = cv.take<V4<float>>(nsp);
   V4<float>* sstr = cv.take<V4<float>>(nsp);
   V4<float>* tpos = same ? spos : cv.take<V4<float>>(pl.nt_pad);
-  float4* tile_lo = CLASSIFY ? cv.take<float4>(pl.ntiles) : nullptr;
-  float4* tile_hi = CLASSIFY ? cv.take<float4>(pl.ntiles) : nullptr;
+  float4* tile_lo = CLASSIFY ? cv.take<float4>((size_t)pl.ntiles * 2) : nullptr;
+  float4* tile_hi = CLASSIFY ? cv.take<float4>((size_t)pl.ntiles * 2) : nullptr;
   float* partial = pl.nsplit > 1 ? cv.take<float>((size_t)pl.nsplit * NC * (ACC ? 2 : 1) * pl.nt_pad) : nullptr;
 
   k_pack_src<C, float, float><<<(nsp + 255) / 256, 256, 0, st>>>(ns, nsp, sx, sy, sz, sr, ssx, ssy, ssz, nullptr,

@@ -4,22 +4,25 @@
 //   spos[ns_pad] : float4 (x, y, z, core parameter of sr)      16 B / source
 //   sstr[ns_pad] : float4 (sx, sy, sz, sr)                     16 B / source
 //   tpos[nt_pad] : float4 (x, y, z, core parameter of tr or 0) 16 B / target
-//   (double4 for the FP64 mode).  Padding sources sit at the origin with zero strength
-//   and core parameter 1, so they add exactly zero (as the reference's Vc padding,
-//   Influence.h:232-238).
+//   (double4 for the FP64 mode).  Padding sources have zero strength and core parameter 1
+//   (as the reference's Vc padding, Influence.h:232-238) and sit at (1e9, 1e9, 1e9): every
+//   core and the singular far-field loop give finite r3 and bbb there (d^4 = 9e36 stays
+//   below the float range), so with zero strength they add exactly zero, also to a target
+//   at the origin.
 //
-// Kernel k_pair: a block of kBlock threads owns kBlock*TPT targets (TPT per thread,
-// strided by kBlock so loads and stores coalesce) and sweeps a contiguous range of
-// source tiles.  Each tile of kBlock sources is staged in shared memory and read by
+// Kernel k_pair: a block of kBlock threads owns kBlock*TPT targets; each warp owns a
+// contiguous run of 32*TPT of them (lane l holds targets l, l+32, ... so loads and stores
+// coalesce) and sweeps a contiguous range of source tiles.  Each tile of kBlock sources is staged in shared memory and read by
 // every thread as a broadcast.  When the targets alone cannot fill the GPU, the source
 // range is split across blockIdx.y and the per-split partial sums go to scratch,
 // reduced afterwards in a fixed order (deterministic, k_reduce).
 //
 // Cores with distance branches (Gaussian, compact exponential) sweep Morton-ordered
-// sources and targets.  For every (target block, source tile) the bounding boxes decide
-// whether all of the tile's pairs lie beyond the core's far-field threshold; such tiles
-// run the branch-free singular loop (r3 = 1/d^3, bbb = -3/d^5), the others the full core.
-// The decision is uniform over the block, so warps never diverge on it.
+// sources and targets.  For every (warp's targets, half tile of kHalf sources) the
+// bounding boxes decide whether all of the pairs lie beyond the core's far-field
+// threshold; such halves run the branch-free singular loop (r3 = 1/d^3, bbb = -3/d^5),
+// the others the full core.  The decision is uniform over the warp, so its lanes never
+// diverge on it.
 #pragma once
 
 #include "o3g_common.cuh"
@@ -28,6 +31,7 @@
 namespace o3g {
 
 constexpr int kBlock = 128;  // threads per block == sources per shared tile
+constexpr int kHalf = 64;    // sources per far-field classification unit (two per tile)
 
 enum { MODE_PLAIN = 0, MODE_COMP = 1, MODE_FP64 = 2 };
 enum { CORE_SING = 5 };      // internal: singular far-field kernel (cst ignored)
@@ -43,8 +47,8 @@ template <class T, class O> struct PairArgs {
   T* partial;                // [nsplit][ncomp * (COMP ? 2 : 1)][nt_pad] or nullptr
   OutPtrs<O> out;            // accumulated into when partial == nullptr
   const uint32_t* tperm;     // sorted target k -> caller's index, or nullptr
-  const float4* tile_lo;     // per source tile: (min x, min y, min z, max core param)
-  const float4* tile_hi;     // per source tile: (max x, max y, max z, -)
+  const float4* tile_lo;     // per half tile: (min x, min y, min z, max core param)
+  const float4* tile_hi;     // per half tile: (max x, max y, max z, -)
 };
 
 // one pair, velocity + gradient.  a[0..2] velocity, a[3..11] gradient sums of
@@ -129,13 +133,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 
 // Sweep the staged tile (kBlock sources in shared memory) for TPT targets.  In the
 // compensated mode the plain partial of every FOLD sources is folded into (hi, lo).
-template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, int NA, int NC, int NH>
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, int NA, int NC, int NH, int NS = kBlock>
 __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, const V4<T>* tp, T (*acc)[NA],
                                            float (*hi)[NH], float (*lo)[NH]) {
   constexpr bool ACC = (MODE == MODE_COMP);
-  constexpr int FOLD = ACC ? 16 : kBlock;
+  constexpr int FOLD = ACC ? 16 : NS;
 #pragma unroll 1
-  for (int j0 = 0; j0 < kBlock; j0 += FOLD) {
+  for (int j0 = 0; j0 < NS; j0 += FOLD) {
 #pragma unroll 4
     for (int j = j0; j < j0 + FOLD; ++j) {
       const V4<T> s = sp[j];
@@ -178,6 +182,50 @@ template <> struct FarRule<CORE_EXP> {
   __device__ static bool far(float d2min, float maxcst) { return d2min * sqrtf(d2min) > 20.0f * maxcst; }
 };
 
+// bounding box and largest core parameter of the real targets of one warp (all lanes get
+// the result), widened by a relative 1e-6 so float rounding never makes it too small;
+// returns false when the warp holds no real target
+template <int TPT, class T>
+__device__ __forceinline__ bool warp_box(const V4<T>* tp, const bool* real, float* blo, float* bhi, float& bw) {
+  float lo3[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi3[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mw = 0.f;
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    if (real[k]) {
+      const float v[3] = {(float)tp[k].x, (float)tp[k].y, (float)tp[k].z};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) { lo3[d] = fminf(lo3[d], v[d]); hi3[d] = fmaxf(hi3[d], v[d]); }
+      mw = fmaxf(mw, (float)tp[k].w);
+      any = true;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo3[d] = fminf(lo3[d], __shfl_xor_sync(0xffffffffu, lo3[d], o));
+      hi3[d] = fmaxf(hi3[d], __shfl_xor_sync(0xffffffffu, hi3[d], o));
+    }
+    mw = fmaxf(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+  }
+  const float pad = 1e-6f * (fabsf(lo3[0]) + fabsf(lo3[1]) + fabsf(lo3[2]) + fabsf(hi3[0]) + fabsf(hi3[1]) +
+                             fabsf(hi3[2]));
+#pragma unroll
+  for (int d = 0; d < 3; ++d) { blo[d] = lo3[d] - pad; bhi[d] = hi3[d] + pad; }
+  bw = mw * 1.000001f;
+  return __any_sync(0xffffffffu, any);
+}
+
+// far-field test of a warp's box against one half tile's box
+template <int C, bool HAVE_TR>
+__device__ __forceinline__ bool half_is_far(const float4& slo, const float4& shi, const float* blo, const float* bhi,
+                                            float bw) {
+  const float gx = fmaxf(0.f, fmaxf(slo.x - bhi[0], blo[0] - shi.x));
+  const float gy = fmaxf(0.f, fmaxf(slo.y - bhi[1], blo[1] - shi.y));
+  const float gz = fmaxf(0.f, fmaxf(slo.z - bhi[2], blo[2] - shi.z));
+  return FarRule<C>::far(gx * gx + gy * gy + gz * gz, HAVE_TR ? slo.w + bw : slo.w);
+}
+
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
 __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
   constexpr bool ACC = (MODE == MODE_COMP);
@@ -187,59 +235,23 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
   constexpr int NH = ACC ? NC : 1;
   __shared__ V4<T> sp[kBlock];
   __shared__ V4<T> sw[kBlock];
-  __shared__ float sbox[kBlock / 32][7];
 
   const int tid = threadIdx.x;
   const int split = blockIdx.y;
-  const int tbase = blockIdx.x * (kBlock * TPT) + tid;
+  // lane l of warp w holds targets tbase + 32 k (k < TPT): a contiguous run per warp
+  const int tbase = blockIdx.x * (kBlock * TPT) + (tid >> 5) * (32 * TPT) + (tid & 31);
 
   V4<T> tp[TPT];
+  bool real[TPT];
 #pragma unroll
-  for (int k = 0; k < TPT; ++k) tp[k] = a.tpos[tbase + k * kBlock];
-
-  // bounding box and largest core parameter of this block's real targets
-  float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
-  if (CLASSIFY) {
-    float lo3[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi3[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mw = 0.f;
-#pragma unroll
-    for (int k = 0; k < TPT; ++k) {
-      if (tbase + k * kBlock < a.nt) {
-        const float v[3] = {(float)tp[k].x, (float)tp[k].y, (float)tp[k].z};
-#pragma unroll
-        for (int d = 0; d < 3; ++d) { lo3[d] = fminf(lo3[d], v[d]); hi3[d] = fmaxf(hi3[d], v[d]); }
-        mw = fmaxf(mw, (float)tp[k].w);
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        lo3[d] = fminf(lo3[d], __shfl_xor_sync(0xffffffffu, lo3[d], o));
-        hi3[d] = fmaxf(hi3[d], __shfl_xor_sync(0xffffffffu, hi3[d], o));
-      }
-      mw = fmaxf(mw, __shfl_xor_sync(0xffffffffu, mw, o));
-    }
-    if ((tid & 31) == 0) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) { sbox[tid >> 5][d] = lo3[d]; sbox[tid >> 5][3 + d] = hi3[d]; }
-      sbox[tid >> 5][6] = mw;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int d = 0; d < 3; ++d) { blo[d] = 3.0e38f; bhi[d] = -3.0e38f; }
-#pragma unroll
-    for (int wq = 0; wq < kBlock / 32; ++wq) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) { blo[d] = fminf(blo[d], sbox[wq][d]); bhi[d] = fmaxf(bhi[d], sbox[wq][3 + d]); }
-      bw = fmaxf(bw, sbox[wq][6]);
-    }
-    // widen by a relative 1e-6 so rounding of the (float) box never makes it too small
-    const float pad = 1e-6f * (fabsf(blo[0]) + fabsf(blo[1]) + fabsf(blo[2]) + fabsf(bhi[0]) + fabsf(bhi[1]) +
-                               fabsf(bhi[2]));
-#pragma unroll
-    for (int d = 0; d < 3; ++d) { blo[d] -= pad; bhi[d] += pad; }
-    bw *= 1.000001f;
+  for (int k = 0; k < TPT; ++k) {
+    tp[k] = a.tpos[tbase + 32 * k];
+    real[k] = tbase + 32 * k < a.nt;
   }
+
+  float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
+  bool live = true;
+  if (CLASSIFY) live = warp_box<TPT, T>(tp, real, blo, bhi, bw);
 
   T acc[TPT][NA];
 #pragma unroll
@@ -259,23 +271,27 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
     sp[tid] = a.spos[(size_t)tile * kBlock + tid];
     sw[tid] = a.sstr[(size_t)tile * kBlock + tid];
     __syncthreads();
-    bool far = false;
-    if (CLASSIFY) {
-      const float4 slo = a.tile_lo[tile], shi = a.tile_hi[tile];
-      const float gx = fmaxf(0.f, fmaxf(slo.x - bhi[0], blo[0] - shi.x));
-      const float gy = fmaxf(0.f, fmaxf(slo.y - bhi[1], blo[1] - shi.y));
-      const float gz = fmaxf(0.f, fmaxf(slo.z - bhi[2], blo[2] - shi.z));
-      const float d2min = gx * gx + gy * gy + gz * gz;
-      far = FarRule<C>::far(d2min, HAVE_TR ? slo.w + bw : slo.w);
+    if constexpr (CLASSIFY) {
+      if (!live) continue;
+#pragma unroll 1
+      for (int hf = 0; hf < kBlock / kHalf; ++hf) {
+        const int u = tile * (kBlock / kHalf) + hf;
+        if (half_is_far<C, HAVE_TR>(a.tile_lo[u], a.tile_hi[u], blo, bhi, bw))
+          sweep_tile<CORE_SING, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH, kHalf>(sp + hf * kHalf, sw + hf * kHalf, tp,
+                                                                               acc, hi, lo);
+        else
+          sweep_tile<C, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH, kHalf>(sp + hf * kHalf, sw + hf * kHalf, tp, acc,
+                                                                       hi, lo);
+      }
+    } else {
+      sweep_tile<C, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
     }
-    if (far) sweep_tile<CORE_SING, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
-    else     sweep_tile<C, MODE, GRADS, HAVE_TR, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
   }
 
   // epilogue
 #pragma unroll
   for (int k = 0; k < TPT; ++k) {
-    const int idx = tbase + k * kBlock;
+    const int idx = tbase + 32 * k;
     if (!ACC && GRADS) fold_grads(acc[k]);
     if (a.partial) {
       if (ACC) {
@@ -340,7 +356,7 @@ __global__ void k_pack_src(int n, int n_pad, const I* __restrict__ x, const I* _
     p.x = (T)x[j]; p.y = (T)y[j]; p.z = (T)z[j]; p.w = core_param<C, T>(ri);
     w.x = (T)sx[j]; w.y = (T)sy[j]; w.z = (T)sz[j]; w.w = ri;
   } else {
-    p.x = T(0); p.y = T(0); p.z = T(0); p.w = T(1);
+    p.x = T(1e9); p.y = T(1e9); p.z = T(1e9); p.w = T(1);
     w.x = T(0); w.y = T(0); w.z = T(0); w.w = T(0);
   }
   spos[i] = p;
@@ -365,8 +381,10 @@ __global__ void k_pack_tgt(int n, int n_pad, const I* __restrict__ x, const I* _
   tpos[i] = p;
 }
 
-// per source tile: bounding box of its real sources and their largest core parameter,
-// widened by a relative 1e-6 so float rounding never shrinks it
+// per half tile (kHalf sources): bounding box of its real sources and their largest core
+// parameter, widened by a relative 1e-6 so float rounding never shrinks it.  One block of
+// kBlock threads per tile; half h is reduced by warps 2h and 2h+1.  A half without real
+// sources gets an empty box (lo > hi), which every far-field test accepts.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_tile_bounds(const V4<T>* __restrict__ spos, int ns, float4* tlo,
                                                         float4* thi) {
@@ -391,15 +409,18 @@ __global__ void __launch_bounds__(kBlock) k_tile_bounds(const V4<T>* __restrict_
 #pragma unroll
     for (int d = 0; d < 7; ++d) red[threadIdx.x >> 5][d] = v[d];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < kBlock / kHalf) {
+    const int hf = threadIdx.x;
+    constexpr int W = kHalf / 32;
     float m[7];
     for (int d = 0; d < 7; ++d) {
-      m[d] = red[0][d];
-      for (int wq = 1; wq < kBlock / 32; ++wq) m[d] = fminf(m[d], red[wq][d]);
+      m[d] = red[hf * W][d];
+      for (int wq = 1; wq < W; ++wq) m[d] = fminf(m[d], red[hf * W + wq][d]);
     }
     const float pad = 1e-6f * (fabsf(m[0]) + fabsf(m[1]) + fabsf(m[2]) + fabsf(m[3]) + fabsf(m[4]) + fabsf(m[5]));
-    tlo[tile] = make_float4(m[0] - pad, m[1] - pad, m[2] - pad, -m[6] * 1.000001f);
-    thi[tile] = make_float4(-m[3] + pad, -m[4] + pad, -m[5] + pad, 0.f);
+    const int u = tile * (kBlock / kHalf) + hf;
+    tlo[u] = make_float4(m[0] - pad, m[1] - pad, m[2] - pad, -m[6] * 1.000001f);
+    thi[u] = make_float4(-m[3] + pad, -m[4] + pad, -m[5] + pad, 0.f);
   }
 }
 
@@ -456,7 +477,7 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   if (pl.nsplit > 1) bytes += align_up((size_t)pl.nsplit * NC * (ACC ? 2 : 1) * pl.nt_pad * sizeof(T));
   size_t sort_bytes = 0;
   if (SORT) {
-    bytes += align_up((size_t)ns * sizeof(uint32_t)) + 2 * align_up((size_t)pl.ntiles * sizeof(float4));
+    bytes += align_up((size_t)ns * sizeof(uint32_t)) + 2 * align_up((size_t)pl.ntiles * 2 * sizeof(float4));
     if (!same) bytes += align_up((size_t)nt * sizeof(uint32_t));
     sort_bytes = morton_sort_bytes(ns > nt ? ns : nt);
     bytes += sort_bytes;
@@ -475,8 +496,8 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   if (SORT) {
     sperm = cv.take<uint32_t>(ns);
     tperm = same ? sperm : cv.take<uint32_t>(nt);
-    tile_lo = cv.take<float4>(pl.ntiles);
-    tile_hi = cv.take<float4>(pl.ntiles);
+    tile_lo = cv.take<float4>((size_t)pl.ntiles * 2);
+    tile_hi = cv.take<float4>((size_t)pl.ntiles * 2);
     char* sort_ws = cv.take<char>(sort_bytes);
     O3G_TRY(morton_sort<I>(sx, sy, sz, ns, sperm, sort_ws, st));
     if (!same) O3G_TRY(morton_sort<I>(tx, ty, tz, nt, tperm, sort_ws, st));
