@@ -444,9 +444,12 @@ def bench_coupled(args, G, torch, W):
     bem = G.BEM(surf.npanels * 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    rk.attach_body(surf, bem)
+    # clear_inner_layer after each move with ips = the nominal particle spacing of the wake box
+    ips = float((5.0 * 3.0 * 3.0 / n) ** (1.0 / 3.0))
+    rk.attach_body(surf, bem, ips=ips)
     torch.cuda.synchronize()
     out["assemble_factor_ms"] = (time.perf_counter() - t0) * 1e3
+    out["ips"] = ips
 
     # the parts of one stage on the initial state
     arr = rk.body_arrays
