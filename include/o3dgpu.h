@@ -332,6 +332,16 @@ int32_t o3g_batch_rk2_create(int32_t core, int32_t prec, int32_t nsys, const int
                              float* const* x, float* const* s, float* r, float* elong, float* const* fx,
                              int32_t use_graph, o3g_rk2_t** h);
 
+/* ---- shedding ------------------------------------------------------------------------------
+ * Replaces Surfaces::represent_as_particles (Surfaces.h:959-1008), which diffusion calls after
+ * its solve_bem (Diffusion.h:187-224): particle i at the centroid of panel i pushed `offset`
+ * along the normal, with strength ts_i, plus (bc1 x1 + bc2 x2) area when bc1 and bc2 (the
+ * reactive boundary-condition values) are given.  Device arrays; np particles out; the
+ * positions and strengths are bit-identical to the reference's float arithmetic. */
+int32_t o3g_represent_as_particles(const o3g_surface_t* surf, float offset, const float* tsx, const float* tsy,
+                                   const float* tsz, const float* bc1, const float* bc2, float* px, float* py,
+                                   float* pz, float* sx, float* sy, float* sz, void* stream);
+
 /* ---- clear_inner_layer ------------------------------------------------------------------
  * Replaces clear_inner_panp2 method 1 (Reflect.h:446-656): every one of the n points (device
  * arrays x, y, z, moved in place) whose height above its closest panels -- the mean normal

@@ -130,6 +130,8 @@ def _declare(l):
     l.o3g_rk2_attach_body.argtypes = [P, P, c_i32, c_i32, P, c_d, c_i32, c_f, P]
     l.o3g_rk2_body_stats.restype = c_i32
     l.o3g_rk2_body_stats.argtypes = [P, P, P, P, P, P]
+    l.o3g_represent_as_particles.restype = c_i32
+    l.o3g_represent_as_particles.argtypes = [P, c_f] + [P] * 11 + [P]
     l.o3g_clear_inner_layer.restype = c_i32
     l.o3g_clear_inner_layer.argtypes = [c_i32, P, P, P, P, c_f, c_f, P, P]
     l.o3g_rk2_body_strengths.restype = c_i32

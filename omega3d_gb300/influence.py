@@ -312,6 +312,26 @@ def clear_inner_layer(bdry, targ, cutoff_mult=0.5 / np.sqrt(2.0 * np.pi), ips=0.
     return n.value
 
 
+def represent_as_particles(bdry, offset, ts=None, bc=None, arrays=None, stream=None):
+    """Surfaces::represent_as_particles (Surfaces.h:959-1008): torch CUDA (positions[3, np],
+    strengths[3, np]) of one particle per panel, `offset` above the centroid along the
+    normal, with the absolute panel strengths ts (default: the surface's) plus the reactive
+    boundary-condition sheet (bc = (bc1, bc2)) when given."""
+    a = arrays or bdry.device_arrays("cuda")
+    s = surface_struct(a)
+    t = a["ts"] if ts is None else ts
+    npan = bdry.npanels
+    px = torch.empty((3, npan), dtype=torch.float32, device=t.device)
+    ps = torch.empty((3, npan), dtype=torch.float32, device=t.device)
+    b1 = b2 = None
+    if bc is not None:
+        b1, b2 = (_base(v) for v in bc)
+    h = stream if stream is not None else ExecEnv().stream_handle(True)
+    L.check(L.lib().o3g_represent_as_particles(ctypes.byref(s), offset, *_rows(t, 3), b1, b2, *_rows(px, 3),
+                                               *_rows(ps, 3), h), "o3g_represent_as_particles")
+    return px, ps
+
+
 def panels_on_panels_coeff(src_arrays, targ_arrays, nunk, is_self, out, ld=None, maxlev=3, stream=None):
     """Coefficients.h:169: write the column-major (ntarg*nunk) x (nsrc*nunk) block into the
     device tensor `out` (viewed with leading dimension ld, default ntarg*nunk)."""

@@ -1118,3 +1118,28 @@ extern "C" int o3o_clear_inner_layer(int prec, int n, void* x, int nn, const voi
   return clear_inner<float>(n, (float*)x, nn, (const float*)nodes, np, idx, (const float*)norm, (float)cutoff_mult,
                             (float)ips, nthreads);
 }
+
+// Surfaces::represent_as_particles, Surfaces.h:959-1008 (float S): centroid in float sums
+// times (1./3.) in double, pushed by offset along the normal; strength ts (+ the reactive
+// boundary-condition sheet when bc1/bc2 are given)
+extern "C" int o3o_represent_as_particles(int nn, const float* nodes, int np, const uint32_t* idx, const float* area,
+                                          const float* x1, const float* x2, const float* norm, float offset,
+                                          const float* ts, const float* bc1, const float* bc2, float* px,
+                                          float* ps) {
+  if (np < 0 || nn < 0) return 1;
+  for (int i = 0; i < np; ++i) {
+    const uint32_t id0 = idx[3 * (size_t)i], id1 = idx[3 * (size_t)i + 1], id2 = idx[3 * (size_t)i + 2];
+    for (int j = 0; j < 3; ++j) {
+      const float* xj = nodes + (size_t)j * nn;
+      float p = (float)((1. / 3.) * (xj[id0] + xj[id1] + xj[id2]));
+      p += offset * norm[(size_t)j * np + i];
+      px[(size_t)j * np + i] = p;
+    }
+    for (int j = 0; j < 3; ++j) {
+      float v = ts[(size_t)j * np + i];
+      if (bc1 && bc2) v += (bc1[i] * x1[(size_t)j * np + i] + bc2[i] * x2[(size_t)j * np + i]) * area[i];
+      ps[(size_t)j * np + i] = v;
+    }
+  }
+  return 0;
+}

@@ -338,3 +338,22 @@ def clear_inner_layer(x, nodes, idx, norm, cutoff_mult=0.5 / np.sqrt(2.0 * np.pi
 
 def ref_reflect_available():
     return os.path.exists(os.path.join(REF_DIR, "libo3dref_reflect.so"))
+
+
+def represent_as_particles(nodes, idx, area, x1, x2, norm, offset, ts, bc1=None, bc2=None):
+    """Surfaces::represent_as_particles (Surfaces.h:959-1008): (positions[3, np],
+    strengths[3, np]) of one particle per panel."""
+    nx = _as(nodes, np.float32)
+    idx = np.ascontiguousarray(idx, np.uint32)
+    np_ = area.shape[0]
+    px = np.zeros((3, np_), np.float32)
+    ps = np.zeros((3, np_), np.float32)
+    arrs = [_as(a, np.float32) for a in (area, x1, x2, norm, ts)]
+    b1 = _as(bc1, np.float32)
+    b2 = _as(bc2, np.float32)
+    rc = lib().o3o_represent_as_particles(ctypes.c_int(nx.shape[1]), _p(nx), ctypes.c_int(np_), _p(idx),
+                                          _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(arrs[3]),
+                                          ctypes.c_float(offset), _p(arrs[4]), _p(b1), _p(b2), _p(px), _p(ps))
+    if rc != 0:
+        raise RuntimeError("oracle represent_as_particles failed")
+    return px, ps

@@ -201,3 +201,15 @@ def test_attach_body_rejects_bad_arguments(cuda):
     assert lib.o3g_rk2_body_stats(rk.h, None, None, None, None, None) == 9
     L.check(lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, 0.0, None), "attach")
     assert lib.o3g_rk2_attach_body(rk.h, ctypes.byref(st), 2, 3, right.h, 1e-10, 30, 0.0, None) == 9
+
+
+@pytest.mark.parametrize("with_bc", [False, True])
+def test_represent_as_particles_bit_exact(cuda, with_bc):
+    s = _sphere(3, 2)
+    arr = s.device_arrays("cuda")
+    rng = np.random.default_rng(17)
+    bc1 = rng.normal(size=s.npanels).astype(np.float32) if with_bc else None
+    bc2 = rng.normal(size=s.npanels).astype(np.float32) if with_bc else None
+    px, ps = G.represent_as_particles(s, 0.0125, bc=(_t(bc1), _t(bc2)) if with_bc else None, arrays=arr)
+    po, so = O.represent_as_particles(s.x, s.idx, s.area, s.x1, s.x2, s.norm, 0.0125, s.ts, bc1, bc2)
+    assert np.array_equal(px.cpu().numpy(), po) and np.array_equal(ps.cpu().numpy(), so)

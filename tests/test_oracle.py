@@ -259,3 +259,18 @@ def test_clear_inner_layer_leaves_points_at_the_cutoff():
     y = x.copy()
     O.clear_inner_layer(y, nodes, idx, nm, ips=ips)
     assert np.abs(y - x).max() <= 0.01 * cut
+
+
+def test_represent_as_particles_geometry():
+    nodes, idx = O.generate_ovoid(2, 2.0, 2.0, 2.0)
+    x1, x2, nm, area = O.compute_bases(nodes, idx)
+    ts = np.random.default_rng(3).normal(size=(3, area.shape[0])).astype(np.float32)
+    px, ps = O.represent_as_particles(nodes, idx, area, x1, x2, nm, 0.02, ts)
+    f = idx.reshape(-1, 3)
+    cen = (nodes[:, f[:, 0]].astype(np.float64) + nodes[:, f[:, 1]] + nodes[:, f[:, 2]]) / 3
+    # 0.02 above each panel's centroid along its normal, carrying the panel strength
+    assert np.abs(((px - cen) * nm).sum(0) - 0.02).max() < 1e-6
+    assert np.array_equal(ps, ts)
+    bc1 = np.ones(area.shape[0], np.float32)
+    _, ps2 = O.represent_as_particles(nodes, idx, area, x1, x2, nm, 0.02, ts, bc1, 0 * bc1)
+    assert np.allclose(ps2 - ts, x1 * area, atol=1e-7)
