@@ -509,6 +509,14 @@ def bench_coupled(args, G, torch, W):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     st = rk.body_stats()
+    # one clear_inner_layer pass over all particles on its own (two run in every step)
+    e0, e1 = ev(), ev()
+    e0.record()
+    pushed = G.clear_inner_layer(surf, G.Points(X, None, None, inert=True), ips=ips, arrays=arr)
+    e1.record()
+    torch.cuda.synchronize()
+    out["clear_inner_layer_ms"] = e0.elapsed_time(e1)
+    out["clear_inner_layer_point_panel_tests_per_s"] = float(n) * surf.npanels / (e0.elapsed_time(e1) * 1e-3)
     out["steps"] = steps
     out["step_ms"] = ms / steps
     out["interactions_per_step"] = 2 * (pairs + float(surf.npanels) * n * 2)

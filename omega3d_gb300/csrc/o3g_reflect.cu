@@ -19,11 +19,26 @@ namespace o3g {
 
 constexpr int kRB = 128;
 
+// per panel: corners, normal, and the panel-only terms of Reflect.h:56-183 -- the edge
+// vectors and their inverse squared lengths 1.0 / |e|^2 (formed in double and rounded to
+// float, as the reference does per call) -- computed once here with the same operations
 struct PanelTri {
   float4 a;   // x0 y0 z0 x1
   float4 b;   // y1 z1 x2 y2
   float4 c;   // z2 nx ny nz
+  float4 e;   // e01 (x1 - x0), inv01
+  float4 f;   // e12 (x2 - x1), inv12
+  float4 g;   // e20 (x0 - x2), inv20
 };
+
+__device__ __forceinline__ float dot_rn(float a0, float a1, float a2, float b0, float b1, float b2) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
+
+__device__ __forceinline__ float4 edge_rec(float ax, float ay, float az, float bx, float by, float bz) {
+  const float ex = __fsub_rn(bx, ax), ey = __fsub_rn(by, ay), ez = __fsub_rn(bz, az);
+  return make_float4(ex, ey, ez, __double2float_rn(__ddiv_rn(1.0, (double)dot_rn(ex, ey, ez, ex, ey, ez))));
+}
 
 __global__ void k_pack_tri(int np, const float* __restrict__ x, const float* __restrict__ y,
                            const float* __restrict__ z, const uint32_t* __restrict__ idx, const float* __restrict__ nx,
@@ -35,17 +50,15 @@ __global__ void k_pack_tri(int np, const float* __restrict__ x, const float* __r
   t.a = make_float4(x[p0], y[p0], z[p0], x[p1]);
   t.b = make_float4(y[p1], z[p1], x[p2], y[p2]);
   t.c = make_float4(z[p2], nx[j], ny[j], nz[j]);
+  t.e = edge_rec(x[p0], y[p0], z[p0], x[p1], y[p1], z[p1]);
+  t.f = edge_rec(x[p1], y[p1], z[p1], x[p2], y[p2], z[p2]);
+  t.g = edge_rec(x[p2], y[p2], z[p2], x[p0], y[p0], z[p0]);
   out[j] = t;
 }
 
-__device__ __forceinline__ float dot_rn(float a0, float a1, float a2, float b0, float b1, float b2) {
-  return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
-}
-
 // squared distance |e x d|^2 / |e|^2 to the edge's line, kept when the foot lies on the edge
-__device__ __forceinline__ void edge_rn(float e0, float e1, float e2, float d0, float d1, float d2, float ox, float oy,
-                                        float oz, float& best, float& px, float& py, float& pz) {
-  const float inv = __double2float_rn(__ddiv_rn(1.0, (double)dot_rn(e0, e1, e2, e0, e1, e2)));
+__device__ __forceinline__ void edge_rn(float e0, float e1, float e2, float inv, float d0, float d1, float d2, float ox,
+                                        float oy, float oz, float& best, float& px, float& py, float& pz) {
   const float r0 = __fsub_rn(__fmul_rn(e1, d2), __fmul_rn(e2, d1));
   const float r1 = __fsub_rn(__fmul_rn(e2, d0), __fmul_rn(e0, d2));
   const float r2 = __fsub_rn(__fmul_rn(e0, d1), __fmul_rn(e1, d0));
@@ -84,12 +97,12 @@ __device__ __forceinline__ void closest_rn(const PanelTri& p, float tx, float ty
   if (db < best) { best = db; px = x1; py = y1; pz = z1; }
   const float dc = dot_rn(c0, c1, c2, c0, c1, c2);
   if (dc < best) { best = dc; px = x2; py = y2; pz = z2; }
-  const float e01x = __fsub_rn(x1, x0), e01y = __fsub_rn(y1, y0), e01z = __fsub_rn(z1, z0);
-  edge_rn(e01x, e01y, e01z, a0, a1, a2, x0, y0, z0, best, px, py, pz);
-  const float e12x = __fsub_rn(x2, x1), e12y = __fsub_rn(y2, y1), e12z = __fsub_rn(z2, z1);
-  edge_rn(e12x, e12y, e12z, b0, b1, b2, x1, y1, z1, best, px, py, pz);
-  const float e20x = __fsub_rn(x0, x2), e20y = __fsub_rn(y0, y2), e20z = __fsub_rn(z0, z2);
-  edge_rn(e20x, e20y, e20z, c0, c1, c2, x2, y2, z2, best, px, py, pz);
+  const float e01x = p.e.x, e01y = p.e.y, e01z = p.e.z;
+  edge_rn(e01x, e01y, e01z, p.e.w, a0, a1, a2, x0, y0, z0, best, px, py, pz);
+  const float e12x = p.f.x, e12y = p.f.y, e12z = p.f.z;
+  edge_rn(e12x, e12y, e12z, p.f.w, b0, b1, b2, x1, y1, z1, best, px, py, pz);
+  const float e20x = p.g.x, e20y = p.g.y, e20z = p.g.z;
+  edge_rn(e20x, e20y, e20z, p.g.w, c0, c1, c2, x2, y2, z2, best, px, py, pz);
   const float s01 = side_rn(nx, ny, nz, e01x, e01y, e01z, a0, a1, a2);
   const float s12 = side_rn(nx, ny, nz, e12x, e12y, e12z, b0, b1, b2);
   const float s20 = side_rn(nx, ny, nz, e20x, e20y, e20z, c0, c1, c2);
