@@ -38,7 +38,8 @@ enum {
   O3G_ERR_TIMEOUT = 6,       /* a bounded device-side wait ran out                 */
   O3G_ERR_SINGULAR = 7,      /* zero or non-finite pivot in a factorisation        */
   O3G_ERR_NONFINITE = 8,     /* non-finite values where finite ones are required   */
-  O3G_ERR_STATE = 9          /* call made in the wrong state (e.g. solve before A) */
+  O3G_ERR_STATE = 9,         /* call made in the wrong state (e.g. solve before A) */
+  O3G_ERR_CAPACITY = 10      /* output arrays too small; the needed count is returned */
 };
 
 /* ---- enumerations -------------------------------------------------------------- */
@@ -55,6 +56,9 @@ enum { O3G_CORE_RM = 0, O3G_CORE_WL = 1, O3G_CORE_EXP = 2, O3G_CORE_GAUSS = 3, O
 enum { O3G_PREC_PLAIN = 0, O3G_PREC_COMPENSATED = 1, O3G_PREC_FP64 = 2 };
 
 enum { O3G_MEM_HOST = 0, O3G_MEM_DEVICE = 1 };
+
+/* Diffusion core types (CoreType, Core.h:27): they set the neighbour weight of the split. */
+enum { O3G_DIFFCORE_GAUSSIAN = 0, O3G_DIFFCORE_COMPACTG = 1 };
 
 /* ---- library ------------------------------------------------------------------- */
 /* Human-readable text for a status code (static storage). */
@@ -352,6 +356,32 @@ int32_t o3g_represent_as_particles(const o3g_surface_t* surf, float offset, cons
  * call waits and returns the number pushed; otherwise it is asynchronous. */
 int32_t o3g_clear_inner_layer(int32_t n, float* x, float* y, float* z, const o3g_surface_t* surf, float cutoff_mult,
                               float ips, int32_t* npushed, void* stream);
+
+/* ---- particle split and merge --------------------------------------------------------
+ * Replaces split_elongated<float> (Split.h:44-270; called after every step by
+ * split_operation, Simulation.cpp:833): every particle with elong > threshold is split in
+ * two along its strength direction, half the strength each, with the reference's
+ * curvature correction from its neighbours within 3 r / overlap (weights from core_func,
+ * O3G_DIFFCORE_*).  Device arrays of `capacity` particles; the split ones are updated in
+ * place and their children appended at [n, n + nsplit) in index order.  When capacity is
+ * below n + nsplit nothing is changed, *nsplit is set and O3G_ERR_CAPACITY returned.
+ * Waits for the result.  Bit-identical to the reference's sequential loop, except where two
+ * neighbours of a split particle are at exactly equal distance (visited here in index
+ * order, by the reference in its kd-tree's order). */
+int32_t o3g_split_elongated(int32_t n, int32_t capacity, float* x, float* y, float* z, float* r, float* elong,
+                            float* sx, float* sy, float* sz, int32_t core_func, float particle_overlap,
+                            float threshold, int32_t* nsplit, void* stream);
+
+/* Replaces merge_close_particles<float> (Merge.h:45-218; called by merge_operation in
+ * diffusion, Diffusion.h:298,355): in index order, each surviving particle absorbs the
+ * surviving neighbours closer than half a nominal separation (r / overlap) whose merge error
+ * is below threshold (relative to the mean strength) or that are closer than a tenth of it;
+ * absorbed particles are removed and the survivors compacted in place, in order, to
+ * n - nremoved.  adapt_radii: merged radii follow the reference's volume rule.  Waits for the
+ * result.  Bit-identical to the reference's sequential loop (ties in distance as above). */
+int32_t o3g_merge_close_particles(int32_t n, float* x, float* y, float* z, float* sx, float* sy, float* sz,
+                                  float* r, float particle_overlap, float threshold, int32_t adapt_radii,
+                                  int32_t* nremoved, void* stream);
 
 /* ---- points_affect_points without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory

@@ -15,6 +15,7 @@ STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "no usable sm_103 device",
     4: "device allocation failed", 5: "iterative refinement did not converge", 6: "device-side wait timed out",
     7: "singular or non-finite pivot", 8: "non-finite input", 9: "call made in the wrong state",
+    10: "output arrays too small",
 }
 CORES = {"rm": 0, "wl": 1, "exp": 2, "gauss": 3, "v2": 4}
 PRECS = {"plain": 0, "compensated": 1, "fp64": 2}
@@ -134,6 +135,10 @@ def _declare(l):
     l.o3g_represent_as_particles.argtypes = [P, c_f] + [P] * 11 + [P]
     l.o3g_clear_inner_layer.restype = c_i32
     l.o3g_clear_inner_layer.argtypes = [c_i32, P, P, P, P, c_f, c_f, P, P]
+    l.o3g_split_elongated.restype = c_i32
+    l.o3g_split_elongated.argtypes = [c_i32, c_i32] + [P] * 8 + [c_i32, c_f, c_f, P, P]
+    l.o3g_merge_close_particles.restype = c_i32
+    l.o3g_merge_close_particles.argtypes = [c_i32] + [P] * 7 + [c_f, c_f, c_i32, P, P]
     l.o3g_rk2_body_strengths.restype = c_i32
     l.o3g_rk2_body_strengths.argtypes = [P, P, P, P]
     l.o3g_bem_size.restype = c_i32

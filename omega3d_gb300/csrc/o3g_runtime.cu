@@ -140,6 +140,7 @@ const char* o3g_status_string(int32_t s) {
     case O3G_ERR_SINGULAR: return "singular or non-finite pivot";
     case O3G_ERR_NONFINITE: return "non-finite input";
     case O3G_ERR_STATE: return "call made in the wrong state";
+    case O3G_ERR_CAPACITY: return "output arrays too small";
     default: return "unknown status";
   }
 }

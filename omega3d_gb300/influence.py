@@ -332,6 +332,62 @@ def represent_as_particles(bdry, offset, ts=None, bc=None, arrays=None, stream=N
     return px, ps
 
 
+DIFFCORES = {"gaussian": 0, "compactg": 1}
+
+
+def _f32_dev(a, shape, what):
+    if not (_is_dev(a) and a.dtype == torch.float32 and a.is_contiguous() and tuple(a.shape) == shape):
+        raise ValueError("%s: need a contiguous float32 CUDA tensor of shape %s" % (what, shape))
+
+
+def split_elongated(x, s, r, elong, core_func="gaussian", overlap=1.5, threshold=1.2, stream=None):
+    """split_elongated<float> (Split.h:44-270) on torch CUDA float32 tensors x[3, n],
+    s[3, n], r[n], elong[n]: every particle with elong > threshold is split in two along its
+    strength, with the reference's curvature correction (core_func 'gaussian' or 'compactg',
+    Core.h:27).  Returns (x, s, r, elong, nsplit): new tensors of n + nsplit particles (the
+    split ones updated, their children appended in index order), or the inputs unchanged
+    when nothing splits."""
+    n = x.shape[1]
+    for a, shp, w in ((x, (3, n), "x"), (s, (3, n), "s"), (r, (n,), "r"), (elong, (n,), "elong")):
+        _f32_dev(a, shp, "split_elongated " + w)
+    h = stream if stream is not None else ExecEnv().stream_handle(True)
+    ns = ctypes.c_int32()
+    core = DIFFCORES[core_func]
+    lib = L.lib()
+    st = lib.o3g_split_elongated(n, n, *_rows(x, 3), _base(r), _base(elong), *_rows(s, 3), core, overlap, threshold,
+                                 ctypes.byref(ns), h)
+    if st == 0:
+        return x, s, r, elong, 0
+    if st != 10:
+        L.check(st, "o3g_split_elongated")
+    cap = n + ns.value
+    x2 = torch.empty((3, cap), dtype=torch.float32, device=x.device)
+    s2 = torch.empty((3, cap), dtype=torch.float32, device=x.device)
+    r2 = torch.empty(cap, dtype=torch.float32, device=x.device)
+    e2 = torch.empty(cap, dtype=torch.float32, device=x.device)
+    x2[:, :n], s2[:, :n], r2[:n], e2[:n] = x, s, r, elong
+    L.check(lib.o3g_split_elongated(n, cap, *_rows(x2, 3), _base(r2), _base(e2), *_rows(s2, 3), core, overlap,
+                                    threshold, ctypes.byref(ns), h), "o3g_split_elongated")
+    return x2, s2, r2, e2, ns.value
+
+
+def merge_close_particles(x, s, r, overlap=1.5, threshold=0.2, adapt_radii=False, stream=None):
+    """merge_close_particles<float> (Merge.h:45-218) on torch CUDA float32 tensors x[3, n],
+    s[3, n], r[n], merged and compacted IN PLACE (the first n - nremoved entries of each row
+    hold the survivors, in order).  Returns (x, s, r, nremoved) with the survivors as new
+    contiguous tensors."""
+    n = x.shape[1]
+    for a, shp, w in ((x, (3, n), "x"), (s, (3, n), "s"), (r, (n,), "r")):
+        _f32_dev(a, shp, "merge_close_particles " + w)
+    h = stream if stream is not None else ExecEnv().stream_handle(True)
+    nr = ctypes.c_int32()
+    L.check(L.lib().o3g_merge_close_particles(n, *_rows(x, 3), *_rows(s, 3), _base(r), overlap, threshold,
+                                              int(bool(adapt_radii)), ctypes.byref(nr), h),
+            "o3g_merge_close_particles")
+    k = n - nr.value
+    return x[:, :k].contiguous(), s[:, :k].contiguous(), r[:k].contiguous(), nr.value
+
+
 def panels_on_panels_coeff(src_arrays, targ_arrays, nunk, is_self, out, ld=None, maxlev=3, stream=None):
     """Coefficients.h:169: write the column-major (ntarg*nunk) x (nsrc*nunk) block into the
     device tensor `out` (viewed with leading dimension ld, default ntarg*nunk)."""

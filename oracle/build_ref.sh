@@ -12,7 +12,11 @@
 #   oracle/ref_driver.cpp (this project's restatement of the loops around them)
 # and oracle/_ref/libo3dref_reflect.so from the reference's Reflect.h (streamed without
 # its includes of Omega3D.h / Points.h / Surfaces.h, which need Eigen and Vc; the
-# declarations it uses come from oracle/reflect_prelude.h) with oracle/ref_reflect_driver.cpp.
+# declarations it uses come from oracle/reflect_prelude.h) with oracle/ref_reflect_driver.cpp,
+# and oracle/_ref/libo3dref_splitmerge.so from the reference's Split.h and Merge.h (each
+# streamed up to its *_operation wrapper, which needs the element classes) with the
+# vendored lib/nanoflann/nanoflann.hpp, oracle/eigen_shim (a stand-in for the few Eigen
+# members they use), oracle/splitmerge_prelude.h and oracle/ref_splitmerge_driver.cpp.
 #
 # The reference location defaults to /root/reference/src; set O3D_REFERENCE_SRC to
 # override.  When the sources are absent (e.g. on a machine without the reference) the
@@ -54,4 +58,15 @@ if [ -f "$REF/Reflect.h" ]; then
   } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w -I"$REF" -x c++ - \
         -o "$OUT/libo3dref_reflect.so"
   echo "build_ref: built $OUT/libo3dref_reflect.so"
+fi
+NANOFLANN="${O3D_REFERENCE_LIB:-$REF/../lib}"
+if [ -f "$REF/Split.h" ] && [ -f "$REF/Merge.h" ] && [ -f "$NANOFLANN/nanoflann/nanoflann.hpp" ]; then
+  {
+    cat "$HERE/splitmerge_prelude.h"
+    sed -n '1,/^\/\/ split any collections of Points/p' "$REF/Split.h"
+    sed -n '1,/^\/\/ run some number of merge ops/p' "$REF/Merge.h"
+    cat "$HERE/ref_splitmerge_driver.cpp"
+  } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fPIC -shared -w -I"$REF" -I"$NANOFLANN" \
+        -I"$HERE/eigen_shim" -x c++ - -o "$OUT/libo3dref_splitmerge.so"
+  echo "build_ref: built $OUT/libo3dref_splitmerge.so"
 fi

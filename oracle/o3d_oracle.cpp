@@ -1143,3 +1143,243 @@ extern "C" int o3o_represent_as_particles(int nn, const float* nodes, int np, co
   }
   return 0;
 }
+
+// ---------------------------------------------------------------------------------
+// Split.h / Merge.h: particle split and merge (float S, the instantiation the simulation
+// uses, Simulation.cpp:833 and Diffusion.h:298,355).
+//
+// Both operators find neighbours with a radius search over the particle positions as
+// they were when the operator started (the reference builds a nanoflann kd-tree over a
+// copy of them, Split.h:65-76, Merge.h:76-87).  The match criterion is nanoflann 1.3.1's
+// (lib/nanoflann/nanoflann.hpp): d2 = ((q0-p0)^2 + (q1-p1)^2) + (q2-p2)^2 in float
+// (L2_Adaptor::evalMetric, :383-405, query minus point) and d2 < radius (strict,
+// RadiusResultSet::addPoint, :249-253).  Matches are visited in increasing d2
+// (params.sorted, :1285-1286); equal d2 are taken in increasing index here, where the
+// reference's order for such ties depends on its kd-tree layout.  The neighbour search
+// below is a uniform cell list; it finds exactly the same match set.
+namespace {
+
+struct OracleCells {
+  double lo[3] = {0, 0, 0};
+  double inv_h = 1.0;
+  std::vector<uint64_t> keys;   // sorted cell keys
+  std::vector<int> order;       // particle index per sorted key
+
+  static constexpr int64_t kMaxCell = (1 << 21) - 1;
+
+  void coords(float px, float py, float pz, int64_t c[3]) const {
+    const double p[3] = {px, py, pz};
+    for (int d = 0; d < 3; ++d) {
+      double u = std::floor((p[d] - lo[d]) * inv_h);
+      if (!(u >= 0.0)) u = 0.0;
+      if (u > (double)kMaxCell) u = (double)kMaxCell;
+      c[d] = (int64_t)u;
+    }
+  }
+  static uint64_t key(int64_t cx, int64_t cy, int64_t cz) {
+    return ((uint64_t)cx << 42) | ((uint64_t)cy << 21) | (uint64_t)cz;
+  }
+  // cell size: the largest search radius, enlarged so that float rounding of a match's
+  // distance can never put it two cells away
+  void build(int n, const float* x, const float* y, const float* z, double rmax) {
+    const double h = rmax > 0.0 ? rmax * (1.0 + 1.0 / 1024.0) : 1.0;
+    inv_h = 1.0 / h;
+    for (int d = 0; d < 3; ++d) lo[d] = std::numeric_limits<double>::max();
+    for (int i = 0; i < n; ++i) {
+      lo[0] = std::min(lo[0], (double)x[i]);
+      lo[1] = std::min(lo[1], (double)y[i]);
+      lo[2] = std::min(lo[2], (double)z[i]);
+    }
+    std::vector<std::pair<uint64_t, int>> kv((size_t)n);
+    for (int i = 0; i < n; ++i) {
+      int64_t c[3];
+      coords(x[i], y[i], z[i], c);
+      kv[i] = {key(c[0], c[1], c[2]), i};
+    }
+    std::sort(kv.begin(), kv.end());
+    keys.resize(n);
+    order.resize(n);
+    for (int i = 0; i < n; ++i) { keys[i] = kv[i].first; order[i] = kv[i].second; }
+  }
+  // (d2, j) for every j with d2(q - p_j) < thr, sorted by (d2, j)
+  void search(float qx, float qy, float qz, float thr, const float* x, const float* y, const float* z,
+              std::vector<std::pair<float, int>>& out) const {
+    out.clear();
+    int64_t c[3];
+    coords(qx, qy, qz, c);
+    for (int64_t cx = std::max<int64_t>(c[0] - 1, 0); cx <= std::min<int64_t>(c[0] + 1, kMaxCell); ++cx)
+      for (int64_t cy = std::max<int64_t>(c[1] - 1, 0); cy <= std::min<int64_t>(c[1] + 1, kMaxCell); ++cy) {
+        const uint64_t k0 = key(cx, cy, std::max<int64_t>(c[2] - 1, 0));
+        const uint64_t k1 = key(cx, cy, std::min<int64_t>(c[2] + 1, kMaxCell));
+        auto b = std::lower_bound(keys.begin(), keys.end(), k0);
+        auto e = std::upper_bound(keys.begin(), keys.end(), k1);
+        for (auto it = b; it != e; ++it) {
+          const int j = order[it - keys.begin()];
+          const float d0 = qx - x[j], d1 = qy - y[j], d2 = qz - z[j];
+          float dist = d0 * d0;
+          dist += d1 * d1;
+          dist += d2 * d2;
+          if (dist < thr) out.push_back({dist, j});
+        }
+      }
+    std::sort(out.begin(), out.end());
+  }
+};
+
+// get_core_coefficient<float> (Core.h:32-35): CoreType gaussian = 0, compactg = 1
+float core_coefficient(int core) {
+  return core == 0 ? (float)(1.0 / (M_PI * std::sqrt(M_PI))) : (float)0.23873241;
+}
+
+}  // namespace
+
+// split_elongated<float> (Split.h:44-270).  Arrays have room for cap particles; the split
+// ones are halved and moved in place and their children appended at [n, n + nsplit).
+// Returns nsplit, or -1 when cap is too small or the arguments are bad.
+extern "C" int o3o_split_elongated(int n, int cap, float* x, float* y, float* z, float* r, float* elong, float* sx,
+                                   float* sy, float* sz, int core, float overlap, float threshold) {
+  if (n < 0 || cap < n) return -1;
+  int m = 0;
+  double rmax = 0.0;
+  for (int i = 0; i < n; ++i)
+    if (elong[i] > threshold) {
+      ++m;
+      const float nom_sep = r[i] / overlap;
+      rmax = std::max(rmax, (double)(float)(3.0 * nom_sep));
+    }
+  if (n + m > cap) return -1;
+  if (m == 0) return 0;
+  // the search runs on the positions before any split (the kd-tree's copy)
+  const std::vector<float> px(x, x + n), py(y, y + n), pz(z, z + n);
+  OracleCells cells;
+  cells.build(n, px.data(), py.data(), pz.data(), rmax);
+  const float coef = core_coefficient(core);
+  std::vector<std::pair<float, int>> matches;
+  int k = n;
+  for (int i = 0; i < n; ++i) {
+    if (!(elong[i] > threshold)) continue;
+    // normalizeVec (MathHelper.h:186-192)
+    float axis[3] = {sx[i], sy[i], sz[i]};
+    const float len = (float)(1.0 / std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]));
+    for (int d = 0; d < 3; ++d) axis[d] *= len;
+    const float nom_sep = r[i] / overlap;
+    const float halfd = (float)(0.25 * elong[i] * nom_sep);
+    const float search_rad = (float)(3.0 * nom_sep);
+    const float thr = (float)std::pow(search_rad, 2);
+    cells.search(x[i], y[i], z[i], thr, px.data(), py.data(), pz.data(), matches);
+    float dVol = 0.0f;
+    float curv[3] = {0.0f, 0.0f, 0.0f};
+    for (const auto& mt : matches) {
+      const int j = mt.second;
+      const float dx[3] = {x[i] - x[j], y[i] - y[j], z[i] - z[j]};
+      const float s0 = sx[j], s1 = sy[j], s2 = sz[j];
+      const float factor = std::sqrt(mt.first / (r[j] * r[i])) * overlap;
+      const float fac2 = (float)(coef * std::exp(-(std::pow(factor, 3))));
+      const float tStr = std::sqrt(s0 * s0 + s1 * s1 + s2 * s2);
+      const float wgt = axis[0] * s0 + axis[1] * s1 + axis[2] * s2;
+      if (tStr > 1.e-15 && wgt > 0.0) {
+        const float dsx = axis[0] - sx[j] / tStr;
+        const float dsy = axis[1] - sy[j] / tStr;
+        const float dsz = axis[2] - sz[j] / tStr;
+        const float thisfac = wgt * fac2 * tStr;
+        curv[0] += thisfac * (dx[1] * dsz - dx[2] * dsy);
+        curv[1] += thisfac * (dx[2] * dsx - dx[0] * dsz);
+        curv[2] += thisfac * (dx[0] * dsy - dx[1] * dsx);
+        dVol += thisfac;
+      }
+    }
+    x[k] = x[i] - halfd * axis[0];
+    y[k] = y[i] - halfd * axis[1];
+    z[k] = z[i] - halfd * axis[2];
+    r[k] = r[i];
+    elong[k] = (float)(0.5 * elong[i]);
+    sx[k] = (float)(0.5 * sx[i]);
+    sy[k] = (float)(0.5 * sy[i]);
+    sz[k] = (float)(0.5 * sz[i]);
+    x[i] += halfd * axis[0];
+    y[i] += halfd * axis[1];
+    z[i] += halfd * axis[2];
+    elong[i] *= 0.5;
+    sx[i] *= 0.5;
+    sy[i] *= 0.5;
+    sz[i] *= 0.5;
+    if (dVol > 1e-15) {
+      for (int d = 0; d < 3; ++d) curv[d] /= dVol;
+      const float f = (float)(overlap * 0.398967 / r[i]);
+      for (int d = 0; d < 3; ++d) curv[d] *= f;
+      const float dsx = sy[i] * curv[2] - sz[i] * curv[1];
+      const float dsy = sz[i] * curv[0] - sx[i] * curv[2];
+      const float dsz = sx[i] * curv[1] - sy[i] * curv[0];
+      sx[k] += dsx;
+      sy[k] += dsy;
+      sz[k] += dsz;
+      sx[i] -= dsx;
+      sy[i] -= dsy;
+      sz[i] -= dsz;
+    }
+    ++k;
+  }
+  return m;
+}
+
+// merge_close_particles<float> (Merge.h:45-218): greedy merge in index order, then the
+// survivors compacted in place.  Returns the number removed, or -1 on bad arguments.
+extern "C" int o3o_merge_close_particles(int n, float* x, float* y, float* z, float* sx, float* sy, float* sz,
+                                         float* r, float overlap, float threshold, int adapt_radii) {
+  if (n < 0) return -1;
+  if (n == 0) return 0;
+  const float initial_thresh = 0.5f;
+  const float always_thresh = 0.1f;
+  float meanstr = 0.0f;
+  for (int i = 0; i < n; ++i) meanstr += std::sqrt(sx[i] * sx[i] + sy[i] * sy[i] + sz[i] * sz[i]);
+  meanstr /= (float)n;
+  double rmax = 0.0;
+  for (int i = 0; i < n; ++i) rmax = std::max(rmax, (double)((r[i] / overlap) * initial_thresh));
+  const std::vector<float> px(x, x + n), py(y, y + n), pz(z, z + n);
+  OracleCells cells;
+  cells.build(n, px.data(), py.data(), pz.data(), rmax);
+  std::vector<char> erase((size_t)n, 0);
+  std::vector<std::pair<float, int>> matches;
+  for (int i = 0; i < n; ++i) {
+    if (erase[i]) continue;
+    const float nom_sep = r[i] / overlap;
+    const float search_rad = nom_sep * initial_thresh;
+    const float thr = (float)std::pow(search_rad, 2);
+    cells.search(x[i], y[i], z[i], thr, px.data(), py.data(), pz.data(), matches);
+    if (matches.size() <= 1) continue;
+    for (const auto& mt : matches) {
+      const int j = mt.second;
+      if (j == i || erase[j]) continue;
+      const float dist = std::sqrt(mt.first);
+      if (!(dist < initial_thresh * r[j] / overlap)) continue;
+      const float si = std::sqrt(sx[i] * sx[i] + sy[i] * sy[i] + sz[i] * sz[i]) + std::numeric_limits<float>::epsilon();
+      const float so = std::sqrt(sx[j] * sx[j] + sy[j] * sy[j] + sz[j] * sz[j]) + std::numeric_limits<float>::epsilon();
+      const float frac = so / (si + so);
+      bool do_merge = false;
+      const float min_rad = std::min(r[j], r[i]) / overlap;
+      if (dist * frac * si < threshold * meanstr * min_rad) do_merge = true;
+      if (dist < always_thresh * min_rad) do_merge = true;
+      if (!do_merge) continue;
+      const float omfrac = (float)(1.0 - frac);
+      const float nx = x[i] * omfrac + x[j] * frac;
+      const float ny = y[i] * omfrac + y[j] * frac;
+      const float nz = z[i] * omfrac + z[j] * frac;
+      x[i] = nx;
+      y[i] = ny;
+      z[i] = nz;
+      if (adapt_radii) r[i] = (float)std::cbrt(omfrac * std::pow(r[i], 3) + frac * std::pow(r[j], 3));
+      sx[i] = sx[i] + sx[j];
+      sy[i] = sy[i] + sy[j];
+      sz[i] = sz[i] + sz[j];
+      erase[j] = 1;
+    }
+  }
+  int copyto = 0;
+  for (int i = 0; i < n; ++i) {
+    if (erase[i]) continue;
+    x[copyto] = x[i]; y[copyto] = y[i]; z[copyto] = z[i]; r[copyto] = r[i];
+    sx[copyto] = sx[i]; sy[copyto] = sy[i]; sz[copyto] = sz[i];
+    ++copyto;
+  }
+  return n - copyto;
+}

@@ -357,3 +357,54 @@ def represent_as_particles(nodes, idx, area, x1, x2, norm, offset, ts, bc1=None,
     if rc != 0:
         raise RuntimeError("oracle represent_as_particles failed")
     return px, ps
+
+
+def ref_splitmerge_available():
+    return os.path.exists(os.path.join(REF_DIR, "libo3dref_splitmerge.so"))
+
+
+def _splitmerge_lib(use_ref):
+    if not use_ref:
+        return lib(), "o3o_"
+    if "splitmerge" not in _ref:
+        _ref["splitmerge"] = ctypes.CDLL(os.path.join(REF_DIR, "libo3dref_splitmerge.so"))
+    return _ref["splitmerge"], "ref_"
+
+
+def split_elongated(x, s, r, elong, core=0, overlap=1.5, threshold=1.2, use_ref=False):
+    """split_elongated<float> (Split.h:44-270) on x[3, n], s[3, n], r[n], elong[n]
+    (core 0 = gaussian, 1 = compactg, Core.h:27).  Returns new arrays
+    (x, s, r, elong) of n + nsplit particles (children appended in index order) and nsplit."""
+    n = x.shape[1]
+    m = int(np.count_nonzero(np.asarray(elong, np.float32) > np.float32(threshold)))
+    cap = n + m
+    xs = np.zeros((3, cap), np.float32)
+    ss = np.zeros((3, cap), np.float32)
+    rs = np.zeros(cap, np.float32)
+    es = np.zeros(cap, np.float32)
+    xs[:, :n], ss[:, :n], rs[:n], es[:n] = x, s, r, elong
+    L, pre = _splitmerge_lib(use_ref)
+    rc = getattr(L, pre + "split_elongated")(
+        ctypes.c_int(n), ctypes.c_int(cap), _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(rs), _p(es), _p(ss[0]), _p(ss[1]),
+        _p(ss[2]), ctypes.c_int(core), ctypes.c_float(overlap), ctypes.c_float(threshold))
+    if rc < 0:
+        raise RuntimeError("split_elongated failed")
+    assert rc == m
+    return xs, ss, rs, es, rc
+
+
+def merge_close_particles(x, s, r, overlap=1.5, threshold=0.2, adapt_radii=False, use_ref=False):
+    """merge_close_particles<float> (Merge.h:45-218) on x[3, n], s[3, n], r[n].  Returns
+    new arrays (x, s, r) of the survivors in their original order and the number removed."""
+    n = x.shape[1]
+    xs = np.array(x, np.float32, order="C", copy=True)
+    ss = np.array(s, np.float32, order="C", copy=True)
+    rs = np.array(r, np.float32, copy=True)
+    L, pre = _splitmerge_lib(use_ref)
+    rc = getattr(L, pre + "merge_close_particles")(
+        ctypes.c_int(n), _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(ss[0]), _p(ss[1]), _p(ss[2]), _p(rs),
+        ctypes.c_float(overlap), ctypes.c_float(threshold), ctypes.c_int(int(bool(adapt_radii))))
+    if rc < 0:
+        raise RuntimeError("merge_close_particles failed")
+    k = n - rc
+    return np.ascontiguousarray(xs[:, :k]), np.ascontiguousarray(ss[:, :k]), rs[:k].copy(), rc

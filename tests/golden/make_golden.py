@@ -2,11 +2,14 @@
 
 Run in a checkout that has the reference sources (oracle/build_ref.sh compiles
 src/Kernels.h, src/CoreFunc.h and src/MathHelper.h of the reference into
-oracle/_ref/libo3dref_<core>.so, and src/Reflect.h into oracle/_ref/libo3dref_reflect.so;
-the loops around them are oracle/ref_driver.cpp and oracle/ref_reflect_driver.cpp):
+oracle/_ref/libo3dref_<core>.so, src/Reflect.h into oracle/_ref/libo3dref_reflect.so, and
+src/Split.h + src/Merge.h with lib/nanoflann into oracle/_ref/libo3dref_splitmerge.so;
+the loops around them are oracle/ref_driver.cpp, oracle/ref_reflect_driver.cpp and
+oracle/ref_splitmerge_driver.cpp):
 
     sh oracle/build_ref.sh && python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py --only reflect                       # reflect.npz alone
+    python tests/golden/make_golden.py --only splitmerge                    # splitmerge.npz alone
 
 Every fixture holds its seeded inputs and the outputs of the reference build for the
 precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
@@ -83,9 +86,33 @@ def write_reflect():
                           "source": "reference Reflect.h"}, x_in=pts, **geo, **out)
 
 
+def write_splitmerge():
+    """Split and merge of a jittered 12^3 lattice by the reference's own Split.h / Merge.h
+    (oracle/_ref/libo3dref_splitmerge.so, with the vendored nanoflann)."""
+    if not O.ref_splitmerge_available():
+        raise SystemExit("oracle/_ref/libo3dref_splitmerge.so missing: run sh oracle/build_ref.sh")
+    x, s, r, e = W.lattice_particles(k=12, seed=16)
+    out = {}
+    for core in (0, 1):
+        xs, ss, rs, es, m = O.split_elongated(x, s, r, e, core, 1.5, 1.2, use_ref=True)
+        out.update({"split%d_x" % core: xs, "split%d_s" % core: ss, "split%d_r" % core: rs,
+                    "split%d_e" % core: es})
+    for name, thr, adapt in (("merge_vrm", 0.2, False), ("merge_core", 0.02, False), ("merge_amr", 0.2, True)):
+        xm, sm, rm, nrem = O.merge_close_particles(x, s, r, 1.5, thr, adapt, use_ref=True)
+        out.update({name + "_x": xm, name + "_s": sm, name + "_r": rm})
+    _save("splitmerge.npz", {"pinned": True, "overlap": 1.5, "split_threshold": 1.2,
+                             "merge": {"merge_vrm": [0.2, False], "merge_core": [0.02, False],
+                                       "merge_amr": [0.2, True]},
+                             "source": "reference Split.h / Merge.h with lib/nanoflann"},
+          x_in=x, s_in=s, r_in=r, e_in=e, **out)
+
+
 def main():
     if "--only" in sys.argv and sys.argv[-1] == "reflect":
         write_reflect()
+        return
+    if "--only" in sys.argv and sys.argv[-1] == "splitmerge":
+        write_splitmerge()
         return
     for core in O.REF_CORES:
         if not O.ref_available(core):
@@ -138,6 +165,7 @@ def main():
     _save("sphere.npz", {"pinned": False, "scale": 2.0, "source": "oracle restatement of generate_ovoid"},
           **arrays)
     write_reflect()
+    write_splitmerge()
 
 
 if __name__ == "__main__":

@@ -274,3 +274,70 @@ def test_represent_as_particles_geometry():
     bc1 = np.ones(area.shape[0], np.float32)
     _, ps2 = O.represent_as_particles(nodes, idx, area, x1, x2, nm, 0.02, ts, bc1, 0 * bc1)
     assert np.allclose(ps2 - ts, x1 * area, atol=1e-7)
+
+
+# ---- split / merge (Split.h, Merge.h) ---------------------------------------------------
+def _bits(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_oracle_split_merge_match_golden():
+    d, meta = _gold("splitmerge.npz")
+    assert meta["pinned"]
+    x, s, r, e = d["x_in"], d["s_in"], d["r_in"], d["e_in"]
+    for core in (0, 1):
+        got = O.split_elongated(x, s, r, e, core, meta["overlap"], meta["split_threshold"])
+        assert got[4] > 0
+        for k, v in zip("xsre", got[:4]):
+            assert _bits(v, d["split%d_%s" % (core, k)])
+    for name, (thr, adapt) in meta["merge"].items():
+        got = O.merge_close_particles(x, s, r, meta["overlap"], thr, adapt)
+        assert got[3] > 0
+        for k, v in zip("xsr", got[:3]):
+            assert _bits(v, d["%s_%s" % (name, k)])
+
+
+@pytest.mark.parametrize("scale", [0.12, 0.03])
+def test_oracle_split_merge_bit_exact_vs_reference(scale):
+    """The restatement against the reference's own Split.h / Merge.h (with its nanoflann
+    kd-tree) on 27,000 jittered lattice particles: every split (both core types) and merge
+    (both thresholds, fixed and adaptive radii) result bit for bit."""
+    if not O.ref_splitmerge_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    x, s, r, e = W.lattice_particles(k=30, seed=31, elong_scale=scale)
+    for core in (0, 1):
+        a = O.split_elongated(x, s, r, e, core, 1.5, 1.2)
+        b = O.split_elongated(x, s, r, e, core, 1.5, 1.2, use_ref=True)
+        assert a[4] == b[4] > 0
+        assert all(_bits(u, v) for u, v in zip(a[:4], b[:4]))
+    for thr in (0.2, 0.02):
+        for adapt in (False, True):
+            a = O.merge_close_particles(x, s, r, 1.5, thr, adapt)
+            b = O.merge_close_particles(x, s, r, 1.5, thr, adapt, use_ref=True)
+            assert a[3] == b[3] > 0
+            assert all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
+
+
+def test_oracle_split_conserves_moments():
+    """Split.h's comment: zeroth and first moments kept.  The two halves' strengths add
+    back to the parent's (to float rounding) and their strength-weighted centre is the
+    parent's position."""
+    x, s, r, e = W.lattice_particles(k=16, seed=32)
+    xs, ss, rs, es, m = O.split_elongated(x, s, r, e, 0, 1.5, 1.2)
+    n = x.shape[1]
+    idx = np.nonzero(e > np.float32(1.2))[0]
+    assert m == idx.size > 0
+    tot = ss[:, idx].astype(np.float64) + ss[:, n:].astype(np.float64)
+    assert np.allclose(tot, s[:, idx], rtol=0, atol=1e-10)
+    mid = 0.5 * (xs[:, idx].astype(np.float64) + xs[:, n:].astype(np.float64))
+    assert np.allclose(mid, x[:, idx], rtol=0, atol=1e-7)
+    assert np.array_equal(es[idx], es[n:]) and np.array_equal(rs[n:], r[idx])
+
+
+def test_oracle_merge_conserves_strength():
+    x, s, r, _ = W.lattice_particles(k=16, seed=33)
+    xm, sm, rm, nrem = O.merge_close_particles(x, s, r, 1.5, 0.2, False)
+    assert nrem > 0 and xm.shape[1] == x.shape[1] - nrem
+    assert np.allclose(sm.astype(np.float64).sum(1), s.astype(np.float64).sum(1), rtol=0, atol=1e-8)
