@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--skip-bem-fp64", action="store_true", help="skip the FP64 LU comparator (~50 s)")
     ap.add_argument("--skip-ring", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
-    ap.add_argument("--only", choices=["bem", "ring", "batch", "coupled"], default=None,
+    ap.add_argument("--skip-splitmerge", action="store_true")
+    ap.add_argument("--only", choices=["bem", "ring", "batch", "coupled", "splitmerge"], default=None,
                     help="run one workload section alone and print its results (profiling)")
     ap.add_argument("--coupled-steps", type=int, default=2,
                     help="coupled sphere + 1M-particle Ralston steps to time (0 skips; 20 = the full run)")
@@ -527,6 +528,57 @@ def bench_coupled(args, G, torch, W):
     return out
 
 
+def bench_splitmerge(args, G, torch, W, reps=3):
+    """Particle split (Split.h:44-270) and merge (Merge.h:45-218) of 1,000,000 particles on
+    a jittered lattice (19 % elongated past the split threshold, 9 % with a neighbour within
+    half a separation).  Each call is timed end to end (both wait for their result) on fresh
+    device copies; the oracle port of the reference's sequential loops runs once on the host
+    for the CPU figure and to confirm the device results bit for bit."""
+    import oracle as O
+    x, s, r, e = W.lattice_particles(k=100, seed=41)
+    n = x.shape[1]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    X, S, R, E = (torch.from_numpy(a).to(dev) for a in (x, s, r, e))
+    out = {"particles": n, "overlap": 1.5, "split_threshold": 1.2, "merge_threshold": 0.2}
+
+    def timed(fn):
+        ts = []
+        res = None
+        for it in range(reps + 1):
+            args_ = (X.clone(), S.clone(), R.clone(), E.clone())
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = fn(*args_)
+            torch.cuda.synchronize()
+            if it > 0:
+                ts.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(ts), res
+
+    sp_ms, sp = timed(lambda a, b, c, d: G.split_elongated(a, b, c, d, "gaussian", 1.5, 1.2))
+    mg_ms, mg = timed(lambda a, b, c, d: G.merge_close_particles(a, b, c, 1.5, 0.2, False))
+    t0 = time.perf_counter()
+    osp = O.split_elongated(x, s, r, e, 0, 1.5, 1.2)
+    cpu_sp = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    omg = O.merge_close_particles(x, s, r, 1.5, 0.2, False)
+    cpu_mg = (time.perf_counter() - t0) * 1e3
+
+    def same(dev_arrs, host_arrs):
+        return all(np.array_equal(a.cpu().numpy().view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+                   for a, b in zip(dev_arrs, host_arrs))
+
+    out["split"] = {"ms": sp_ms, "particles_per_s": n / (sp_ms * 1e-3), "nsplit": sp[4],
+                    "cpu_port_ms": cpu_sp, "speedup_vs_cpu_port": cpu_sp / sp_ms,
+                    "bit_identical_to_port": bool(sp[4] == osp[4] and same(sp[:4], osp[:4]))}
+    out["merge"] = {"ms": mg_ms, "particles_per_s": n / (mg_ms * 1e-3), "nremoved": mg[3],
+                    "cpu_port_ms": cpu_mg, "speedup_vs_cpu_port": cpu_mg / mg_ms,
+                    "bit_identical_to_port": bool(mg[3] == omg[3] and same(mg[:3], omg[:3]))}
+    out["cpu_port"] = {"cores": 1, "kind": "port",
+                       "sample": "the whole 1,000,000-particle operator, single thread (the reference's loops are "
+                                 "sequential)"}
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -549,7 +601,8 @@ def run_ours(args):
         fn = {"bem": lambda: bench_bem(args, G, torch, W, fp64=not args.skip_bem_fp64),
               "ring": lambda: bench_ring(args, G, torch, W),
               "batch": lambda: bench_batch(args, G, torch, W, flush),
-              "coupled": lambda: bench_coupled(args, G, torch, W)}[args.only]
+              "coupled": lambda: bench_coupled(args, G, torch, W),
+              "splitmerge": lambda: bench_splitmerge(args, G, torch, W)}[args.only]
         res = fn()
         torch.cuda.synchronize()
         if rank == 0:
@@ -699,6 +752,9 @@ def run_ours(args):
     coupled = None
     if args.coupled_steps > 0:
         coupled = bench_coupled(args, G, torch, W)
+    splitmerge = None
+    if not args.skip_splitmerge:
+        splitmerge = bench_splitmerge(args, G, torch, W)
 
     if rank == 0:
         cpu_v, cpu_cores, cpu_sample, _ = cpu_reference(args)
@@ -726,7 +782,7 @@ def run_ours(args):
             "fp64_same_gpu": fp64 and {"value": fp64["value"], "unit": UNIT, "targets": fp64["targets"],
                                        "compensated_speedup": local_rate / fp64["value"]},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_sample},
-            "bem_solve": bem, "ring_rk2": ring, "batch": batch, "coupled": coupled,
+            "bem_solve": bem, "ring_rk2": ring, "batch": batch, "coupled": coupled, "split_merge": splitmerge,
             "clocks": clk, "gpu_launches": comp_launches, "num_sms": nsm,
             "wall_s_timed_region": comp_wall,
         }

@@ -7,25 +7,34 @@
 // (Split.h:65-76, Merge.h:76-87).  Here the search runs on a uniform cell list:
 //   * cell size = the largest search radius × (1 + 2^-10), so a match is never more than
 //     one cell away per axis, even after float rounding of its distance;
-//   * cells are keyed (cx << 42 | cy << 21 | cz) and particles radix-sorted by key, so the
-//     3 cells along z of each (cx, cy) column are one contiguous range (9 binary searches
-//     per query); positions are gathered into key order for coalesced candidate reads;
+//   * cells are keyed by their linear index (or, for grids of more than 16 cells per
+//     particle, cx << 42 | cy << 21 | cz) and particles radix-sorted by key, so the 3 cells
+//     along z of each (cx, cy) column are one contiguous range: 9 ranges per query, read
+//     from a start table (count + exclusive scan) or, for the packed keys, found by binary
+//     search; positions are gathered into key order for coalesced candidate reads;
 //   * the match test is nanoflann's: d2 = ((q0-p0)^2 + (q1-p1)^2) + (q2-p2)^2 in float
 //     (L2_Adaptor::evalMetric, query minus point), d2 < radius strictly
 //     (RadiusResultSet::addPoint);
-//   * each query's matches are written as (d2 bits << 32 | index) and sorted per query
-//     (CUB segmented sort), the reference's visiting order (params.sorted); equal d2 go in
-//     increasing index, where the reference's order for such ties follows its kd-tree.
+//   * each query's matches are written as (d2 bits << 32 | index) and put in that order,
+//     the reference's visiting order (params.sorted): by a rank sort in shared memory for
+//     the split (one warp per query, ~113 matches), by a CUB segmented sort for the merge
+//     (under one match per query on average); equal d2 go in increasing index, where the
+//     reference's order for such ties follows its kd-tree.
 //
 // Split.  Particle i's result reads, for every neighbour j < i that was itself split, j's
 // state after its split (x moved by halfd * axis, strength halved and corrected), and for
 // every other neighbour the state before the operator.  That is a dependency chain in
-// index order (about 300 deep for 12,000 splits of 64,000 particles).  One cooperative
-// kernel walks it: warps claim the elongated particles in increasing index through an
-// atomic counter, and a warp waits (bounded) only for the ready flags of lower-index split
-// neighbours, which were claimed earlier by running warps, so the smallest unfinished
-// particle always progresses.  The per-neighbour terms are computed by the warp's lanes;
-// the four sums (curvature and dVol) are then added in the sorted order by four lanes.
+// index order (about 300 deep for 12,000 splits of 64,000 particles, 829 for 189,000 of
+// 1,000,000).  A light kernel first gives every split particle its level in that graph
+// (one thread per particle, waiting only for lower ranks); the particles are sorted by
+// level; then one cooperative kernel walks the chain: warps claim particles in level order
+// through an atomic counter and wait (bounded) only for the ready flags of their
+// dependencies, which have lower levels, were claimed earlier by running warps, and so
+// always progress.  Claiming in level order instead of index order keeps every resident
+// warp on work whose dependencies are at most a level away.  Every term that reads no split state (neighbours not split,
+// or split later in index order: about 90 %) is computed beforehand by the parallel fill
+// kernel; the chain computes only the others, from the published states, and adds the four
+// sums (curvature and dVol) in the sorted order, one lane per sum.
 //
 // Merge.  Particle i's processing reads and writes only i and its matches, so particles
 // interact only within connected groups of the match graph.  Groups come from a lock-free
@@ -33,8 +42,9 @@
 // every loop ends); then one thread per group replays the reference's loop over the
 // group's particles in increasing index, in place.  The mean strength
 // (Merge.h:100-104) is the reference's sequential float sum: one thread adds the terms in
-// index order while the rest of its block stages them in shared memory.  The survivors are
-// compacted in order (Merge.h:181-204).
+// index order while the rest of its block stages them in shared memory, on a second stream
+// so that it overlaps the neighbour search.  The survivors are compacted in order
+// (Merge.h:181-204).
 //
 // Arithmetic follows the reference's expressions operation by operation, with the float /
 // double promotions its C++ implies, using _rn intrinsics so nothing is contracted.
@@ -46,6 +56,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 namespace o3g {
@@ -55,16 +66,22 @@ constexpr int64_t kMaxCell = (1 << 21) - 1;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kReadySpin = 1u << 28;
 constexpr uint64_t kReadyNs = 10ull * 1000 * 1000 * 1000;   // 10 s
+// pause between polls of a flag: thousands of waiting threads polling back to back load
+// the L2 enough to slow the stores they wait for
+constexpr unsigned kPollNs = 128;
 
 struct GridDev {
   double lo[3];
   double inv_h;
+  int64_t cmax[3];   // largest cell coordinate per axis
+  int dense;         // 1: keys are linear cell indices with a start table, 0: packed keys
 };
 
 struct CellList {
   const uint64_t* keys;   // sorted cell keys
   const int* order;       // particle index per sorted slot
   const float4* pos;      // positions in sorted order
+  const int* cstart;      // dense grids: first sorted slot of every cell (one past the end last)
   int n;
 };
 
@@ -74,7 +91,9 @@ __device__ __forceinline__ int ord(float f) {
 }
 __device__ __forceinline__ float unord(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
-__device__ __forceinline__ uint64_t cell_key(int64_t cx, int64_t cy, int64_t cz) {
+__device__ __forceinline__ uint64_t cell_key(const GridDev& g, int64_t cx, int64_t cy, int64_t cz) {
+  if (g.dense) return ((uint64_t)cx * (uint64_t)(g.cmax[1] + 1) + (uint64_t)cy) * (uint64_t)(g.cmax[2] + 1) +
+                      (uint64_t)cz;
   return ((uint64_t)cx << 42) | ((uint64_t)cy << 21) | (uint64_t)cz;
 }
 
@@ -84,7 +103,7 @@ __device__ __forceinline__ void cell_of(const GridDev& g, float px, float py, fl
   for (int d = 0; d < 3; ++d) {
     double u = floor((p[d] - g.lo[d]) * g.inv_h);
     if (!(u >= 0.0)) u = 0.0;
-    if (u > (double)kMaxCell) u = (double)kMaxCell;
+    if (u > (double)g.cmax[d]) u = (double)g.cmax[d];
     c[d] = (int64_t)u;
   }
 }
@@ -126,13 +145,15 @@ __device__ __forceinline__ void visit_cells(const CellList& cl, const GridDev& g
                                             int lane, F&& f) {
   int64_t c[3];
   cell_of(g, qx, qy, qz, c);
-  const int64_t z0 = c[2] > 0 ? c[2] - 1 : 0, z1 = c[2] < kMaxCell ? c[2] + 1 : kMaxCell;
-  const int64_t x0 = c[0] > 0 ? c[0] - 1 : 0, x1 = c[0] < kMaxCell ? c[0] + 1 : kMaxCell;
-  const int64_t y0 = c[1] > 0 ? c[1] - 1 : 0, y1 = c[1] < kMaxCell ? c[1] + 1 : kMaxCell;
+  const int64_t z0 = c[2] > 0 ? c[2] - 1 : 0, z1 = c[2] < g.cmax[2] ? c[2] + 1 : g.cmax[2];
+  const int64_t x0 = c[0] > 0 ? c[0] - 1 : 0, x1 = c[0] < g.cmax[0] ? c[0] + 1 : g.cmax[0];
+  const int64_t y0 = c[1] > 0 ? c[1] - 1 : 0, y1 = c[1] < g.cmax[1] ? c[1] + 1 : g.cmax[1];
   for (int64_t cx = x0; cx <= x1; ++cx)
     for (int64_t cy = y0; cy <= y1; ++cy) {
-      const int b = lower_bound_u64(cl.keys, cl.n, cell_key(cx, cy, z0));
-      const int e = upper_bound_u64(cl.keys, cl.n, cell_key(cx, cy, z1));
+      const uint64_t k0 = cell_key(g, cx, cy, z0), k1 = cell_key(g, cx, cy, z1);
+      // the cells (cx, cy, z0..z1) are consecutive keys: one range of sorted slots
+      const int b = g.dense ? cl.cstart[k0] : lower_bound_u64(cl.keys, cl.n, k0);
+      const int e = g.dense ? cl.cstart[k1 + 1] : upper_bound_u64(cl.keys, cl.n, k1);
       for (int t0 = b; t0 < e; t0 += LANES) {
         const int t = t0 + lane;
         f(t, t < e);
@@ -160,46 +181,69 @@ __device__ __forceinline__ float sumsq3(float a, float b, float c) {
 // ---------------------------------------------------------------------------------
 // cell list
 
-__global__ void k_sm_init(int* lo_ord, int* rmax_bits) {
-  if (threadIdx.x < 3) lo_ord[threadIdx.x] = 0x7fffffff;
-  if (threadIdx.x == 3) *rmax_bits = 0;
+// bb: ordered-int minimum [0..2] and maximum [3..5] of the positions
+__global__ void k_sm_init(int* bb, int* rmax_bits) {
+  if (threadIdx.x < 3) bb[threadIdx.x] = 0x7fffffff;
+  else if (threadIdx.x < 6) bb[threadIdx.x] = (int)0x80000000;
+  if (threadIdx.x == 6) *rmax_bits = 0;
 }
 
-__global__ void k_bbox_lo(int n, const float* __restrict__ x, const float* __restrict__ y,
-                          const float* __restrict__ z, int* lo_ord) {
-  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f};
+__global__ void k_bbox(int n, const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ z,
+                       int* bb) {
+  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    lo[0] = fminf(lo[0], x[i]);
-    lo[1] = fminf(lo[1], y[i]);
-    lo[2] = fminf(lo[2], z[i]);
+    const float v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { lo[d] = fminf(lo[d], v[d]); hi[d] = fmaxf(hi[d], v[d]); }
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    for (int o = 16; o > 0; o >>= 1) lo[d] = fminf(lo[d], __shfl_xor_sync(kFull, lo[d], o));
-    if ((threadIdx.x & 31) == 0) atomicMin(&lo_ord[d], ord(lo[d]));
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(kFull, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(kFull, hi[d], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&bb[d], ord(lo[d]));
+      atomicMax(&bb[3 + d], ord(hi[d]));
+    }
   }
 }
 
-__global__ void k_grid(const int* lo_ord, const int* rmax_bits, GridDev* g) {
+// cell size and origin; a dense start table when the grid has at most `cap` cells
+__global__ void k_grid(const int* bb, const int* rmax_bits, long long cap, GridDev* g) {
   const float rmax = __int_as_float(*rmax_bits);
   double h = 1.0;
   if (rmax > 0.0f && rmax <= 3.0e38f) h = (double)rmax * (1.0 + 1.0 / 1024.0);
+  const double inv_h = 1.0 / h;
+  double ncells = 1.0;
   for (int d = 0; d < 3; ++d) {
-    const float lo = unord(lo_ord[d]);
-    g->lo[d] = (lo >= -3.0e38f && lo <= 3.0e38f) ? (double)lo : 0.0;
+    const float lo = unord(bb[d]), hi = unord(bb[3 + d]);
+    const bool fin = lo >= -3.0e38f && lo <= 3.0e38f && hi >= -3.0e38f && hi <= 3.0e38f && hi >= lo;
+    g->lo[d] = fin ? (double)lo : 0.0;
+    double u = fin ? floor(((double)hi - (double)lo) * inv_h) : (double)kMaxCell;
+    if (!(u >= 0.0)) u = 0.0;
+    if (u > (double)kMaxCell) u = (double)kMaxCell;
+    g->cmax[d] = (int64_t)u;
+    ncells *= u + 1.0;
   }
-  g->inv_h = 1.0 / h;
+  g->inv_h = inv_h;
+  g->dense = ncells <= (double)cap ? 1 : 0;
+  if (!g->dense)
+    for (int d = 0; d < 3; ++d) g->cmax[d] = kMaxCell;
 }
 
 __global__ void k_cell_keys(int n, const float* __restrict__ x, const float* __restrict__ y,
-                            const float* __restrict__ z, const GridDev* __restrict__ gp, uint64_t* keys, int* idx) {
+                            const float* __restrict__ z, const GridDev* __restrict__ gp, uint64_t* keys, int* idx,
+                            int* ccount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const GridDev g = *gp;
   int64_t c[3];
   cell_of(g, x[i], y[i], z[i], c);
-  keys[i] = cell_key(c[0], c[1], c[2]);
+  const uint64_t key = cell_key(g, c[0], c[1], c[2]);
+  keys[i] = key;
   idx[i] = i;
+  if (g.dense) atomicAdd(&ccount[key], 1);
 }
 
 __global__ void k_gather_pos(int n, const int* __restrict__ order, const float* __restrict__ x,
@@ -260,41 +304,229 @@ __global__ void k_split_count(int m, const int* __restrict__ list, const float* 
   if (lane == 0) cnt[k] = c;
 }
 
-__global__ void k_split_fill(int m, const int* __restrict__ list, const float* __restrict__ x,
-                             const float* __restrict__ y, const float* __restrict__ z, const float* __restrict__ r,
-                             float overlap, CellList cl, const GridDev* __restrict__ gp, const int* __restrict__ off,
-                             uint64_t* keys, int* err) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (k >= m) return;
-  const GridDev g = *gp;
-  const int i = list[k];
-  const float qx = x[i], qy = y[i], qz = z[i];
-  const float thr = radius_sq(split_radius(r[i], overlap));
-  const int base = off[k], end = off[k + 1];
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// particle i's own part of the split (Split.h:120-129): position, radius and strength axis
+struct SplitSelf {
+  float x, y, z, r, ax, ay, az;
+};
+
+__device__ __forceinline__ SplitSelf split_self(float xi, float yi, float zi, float ri, float sxi, float syi,
+                                                float szi) {
+  // normalizeVec (MathHelper.h:186-192)
+  const float len = __double2float_rn(__ddiv_rn(1.0, (double)__fsqrt_rn(sumsq3(sxi, syi, szi))));
+  return SplitSelf{xi, yi, zi, ri, __fmul_rn(sxi, len), __fmul_rn(syi, len), __fmul_rn(szi, len)};
+}
+
+// Split.h:146-177: neighbour j's terms (curv x, y, z, dVol) for split particle p; false
+// where the reference skips the neighbour (tStr <= 1e-15 or wgt <= 0)
+__device__ __forceinline__ bool split_term(const SplitSelf& p, float xj, float yj, float zj, float s0, float s1,
+                                           float s2, float rj, float d2, float overlap, float coef, float4& tv) {
+  const float dx0 = __fsub_rn(p.x, xj), dx1 = __fsub_rn(p.y, yj), dx2 = __fsub_rn(p.z, zj);
+  const float factor = __fmul_rn(__fsqrt_rn(__fdiv_rn(d2, __fmul_rn(rj, p.r))), overlap);
+  const double fd = (double)factor;
+  const double cube = __dmul_rn(__dmul_rn(fd, fd), fd);
+  const float fac2 = __double2float_rn(__dmul_rn((double)coef, exp(-cube)));
+  const float tstr = __fsqrt_rn(sumsq3(s0, s1, s2));
+  const float wgt = __fadd_rn(__fadd_rn(__fmul_rn(p.ax, s0), __fmul_rn(p.ay, s1)), __fmul_rn(p.az, s2));
+  if (!((double)tstr > 1.e-15 && wgt > 0.0f)) return false;
+  const float dsx = __fsub_rn(p.ax, __fdiv_rn(s0, tstr));
+  const float dsy = __fsub_rn(p.ay, __fdiv_rn(s1, tstr));
+  const float dsz = __fsub_rn(p.az, __fdiv_rn(s2, tstr));
+  const float thisfac = __fmul_rn(__fmul_rn(wgt, fac2), tstr);
+  tv.x = __fmul_rn(thisfac, __fsub_rn(__fmul_rn(dx1, dsz), __fmul_rn(dx2, dsy)));
+  tv.y = __fmul_rn(thisfac, __fsub_rn(__fmul_rn(dx2, dsx), __fmul_rn(dx0, dsz)));
+  tv.z = __fmul_rn(thisfac, __fsub_rn(__fmul_rn(dx0, dsy), __fmul_rn(dx1, dsx)));
+  tv.w = thisfac;
+  return true;
+}
+
+// codes of a sorted match: its term is precomputed, skipped, or waits for split particle >= 0
+constexpr int kCodeTerm = -1;
+constexpr int kCodeSkip = -2;
+
+constexpr int kFillWarps = 8;
+constexpr int kSortSmem = 256;   // matches of one query sorted in shared memory (more: from global)
+constexpr int kOwn = 8;          // matches a lane ranks per pass (kOwn * 32 = kSortSmem)
+
+struct SplitFillArgs {
+  int m;
+  const int* list;
+  const int* pos_of;
+  const float *x, *y, *z, *r, *sx, *sy, *sz;
+  float overlap, coef;
+  CellList cl;
+  const GridDev* g;
+  const int* off;
+  uint64_t* ukeys;   // matches in discovery order (scratch)
+  uint64_t* keys;    // matches in the reference's order: (d2, index)
+  float4* terms;     // precomputed terms, in that order
+  int* code;         // kCodeTerm, kCodeSkip, or the split rank the term waits for
+  int* dep;          // the split ranks waited for, compacted at the start of each segment
+  int* ndep;         // their number per split particle
+  int* err;
+};
+
+// one warp per split particle: its matches, ranked into (d2, index) order, and every term
+// that does not depend on an earlier split (neighbours that are not split, or split later)
+__global__ void __launch_bounds__(kFillWarps * 32) k_split_fill(SplitFillArgs a) {
+  __shared__ uint64_t sk[kFillWarps][kSortSmem];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kFillWarps + w;
+  if (k >= a.m) return;
+  const GridDev g = *a.g;
+  const int i = a.list[k];
+  const float qx = a.x[i], qy = a.y[i], qz = a.z[i], ri = a.r[i];
+  const float thr = radius_sq(split_radius(ri, a.overlap));
+  const int base = a.off[k], end = a.off[k + 1], c = end - base;
   int run = 0;
-  visit_cells<32>(cl, g, qx, qy, qz, lane, [&](int t, bool in) {
+  visit_cells<32>(a.cl, g, qx, qy, qz, lane, [&](int t, bool in) {
     float d2 = 0.0f;
     bool hit = false;
     if (in) {
-      d2 = nf_dist2(qx, qy, qz, cl.pos[t]);
+      d2 = nf_dist2(qx, qy, qz, a.cl.pos[t]);
       hit = d2 < thr;
     }
     const unsigned b = __ballot_sync(kFull, hit);
     if (hit) {
       const int slot = base + run + __popc(b & ((1u << lane) - 1u));
-      if (slot < end) keys[slot] = match_key(d2, cl.order[t]);
-      else atomicCAS(err, 0, O3G_ERR_STATE);
+      if (slot < end) a.ukeys[slot] = match_key(d2, a.cl.order[t]);
+      else atomicCAS(a.err, 0, O3G_ERR_STATE);
     }
     run += __popc(b);
   });
+  if (run != c) {
+    if (lane == 0) atomicCAS(a.err, 0, O3G_ERR_STATE);
+    return;
+  }
+  __syncwarp();
+  const bool in_smem = c <= kSortSmem;
+  if (in_smem) {
+    for (int q = lane; q < c; q += 32) sk[w][q] = a.ukeys[base + q];
+    __syncwarp();
+  }
+  const SplitSelf p = split_self(qx, qy, qz, ri, a.sx[i], a.sy[i], a.sz[i]);
+  int nd = 0;
+  for (int cb = 0; cb < c; cb += 32 * kOwn) {
+    const int nown = min(kOwn, (c - cb + 31) >> 5);
+    uint64_t own[kOwn];
+    int rk[kOwn];
+#pragma unroll
+    for (int r = 0; r < kOwn; ++r) {
+      const int q = cb + r * 32 + lane;
+      own[r] = (r < nown && q < c) ? (in_smem ? sk[w][q] : a.ukeys[base + q]) : ~0ull;
+      rk[r] = 0;
+    }
+    // keys are distinct (one per neighbour index): rank = number of smaller keys
+    for (int q = 0; q < c; ++q) {
+      const uint64_t v = in_smem ? sk[w][q] : a.ukeys[base + q];
+#pragma unroll
+      for (int r = 0; r < kOwn; ++r)
+        if (r < nown) rk[r] += v < own[r] ? 1 : 0;
+    }
+#pragma unroll
+    for (int r = 0; r < kOwn; ++r) {
+      const int q = cb + r * 32 + lane;
+      const bool mine = r < nown && q < c;
+      const uint64_t kv = own[r];
+      const int j = (int)(uint32_t)kv;
+      const int pj = mine ? a.pos_of[j] : -1;
+      const bool waits = mine && pj >= 0 && j < i;
+      const unsigned wb = __ballot_sync(kFull, waits);
+      if (waits) a.dep[base + nd + __popc(wb & ((1u << lane) - 1u))] = pj;
+      nd += __popc(wb);
+      if (!mine) continue;
+      const int dst = base + rk[r];
+      a.keys[dst] = kv;
+      if (waits) {
+        a.code[dst] = pj;
+      } else {
+        float4 tv = make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool ok = split_term(p, a.x[j], a.y[j], a.z[j], a.sx[j], a.sy[j], a.sz[j], a.r[j],
+                                   __uint_as_float((uint32_t)(kv >> 32)), a.overlap, a.coef, tv);
+        a.code[dst] = ok ? kCodeTerm : kCodeSkip;
+        a.terms[dst] = tv;
+      }
+    }
+  }
+  if (lane == 0) a.ndep[k] = nd;
+}
+
+// level of every split particle in the dependency graph: 0 without dependencies, else one
+// more than the deepest particle it waits for.  One thread per particle, claimed 32 at a
+// time in index order (dependencies always have lower ranks); a particle publishes level + 1
+// with a release store, read with acquire loads by the particles that wait for it.
+struct LevelArgs {
+  int m;
+  const int* off;
+  const int* dep;
+  const int* ndep;
+  int* lvl1;     // level + 1, 0 until published
+  int* claim;
+  int* err;
+  int spread;    // 1: every particle has its own resident thread (no claiming)
+};
+
+__global__ void k_split_levels(LevelArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int round = 0;; ++round) {
+    int k;
+    if (a.spread) {
+      // consecutive ranks (often dependent on each other) land in different warps
+      if (round > 0) break;
+      k = lane * nwarps + gw;
+    } else {
+      int k0 = 0;
+      if (lane == 0) k0 = atomicAdd(a.claim, 32);
+      k0 = __shfl_sync(kFull, k0, 0);
+      if (k0 >= a.m) break;
+      k = k0 + lane;
+    }
+    if (k < a.m) {
+      const int b = a.off[k], nd = a.ndep[k];
+      int lv = 0;
+      for (int q = 0; q < nd; ++q) {
+        const int pj = a.dep[b + q];
+        const uint64_t t0 = global_ns();
+        int v = 0;
+        for (uint32_t it = 0; it < kReadySpin; ++it) {
+          asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(a.lvl1 + pj) : "memory");
+          if (v) break;
+          if ((it & 1023u) == 1023u && (*(volatile int*)a.err || global_ns() - t0 > kReadyNs)) break;
+          __nanosleep(kPollNs);
+        }
+        if (!v) {
+          atomicCAS(a.err, 0, O3G_ERR_TIMEOUT);
+          break;
+        }
+        lv = max(lv, v);
+      }
+      asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a.lvl1 + k), "r"(lv + 1) : "memory");
+    }
+  }
+}
+
+__global__ void k_level_keys(int m, const int* __restrict__ lvl1, uint32_t* key, int* val) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  key[k] = (uint32_t)lvl1[k];
+  val[k] = k;
 }
 
 struct SplitArgs {
   int m;
+  const int* order;             // split ranks by level: every dependency comes earlier
   const int* list;
-  const int* pos_of;
   const int* off;
   const uint64_t* keys;         // sorted matches per split particle
+  const float4* terms;          // their precomputed terms
+  const int* code;
   const float *x, *y, *z, *r, *elong, *sx, *sy, *sz;   // state before the operator
   float overlap;
   float coef;                   // get_core_coefficient<float>
@@ -307,12 +539,6 @@ struct SplitArgs {
   int* err;
 };
 
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
 // waits for a ready flag; gives up (setting the error word) after kReadyNs of wall time or
 // kReadySpin polls, or at once when another wait already gave up
 __device__ __forceinline__ bool wait_ready(const int* flag, int* err) {
@@ -321,85 +547,90 @@ __device__ __forceinline__ bool wait_ready(const int* flag, int* err) {
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
     if (v) return true;
-    if ((it & 255u) == 255u) {
+    if ((it & 1023u) == 1023u) {
       if (*(volatile int*)err) return false;
       if (global_ns() - t0 > kReadyNs) break;
     }
-    __nanosleep(64);
+    __nanosleep(kPollNs);
   }
   atomicCAS(err, 0, O3G_ERR_TIMEOUT);
   return false;
 }
 
 constexpr int kChainWarps = 4;
+constexpr int kPre = 4;   // rounds of 32 matches whose codes and terms are loaded together
 
-// Split.h:116-243 for every elongated particle, in the dependency order described above
+// Split.h:116-243 for every elongated particle, in the dependency order described above:
+// the precomputed terms are read, the ones that wait for an earlier split are computed from
+// its published state, and the sums are added in the sorted order
 __global__ void __launch_bounds__(kChainWarps * 32) k_split_chain(SplitArgs a) {
   __shared__ float4 term[kChainWarps][32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
-    int k = 0;
-    if (lane == 0) k = atomicAdd(a.claim, 1);
-    k = __shfl_sync(kFull, k, 0);
-    if (k >= a.m) break;
+    int c = 0;
+    if (lane == 0) c = atomicAdd(a.claim, 1);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= a.m) break;
+    const int k = a.order[c];
     const int i = a.list[k];
     const float xi = a.x[i], yi = a.y[i], zi = a.z[i], ri = a.r[i], ei = a.elong[i];
     const float sxi = a.sx[i], syi = a.sy[i], szi = a.sz[i];
-    // normalizeVec (MathHelper.h:186-192)
-    const float len = __double2float_rn(__ddiv_rn(1.0, (double)__fsqrt_rn(sumsq3(sxi, syi, szi))));
-    const float ax = __fmul_rn(sxi, len), ay = __fmul_rn(syi, len), az = __fmul_rn(szi, len);
+    const SplitSelf p = split_self(xi, yi, zi, ri, sxi, syi, szi);
     float acc = 0.0f;   // lane 0..2: curv[lane], lane 3: dVol
     const int b = a.off[k], e = a.off[k + 1];
-    for (int base = b; base < e; base += 32) {
-      const int t = base + lane;
-      bool valid = false;
-      float4 tv = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (t < e) {
-        const uint64_t kv = a.keys[t];
-        const int j = (int)(uint32_t)kv;
-        const float d2 = __uint_as_float((uint32_t)(kv >> 32));
-        float xj, yj, zj, s0, s1, s2;
-        const int pj = a.pos_of[j];
-        if (pj >= 0 && j < i) {
-          wait_ready(&a.ready[pj], a.err);
-          const float4 px = __ldcg(&a.post_x[pj]);
-          const float4 ps = __ldcg(&a.post_s[pj]);
-          xj = px.x; yj = px.y; zj = px.z;
-          s0 = ps.x; s1 = ps.y; s2 = ps.z;
-        } else {
-          xj = a.x[j]; yj = a.y[j]; zj = a.z[j];
-          s0 = a.sx[j]; s1 = a.sy[j]; s2 = a.sz[j];
-        }
-        const float rj = a.r[j];
-        const float dx0 = __fsub_rn(xi, xj), dx1 = __fsub_rn(yi, yj), dx2 = __fsub_rn(zi, zj);
-        const float factor = __fmul_rn(__fsqrt_rn(__fdiv_rn(d2, __fmul_rn(rj, ri))), a.overlap);
-        const double fd = (double)factor;
-        const double cube = __dmul_rn(__dmul_rn(fd, fd), fd);
-        const float fac2 = __double2float_rn(__dmul_rn((double)a.coef, exp(-cube)));
-        const float tstr = __fsqrt_rn(sumsq3(s0, s1, s2));
-        const float wgt = __fadd_rn(__fadd_rn(__fmul_rn(ax, s0), __fmul_rn(ay, s1)), __fmul_rn(az, s2));
-        if ((double)tstr > 1.e-15 && wgt > 0.0f) {
-          valid = true;
-          const float dsx = __fsub_rn(ax, __fdiv_rn(s0, tstr));
-          const float dsy = __fsub_rn(ay, __fdiv_rn(s1, tstr));
-          const float dsz = __fsub_rn(az, __fdiv_rn(s2, tstr));
-          const float thisfac = __fmul_rn(__fmul_rn(wgt, fac2), tstr);
-          tv.x = __fmul_rn(thisfac, __fsub_rn(__fmul_rn(dx1, dsz), __fmul_rn(dx2, dsy)));
-          tv.y = __fmul_rn(thisfac, __fsub_rn(__fmul_rn(dx2, dsx), __fmul_rn(dx0, dsz)));
-          tv.z = __fmul_rn(thisfac, __fsub_rn(__fmul_rn(dx0, dsy), __fmul_rn(dx1, dsx)));
-          tv.w = thisfac;
-        }
+    for (int cb = b; cb < e; cb += 32 * kPre) {
+      int cd[kPre];
+      float4 tv[kPre];
+      uint64_t kv[kPre];
+#pragma unroll
+      for (int r = 0; r < kPre; ++r) {
+        const int t = cb + r * 32 + lane;
+        cd[r] = t < e ? a.code[t] : kCodeSkip;
+        tv[r] = t < e ? a.terms[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        kv[r] = t < e ? a.keys[t] : 0ull;
       }
-      term[w][lane] = tv;
-      const unsigned vm = __ballot_sync(kFull, valid);
-      __syncwarp();
-      if (lane < 4) {
-        const float* tp = reinterpret_cast<const float*>(&term[w][0]) + lane;
-        const int cnt = min(32, e - base);
-        for (int q = 0; q < cnt; ++q)
-          if ((vm >> q) & 1u) acc = __fadd_rn(acc, tp[4 * q]);
+      // terms that wait for an earlier split: radii first (never change), then every wait,
+      // then all the published states at once
+      float rj[kPre];
+#pragma unroll
+      for (int r = 0; r < kPre; ++r) rj[r] = cd[r] >= 0 ? a.r[(int)(uint32_t)kv[r]] : 0.0f;
+#pragma unroll
+      for (int r = 0; r < kPre; ++r)
+        if (cd[r] >= 0) wait_ready(&a.ready[cd[r]], a.err);
+      float4 px[kPre], ps[kPre];
+#pragma unroll
+      for (int r = 0; r < kPre; ++r)
+        if (cd[r] >= 0) {
+          px[r] = __ldcg(&a.post_x[cd[r]]);
+          ps[r] = __ldcg(&a.post_s[cd[r]]);
+        }
+#pragma unroll
+      for (int r = 0; r < kPre; ++r)
+        if (cd[r] >= 0) {
+          tv[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+          const bool ok = split_term(p, px[r].x, px[r].y, px[r].z, ps[r].x, ps[r].y, ps[r].z, rj[r],
+                                     __uint_as_float((uint32_t)(kv[r] >> 32)), a.overlap, a.coef, tv[r]);
+          cd[r] = ok ? kCodeTerm : kCodeSkip;
+        }
+#pragma unroll
+      for (int r = 0; r < kPre; ++r) {
+        const int rb = cb + r * 32;
+        if (rb >= e) break;
+        term[w][lane] = tv[r];
+        const unsigned vm = __ballot_sync(kFull, cd[r] == kCodeTerm);
+        __syncwarp();
+        if (lane < 4) {
+          // the 32 values are read first, then added in order (vm is zero past the end)
+          const float* tp = reinterpret_cast<const float*>(&term[w][0]) + lane;
+          float v[32];
+#pragma unroll
+          for (int q = 0; q < 32; ++q) v[q] = tp[4 * q];
+#pragma unroll
+          for (int q = 0; q < 32; ++q)
+            if ((vm >> q) & 1u) acc = __fadd_rn(acc, v[q]);
+        }
+        __syncwarp();
       }
-      __syncwarp();
     }
     float curv0 = __shfl_sync(kFull, acc, 0), curv1 = __shfl_sync(kFull, acc, 1);
     float curv2 = __shfl_sync(kFull, acc, 2);
@@ -426,12 +657,12 @@ __global__ void __launch_bounds__(kChainWarps * 32) k_split_chain(SplitArgs a) {
         csx = __fadd_rn(csx, dsx); csy = __fadd_rn(csy, dsy); csz = __fadd_rn(csz, dsz);
         psx = __fsub_rn(psx, dsx); psy = __fsub_rn(psy, dsy); psz = __fsub_rn(psz, dsz);
       }
-      const float mx = __fmul_rn(halfd, ax), my = __fmul_rn(halfd, ay), mz = __fmul_rn(halfd, az);
+      const float mx = __fmul_rn(halfd, p.ax), my = __fmul_rn(halfd, p.ay), mz = __fmul_rn(halfd, p.az);
       a.child_x[k] = make_float4(__fsub_rn(xi, mx), __fsub_rn(yi, my), __fsub_rn(zi, mz), 0.0f);
       a.child_s[k] = make_float4(csx, csy, csz, 0.0f);
       a.post_x[k] = make_float4(__fadd_rn(xi, mx), __fadd_rn(yi, my), __fadd_rn(zi, mz), he);
       a.post_s[k] = make_float4(psx, psy, psz, 0.0f);
-      __threadfence();
+      // the release store orders the four writes above before the flag
       asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(&a.ready[k]), "r"(1) : "memory");
     }
     __syncwarp();
@@ -476,7 +707,7 @@ constexpr int kMeanChunk = 4096;
 // meanstr = (sum in index order of the terms) / (float)n, the reference's float loop;
 // warps 1.. stage chunk c+1 in shared memory while thread 0 adds chunk c
 __global__ void __launch_bounds__(kMeanThreads) k_meanstr(int n, const float* __restrict__ term, float* out) {
-  __shared__ float buf[2][kMeanChunk];
+  __shared__ __align__(16) float buf[2][kMeanChunk];
   const int nch = (n + kMeanChunk - 1) / kMeanChunk;
   const int loaders = kMeanThreads - 32, lt = threadIdx.x - 32;
   if (threadIdx.x >= 32)
@@ -491,7 +722,25 @@ __global__ void __launch_bounds__(kMeanThreads) k_meanstr(int n, const float* __
     if (threadIdx.x == 0) {
       const int cnt = min(kMeanChunk, n - c * kMeanChunk);
       const float* p = buf[c & 1];
-      for (int q = 0; q < cnt; ++q) s = __fadd_rn(s, p[q]);
+      // the next 8 terms are read while the current 8 are added
+      int q = 0;
+      float4 v0, v1;
+      if (cnt >= 8) {
+        v0 = *reinterpret_cast<const float4*>(p);
+        v1 = *reinterpret_cast<const float4*>(p + 4);
+      }
+      for (; q + 8 <= cnt; q += 8) {
+        float4 n0 = v0, n1 = v1;
+        if (q + 16 <= cnt) {
+          n0 = *reinterpret_cast<const float4*>(p + q + 8);
+          n1 = *reinterpret_cast<const float4*>(p + q + 12);
+        }
+        s = __fadd_rn(s, v0.x); s = __fadd_rn(s, v0.y); s = __fadd_rn(s, v0.z); s = __fadd_rn(s, v0.w);
+        s = __fadd_rn(s, v1.x); s = __fadd_rn(s, v1.y); s = __fadd_rn(s, v1.z); s = __fadd_rn(s, v1.w);
+        v0 = n0;
+        v1 = n1;
+      }
+      for (; q < cnt; ++q) s = __fadd_rn(s, p[q]);
     }
     __syncthreads();
   }
@@ -721,21 +970,27 @@ int32_t read_int(const int* dev, int* host, cudaStream_t st) {
 
 // the cell list over n positions; lo_ord / rmax_bits already hold the bbox minimum and
 // the largest search radius
-int32_t build_cells(Scratch& sc, int n, const float* x, const float* y, const float* z, const int* lo_ord,
+int32_t build_cells(Scratch& sc, int n, const float* x, const float* y, const float* z, const int* bb,
                     const int* rmax_bits, CellList* cl, GridDev** grid) {
   cudaStream_t st = sc.st;
   GridDev* g = nullptr;
   uint64_t *kin = nullptr, *kout = nullptr;
-  int *iin = nullptr, *iout = nullptr;
+  int *iin = nullptr, *iout = nullptr, *ccount = nullptr, *cstart = nullptr;
   float4* pos = nullptr;
+  // a dense start table for up to 16 cells per particle (at least 2^20, at most 2^28)
+  const long long cap = std::min<long long>(std::max<long long>(16ll * n, 1ll << 20), 1ll << 28);
   O3G_TRY(sc.get(&g, 1));
   O3G_TRY(sc.get(&kin, n));
   O3G_TRY(sc.get(&kout, n));
   O3G_TRY(sc.get(&iin, n));
   O3G_TRY(sc.get(&iout, n));
   O3G_TRY(sc.get(&pos, n));
-  k_grid<<<1, 1, 0, st>>>(lo_ord, rmax_bits, g);
-  k_cell_keys<<<blocks(n), 256, 0, st>>>(n, x, y, z, g, kin, iin);
+  O3G_TRY(sc.get(&ccount, (size_t)cap + 1));
+  O3G_TRY(sc.get(&cstart, (size_t)cap + 1));
+  O3G_CUDA_TRY(cudaMemsetAsync(ccount, 0, ((size_t)cap + 1) * sizeof(int), st));
+  k_grid<<<1, 1, 0, st>>>(bb, rmax_bits, cap, g);
+  k_cell_keys<<<blocks(n), 256, 0, st>>>(n, x, y, z, g, kin, iin, ccount);
+  O3G_TRY(exclusive_sum(sc, ccount, cstart, (int)(cap + 1)));
   size_t tb = 0;
   O3G_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, kin, kout, iin, iout, n, 0, 63, st));
   void* tmp = nullptr;
@@ -747,6 +1002,7 @@ int32_t build_cells(Scratch& sc, int n, const float* x, const float* y, const fl
   cl->keys = kout;
   cl->order = iout;
   cl->pos = pos;
+  cl->cstart = cstart;
   cl->n = n;
   *grid = g;
   return O3G_OK;
@@ -778,12 +1034,12 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
                   float* sz, int core, float overlap, float threshold, int* nsplit, cudaStream_t st) {
   Scratch sc(st);
   int *lo_ord = nullptr, *rmax = nullptr, *flag = nullptr, *rank = nullptr, *err = nullptr;
-  O3G_TRY(sc.get(&lo_ord, 4));
+  O3G_TRY(sc.get(&lo_ord, 6));
   O3G_TRY(sc.get(&rmax, 1));
-  O3G_TRY(sc.get(&err, 2));
+  O3G_TRY(sc.get(&err, 3));   // error word, chain claim counter, level claim counter
   O3G_TRY(sc.get(&flag, (size_t)n + 1));
   O3G_TRY(sc.get(&rank, (size_t)n + 1));
-  O3G_CUDA_TRY(cudaMemsetAsync(err, 0, 2 * sizeof(int), st));
+  O3G_CUDA_TRY(cudaMemsetAsync(err, 0, 3 * sizeof(int), st));
   k_sm_init<<<1, 32, 0, st>>>(lo_ord, rmax);
   k_split_flag<<<blocks(n), 256, 0, st>>>(n, elong, r, overlap, threshold, flag, rmax);
   O3G_CUDA_TRY(cudaMemsetAsync(flag + n, 0, sizeof(int), st));
@@ -804,7 +1060,7 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   O3G_TRY(sc.get(&off, (size_t)m + 1));
   O3G_TRY(sc.get(&ready, m));
   k_scatter_flagged<<<blocks(n), 256, 0, st>>>(n, flag, rank, list, pos_of);
-  k_bbox_lo<<<std::min(blocks(n), 1024), 256, 0, st>>>(n, x, y, z, lo_ord);
+  k_bbox<<<std::min(blocks(n), 1024), 256, 0, st>>>(n, x, y, z, lo_ord);
   note_launch(2);
   CellList cl{};
   GridDev* g = nullptr;
@@ -815,11 +1071,61 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   O3G_TRY(exclusive_sum(sc, cnt, off, m + 1));
   int total = 0;
   O3G_TRY(read_int(off + m, &total, st));
-  uint64_t *keys = nullptr, *sorted = nullptr;
+  uint64_t *ukeys = nullptr, *keys = nullptr;
+  float4* terms = nullptr;
+  int *code = nullptr, *dep = nullptr, *ndep = nullptr;
+  O3G_TRY(sc.get(&ukeys, total));
   O3G_TRY(sc.get(&keys, total));
-  k_split_fill<<<blocks((long long)m * 32), 256, 0, st>>>(m, list, x, y, z, r, overlap, cl, g, off, keys, err);
+  O3G_TRY(sc.get(&terms, total));
+  O3G_TRY(sc.get(&code, total));
+  O3G_TRY(sc.get(&dep, total));
+  O3G_TRY(sc.get(&ndep, m));
+  const double pi = 3.14159265358979323846;
+  // get_core_coefficient<float> (Core.h:32-35): gaussian 1/(pi sqrt(pi)) in double, else 0.23873241
+  const float coef = core == O3G_DIFFCORE_GAUSSIAN ? (float)(1.0 / (pi * std::sqrt(pi))) : (float)0.23873241;
+  SplitFillArgs fa;
+  fa.m = m; fa.list = list; fa.pos_of = pos_of;
+  fa.x = x; fa.y = y; fa.z = z; fa.r = r; fa.sx = sx; fa.sy = sy; fa.sz = sz;
+  fa.overlap = overlap; fa.coef = coef; fa.cl = cl; fa.g = g; fa.off = off;
+  fa.ukeys = ukeys; fa.keys = keys; fa.terms = terms; fa.code = code; fa.dep = dep; fa.ndep = ndep;
+  fa.err = err;
+  k_split_fill<<<(m + kFillWarps - 1) / kFillWarps, kFillWarps * 32, 0, st>>>(fa);
   note_launch(1);
-  O3G_TRY(sort_matches(sc, keys, &sorted, total, m, off));
+
+  // levels, and the split ranks sorted by level: the chain's claim order
+  DeviceFacts f;
+  O3G_TRY(device_facts(&f));
+  int *lvl1 = nullptr, *kin = nullptr, *order = nullptr;
+  uint32_t *lkey = nullptr, *lkey2 = nullptr;
+  O3G_TRY(sc.get(&lvl1, m));
+  O3G_TRY(sc.get(&kin, m));
+  O3G_TRY(sc.get(&order, m));
+  O3G_TRY(sc.get(&lkey, m));
+  O3G_TRY(sc.get(&lkey2, m));
+  O3G_CUDA_TRY(cudaMemsetAsync(lvl1, 0, (size_t)m * sizeof(int), st));
+  {
+    int lb = 0;
+    O3G_TRY(occupancy_blocks((const void*)k_split_levels, 256, &lb));
+    int lgrid = std::max(1, lb) * f.num_sms;
+    lgrid = std::min(lgrid, (m + 255) / 256);
+    // with a thread for every particle all of them are in flight at once, so any mapping is
+    // deadlock-free; otherwise they are claimed in rank order
+    const int spread = (long long)lgrid * 256 >= (long long)m ? 1 : 0;
+    LevelArgs la{m, off, dep, ndep, lvl1, err + 2, err, spread};
+    void* largs[] = {&la};
+    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_split_levels, dim3(lgrid), dim3(256), largs, 0, st));
+  }
+  k_level_keys<<<blocks(m), 256, 0, st>>>(m, lvl1, lkey, kin);
+  note_launch(2);
+  {
+    int lbits = 1;
+    while (lbits < 31 && (1ll << lbits) <= (long long)m + 1) ++lbits;
+    size_t tb = 0;
+    O3G_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, lkey, lkey2, kin, order, m, 0, lbits, st));
+    void* tmp = nullptr;
+    O3G_TRY(sc.get((char**)&tmp, tb));
+    O3G_CUDA_TRY(cub::DeviceRadixSort::SortPairs(tmp, tb, lkey, lkey2, kin, order, m, 0, lbits, st));
+  }
 
   float4 *post_x = nullptr, *post_s = nullptr, *child_x = nullptr, *child_s = nullptr;
   O3G_TRY(sc.get(&post_x, m));
@@ -828,18 +1134,14 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   O3G_TRY(sc.get(&child_s, m));
   O3G_CUDA_TRY(cudaMemsetAsync(ready, 0, (size_t)m * sizeof(int), st));
   SplitArgs a;
-  a.m = m; a.list = list; a.pos_of = pos_of; a.off = off; a.keys = sorted;
+  a.m = m; a.order = order; a.list = list; a.off = off; a.keys = keys; a.terms = terms; a.code = code;
   a.x = x; a.y = y; a.z = z; a.r = r; a.elong = elong; a.sx = sx; a.sy = sy; a.sz = sz;
   a.overlap = overlap;
-  // get_core_coefficient<float> (Core.h:32-35): gaussian 1/(pi sqrt(pi)) in double, else 0.23873241
-  const double pi = 3.14159265358979323846;
-  a.coef = core == O3G_DIFFCORE_GAUSSIAN ? (float)(1.0 / (pi * std::sqrt(pi))) : (float)0.23873241;
+  a.coef = coef;
   a.post_x = post_x; a.post_s = post_s; a.child_x = child_x; a.child_s = child_s;
   a.ready = ready; a.claim = err + 1; a.err = err;
   int nb = 0;
   O3G_TRY(occupancy_blocks((const void*)k_split_chain, kChainWarps * 32, &nb));
-  DeviceFacts f;
-  O3G_TRY(device_facts(&f));
   int grid = std::max(1, nb) * f.num_sms;
   grid = std::min(grid, (m + kChainWarps - 1) / kChainWarps);
   void* args[] = {&a};
@@ -852,12 +1154,40 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   return check_err(err, st, "o3g_split_elongated: a device-side check failed (ready-flag wait or match count)");
 }
 
+// a second stream per device for the mean-strength sum, which overlaps the neighbour search
+int32_t side_stream(cudaStream_t* out) {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  O3G_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("o3g_merge_close_particles: device index out of range");
+    return O3G_ERR_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!streams[dev]) O3G_CUDA_TRY(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
+  *out = streams[dev];
+  return O3G_OK;
+}
+
+// joins the side stream back into the caller's stream before the scratch it reads is freed
+struct Join {
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  ~Join() {
+    if (done) {
+      cudaStreamWaitEvent(st, done, 0);
+      cudaEventDestroy(done);
+    }
+  }
+};
+
 int32_t merge_run(int n, float* x, float* y, float* z, float* sx, float* sy, float* sz, float* r, float overlap,
                   float threshold, int adapt, int* nremoved, cudaStream_t st) {
   Scratch sc(st);
   int *lo_ord = nullptr, *rmax = nullptr, *err = nullptr, *cnt = nullptr, *off = nullptr;
   float *term = nullptr, *meanstr = nullptr;
-  O3G_TRY(sc.get(&lo_ord, 4));
+  O3G_TRY(sc.get(&lo_ord, 6));
   O3G_TRY(sc.get(&rmax, 1));
   O3G_TRY(sc.get(&err, 1));
   O3G_TRY(sc.get(&term, n));
@@ -867,8 +1197,24 @@ int32_t merge_run(int n, float* x, float* y, float* z, float* sx, float* sy, flo
   O3G_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
   k_sm_init<<<1, 32, 0, st>>>(lo_ord, rmax);
   k_merge_prep<<<blocks(n), 256, 0, st>>>(n, sx, sy, sz, r, overlap, term, rmax);
-  k_meanstr<<<1, kMeanThreads, 0, st>>>(n, term, meanstr);
-  k_bbox_lo<<<std::min(blocks(n), 1024), 256, 0, st>>>(n, x, y, z, lo_ord);
+  // the sequential sum runs on the side stream from here until k_merge_resolve needs it
+  cudaStream_t side = nullptr;
+  O3G_TRY(side_stream(&side));
+  Join join;
+  cudaEvent_t prepped = nullptr;
+  O3G_CUDA_TRY(cudaEventCreateWithFlags(&prepped, cudaEventDisableTiming));
+  cudaError_t ev = cudaEventRecord(prepped, st);
+  if (ev == cudaSuccess) ev = cudaStreamWaitEvent(side, prepped, 0);
+  cudaEventDestroy(prepped);
+  if (ev != cudaSuccess) {
+    set_error_cuda("o3g_merge_close_particles: stream fork", ev);
+    return O3G_ERR_CUDA;
+  }
+  k_meanstr<<<1, kMeanThreads, 0, side>>>(n, term, meanstr);
+  join.st = st;
+  O3G_CUDA_TRY(cudaEventCreateWithFlags(&join.done, cudaEventDisableTiming));
+  O3G_CUDA_TRY(cudaEventRecord(join.done, side));
+  k_bbox<<<std::min(blocks(n), 1024), 256, 0, st>>>(n, x, y, z, lo_ord);
   note_launch(4);
   CellList cl{};
   GridDev* g = nullptr;
@@ -932,6 +1278,7 @@ int32_t merge_run(int n, float* x, float* y, float* z, float* sx, float* sy, flo
   a.x = x; a.y = y; a.z = z; a.sx = sx; a.sy = sy; a.sz = sz; a.r = r;
   a.erase = erase; a.meanstr = meanstr; a.overlap = overlap; a.threshold = threshold; a.adapt = adapt;
   if (ng > 0) {
+    O3G_CUDA_TRY(cudaStreamWaitEvent(st, join.done, 0));
     k_merge_resolve<<<blocks(ng, 128), 128, 0, st>>>(a);
     note_launch(1);
   }
