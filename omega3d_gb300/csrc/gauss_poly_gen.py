@@ -26,7 +26,9 @@ from scipy.special import erf
 
 EDGES = [0.0, 1.0, 4.0, 9.0, 16.0, 25.0, 36.0, 48.0]
 DEG = 9
-STRIDE = 2 + 2 * (DEG + 1) + 1      # s, o, G coefficients, D coefficients, pad (odd stride)
+# one interval's row, read as 6 float4: s, o, then (G_k, D_k) from k = DEG down to 0 (the
+# order Horner's rule consumes them), then two pad entries
+STRIDE = 2 + 2 * (DEG + 1) + 2
 CONST = np.sqrt(2.0 / np.pi)
 
 
@@ -79,6 +81,7 @@ def fit():
         q = np.linspace(lo, hi, 40001)
         t = q * s + o
         row = [s, o]
+        polys = []
         for F in (gauss_G, gauss_D):
             y = F(q)
             p = C.cheb2poly(C.chebfit(t, y, DEG))
@@ -90,8 +93,10 @@ def fit():
             tt = (qq.astype(np.float32).astype(np.float64) * np.float64(np.float32(s)) +
                   np.float64(np.float32(o))).astype(np.float32)
             worst = max(worst, float(np.max(np.abs(_horner_f32(p, tt) - yy) / np.abs(yy))))
-            row += list(p)
-        row.append(0.0)
+            polys.append(p)
+        for k in range(DEG, -1, -1):
+            row += [polys[0][k], polys[1][k]]
+        row += [0.0, 0.0]
         table.append(row)
     return table, worst
 
@@ -112,8 +117,8 @@ def write(table, worst, path):
 namespace o3g {{
 
 constexpr int kGaussPolyDeg = {DEG};
-constexpr int kGaussPolyStride = {STRIDE};   // s, o, G[0..{DEG}], D[0..{DEG}], pad
-__device__ const float kGaussPoly[{len(table)} * {STRIDE}] = {{
+constexpr int kGaussPolyStride = {STRIDE};   // s, o, (G[k], D[k]) for k = {DEG}..0, pad, pad
+__device__ const __align__(16) float kGaussPoly[{len(table)} * {STRIDE}] = {{
 {body}
 }};
 

@@ -142,31 +142,39 @@ __device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 
 // G(q) and D(q) = 2 G'(q) of the Gaussian core for q in [0, qfar] in FP32, from the
-// piecewise polynomials of o3g_gauss_poly.h (interval j = number of edges 1, 4, ..., 36 at
-// or below q; Horner's rule in t = q s_j + o_j): branch-free, no erf/exp/division
+// piecewise polynomials of o3g_gauss_poly.h (Horner's rule in t = q s_j + o_j): branch-free,
+// no erf/exp/division.
+//
+// Interval of q: j covers [j^2, (j+1)^2) for j < 6 and [36, 48] for j = 6, so j = floor(sqrt q)
+// capped at 6.  With the hardware reciprocal square root, q within about 1e-7 (relative) of
+// an edge may land in the neighbouring interval, whose polynomial is still fitted there
+// (the fits are checked 1e-4 of their width beyond both ends).
+__device__ __forceinline__ int gauss_interval(float q) {
+  const float qq = fmaxf(q, 1.0e-30f);
+  return min((int)(qq * rsqrtf(qq)), 6);
+}
+
+// G(q) and D(q) by Horner's rule in t; the row holds (s, o), then (G_k, D_k) for k = 9..0 in
+// the order used.  Scalar loads: vector loads of the row made the compiler keep all of it
+// live, which cost the pair kernel a fifth of its occupancy.
 __device__ __forceinline__ void gauss_poly(float q, float& G, float& D) {
-  const int j = (q >= 1.f) + (q >= 4.f) + (q >= 9.f) + (q >= 16.f) + (q >= 25.f) + (q >= 36.f);
-  const float* c = kGaussPoly + j * kGaussPolyStride;
+  const float* c = kGaussPoly + gauss_interval(q) * kGaussPolyStride;
   const float t = fmaf(q, __ldg(c), __ldg(c + 1));
-  const float* cg = c + 2;
-  const float* cd = cg + (kGaussPolyDeg + 1);
-  float g = __ldg(cg + kGaussPolyDeg), d = __ldg(cd + kGaussPolyDeg);
+  float g = __ldg(c + 2), d = __ldg(c + 3);
 #pragma unroll
-  for (int k = kGaussPolyDeg - 1; k >= 0; --k) {
-    g = fmaf(g, t, __ldg(cg + k));
-    d = fmaf(d, t, __ldg(cd + k));
+  for (int k = 1; k <= kGaussPolyDeg; ++k) {
+    g = fmaf(g, t, __ldg(c + 2 + 2 * k));
+    d = fmaf(d, t, __ldg(c + 3 + 2 * k));
   }
   G = g;
   D = d;
 }
 __device__ __forceinline__ float gauss_poly_g(float q) {
-  const int j = (q >= 1.f) + (q >= 4.f) + (q >= 9.f) + (q >= 16.f) + (q >= 25.f) + (q >= 36.f);
-  const float* c = kGaussPoly + j * kGaussPolyStride;
+  const float* c = kGaussPoly + gauss_interval(q) * kGaussPolyStride;
   const float t = fmaf(q, __ldg(c), __ldg(c + 1));
-  const float* cg = c + 2;
-  float g = __ldg(cg + kGaussPolyDeg);
+  float g = __ldg(c + 2);
 #pragma unroll
-  for (int k = kGaussPolyDeg - 1; k >= 0; --k) g = fmaf(g, t, __ldg(cg + k));
+  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, __ldg(c + 2 + 2 * k));
   return g;
 }
 
