@@ -24,11 +24,13 @@ import numpy as np
 from numpy.polynomial import chebyshev as C
 from scipy.special import erf
 
-EDGES = [0.0, 1.0, 4.0, 9.0, 16.0, 25.0, 36.0, 48.0]
-DEG = 9
-# one interval's row, read as 6 float4: s, o, then (G_k, D_k) from k = DEG down to 0 (the
-# order Horner's rule consumes them), then two pad entries
-STRIDE = 2 + 2 * (DEG + 1) + 2
+# interval j = [(j/2)^2, ((j+1)/2)^2) for j < 13 and [42.25, 48] for j = 13, so that the
+# kernels find j as floor(2 sqrt q) capped at 13
+EDGES = [(j / 2.0) ** 2 for j in range(14)] + [48.0]
+DEG = 6
+# one interval's row: s, o, then (G_k, D_k) from k = DEG down to 0 (the order Horner's rule
+# consumes them)
+STRIDE = 2 + 2 * (DEG + 1)
 CONST = np.sqrt(2.0 / np.pi)
 
 
@@ -96,7 +98,7 @@ def fit():
             polys.append(p)
         for k in range(DEG, -1, -1):
             row += [polys[0][k], polys[1][k]]
-        row += [0.0, 0.0]
+        row += [0.0] * (STRIDE - len(row))
         table.append(row)
     return table, worst
 
@@ -117,7 +119,8 @@ def write(table, worst, path):
 namespace o3g {{
 
 constexpr int kGaussPolyDeg = {DEG};
-constexpr int kGaussPolyStride = {STRIDE};   // s, o, (G[k], D[k]) for k = {DEG}..0, pad, pad
+constexpr int kGaussPolyStride = {STRIDE};   // s, o, (G[k], D[k]) for k = {DEG}..0
+constexpr int kGaussPolyLast = {len(table) - 1};       // interval j covers [(j/2)^2, ((j+1)/2)^2)
 __device__ const __align__(16) float kGaussPoly[{len(table)} * {STRIDE}] = {{
 {body}
 }};

@@ -145,13 +145,13 @@ __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 // piecewise polynomials of o3g_gauss_poly.h (Horner's rule in t = q s_j + o_j): branch-free,
 // no erf/exp/division.
 //
-// Interval of q: j covers [j^2, (j+1)^2) for j < 6 and [36, 48] for j = 6, so j = floor(sqrt q)
-// capped at 6.  With the hardware reciprocal square root, q within about 1e-7 (relative) of
-// an edge may land in the neighbouring interval, whose polynomial is still fitted there
-// (the fits are checked 1e-4 of their width beyond both ends).
+// Interval of q: j covers [(j/2)^2, ((j+1)/2)^2) up to [42.25, 48], so j = floor(2 sqrt q)
+// capped at the last.  With the hardware reciprocal square root, q within about 1e-7
+// (relative) of an edge may land in the neighbouring interval, whose polynomial is still
+// fitted there (the fits are checked 1e-4 of their width beyond both ends).
 __device__ __forceinline__ int gauss_interval(float q) {
   const float qq = fmaxf(q, 1.0e-30f);
-  return min((int)(qq * rsqrtf(qq)), 6);
+  return min((int)(2.0f * qq * rsqrtf(qq)), kGaussPolyLast);
 }
 
 // G(q) and D(q) by Horner's rule in t; the row holds (s, o), then (G_k, D_k) for k = 9..0 in
