@@ -161,6 +161,20 @@ int32_t o3g_panels_affect_points(int32_t prec, int32_t mem, int32_t maxlev,
                                  int32_t nt, const float* tx, const float* ty, const float* tz,
                                  float* tu, float* tv, float* tw, float* const* tug, void* stream);
 
+/* ---- panels_affect_panels ----------------------------------------------------------
+ * Replaces panels_affect_panels<float,A>, Influence.h:1223-1243: the velocity the np source
+ * panels induce at the tnp target panels' collocation points (centroid pushed 0.0001 along
+ * the target normal, as Surfaces::represent_as_particles(0.0001, ...) places them), computed
+ * like o3g_panels_affect_points (velocity only) and WRITTEN into tu, tv, tw: the reference
+ * copies the result over the target's panel velocities instead of accumulating. */
+int32_t o3g_panels_affect_panels(int32_t prec, int32_t mem, int32_t maxlev,
+                                 int32_t nn, const float* nx, const float* ny, const float* nz,
+                                 int32_t np, const uint32_t* idx, const float* area,
+                                 const float* tsx, const float* tsy, const float* tsz, const float* sss,
+                                 int32_t tnn, const float* tnx, const float* tny, const float* tnz,
+                                 int32_t tnp, const uint32_t* tidx, const float* tnormx, const float* tnormy,
+                                 const float* tnormz, float* tu, float* tv, float* tw, void* stream);
+
 /* ---- points_affect_panels ----------------------------------------------------------
  * Replaces points_affect_panels<float,A>, Influence.h:1107-1221: panel-averaged velocity
  * induced by ns vortex particles on np panels (the BEM right-hand side), computed like the

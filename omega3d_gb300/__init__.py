@@ -5,11 +5,13 @@ from ._lib import CORES, PRECS, O3GError, lib, header_symbols  # noqa: F401
 from .influence import (BEM, Batch, BatchRalston, BatchSystem, ExecEnv, Ralston, InfluenceVisitor, Points,  # noqa: F401
                         ResultsType, Surfaces, clear_inner_layer, merge_close_particles, represent_as_particles,
                         split_elongated,
-                        generate_ovoid, panels_affect_points, panels_on_panels_coeff, points_affect_panels,
+                        generate_ovoid, panels_affect_panels, panels_affect_points, panels_on_panels_coeff,
+                        points_affect_panels,
                         points_affect_points, solve_bem)
 
 __all__ = ["CORES", "PRECS", "O3GError", "lib", "header_symbols", "ExecEnv", "InfluenceVisitor", "Points",
            "ResultsType", "points_affect_points", "Surfaces", "generate_ovoid", "panels_affect_points",
+           "panels_affect_panels",
            "points_affect_panels", "panels_on_panels_coeff", "BEM", "solve_bem", "Ralston", "Batch",
            "BatchSystem", "BatchRalston", "clear_inner_layer",
            "represent_as_particles", "split_elongated", "merge_close_particles"]

@@ -135,6 +135,9 @@ def _declare(l):
     l.o3g_represent_as_particles.argtypes = [P, c_f] + [P] * 11 + [P]
     l.o3g_clear_inner_layer.restype = c_i32
     l.o3g_clear_inner_layer.argtypes = [c_i32, P, P, P, P, c_f, c_f, P, P]
+    l.o3g_panels_affect_panels.restype = c_i32
+    l.o3g_panels_affect_panels.argtypes = [c_i32, c_i32, c_i32, c_i32, P, P, P, c_i32, P, P, P, P, P, P,
+                                           c_i32, P, P, P, c_i32, P, P, P, P, P, P, P, P]
     l.o3g_split_elongated.restype = c_i32
     l.o3g_split_elongated.argtypes = [c_i32, c_i32] + [P] * 8 + [c_i32, c_f, c_f, P, P]
     l.o3g_merge_close_particles.restype = c_i32

@@ -4,7 +4,11 @@
 // a reactive surface with boundary-condition values).  Diffusion sheds these after its
 // solve_bem (Diffusion.h:187-224).  The float arithmetic is the reference's, without
 // contraction: centroid = (1/3 in double) * (x0 + x1 + x2 in float), rounded to float.
+// The same collocation points serve panels_affect_panels (Influence.h:1223-1243).
 #include "o3g_common.cuh"
+
+#include <algorithm>
+#include <vector>
 
 namespace o3g {
 
@@ -45,9 +49,89 @@ __global__ void k_represent_as_particles(int np, const float* __restrict__ nx, c
   sz[i] = s[2];
 }
 
+// collocation points of panels_affect_panels: the same centroid + offset * normal
+__global__ void k_collocation(int np, const float* __restrict__ nx, const float* __restrict__ ny,
+                              const float* __restrict__ nz, const uint32_t* __restrict__ idx,
+                              const float* __restrict__ nmx, const float* __restrict__ nmy,
+                              const float* __restrict__ nmz, float offset, float* px, float* py, float* pz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const uint32_t a = idx[3 * (size_t)i], b = idx[3 * (size_t)i + 1], c = idx[3 * (size_t)i + 2];
+  const float* node[3] = {nx, ny, nz};
+  const float* nrm[3] = {nmx, nmy, nmz};
+  float* pos[3] = {px, py, pz};
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float sum = __fadd_rn(__fadd_rn(node[j][a], node[j][b]), node[j][c]);
+    const float cen = __double2float_rn(__dmul_rn(1.0 / 3.0, (double)sum));
+    pos[j][i] = __fadd_rn(cen, __fmul_rn(offset, nrm[j][i]));
+  }
+}
+
 }  // namespace o3g
 
 using namespace o3g;
+
+// panels_affect_panels<float,A>, Influence.h:1223-1243: the target panels become points at
+// their centroids pushed 0.0001 along the normal (represent_as_particles(0.0001, ...)), the
+// source panels' velocity there is computed by panels_affect_points (velocity only), and the
+// result is copied into the target panel velocities -- written, not accumulated.
+extern "C" int32_t o3g_panels_affect_panels(int32_t prec, int32_t mem, int32_t maxlev, int32_t nn, const float* nx,
+                                            const float* ny, const float* nz, int32_t np, const uint32_t* idx,
+                                            const float* area, const float* tsx, const float* tsy,
+                                            const float* tsz, const float* sss, int32_t tnn, const float* tnx,
+                                            const float* tny, const float* tnz, int32_t tnp,
+                                            const uint32_t* tidx, const float* tnmx, const float* tnmy,
+                                            const float* tnmz, float* tu, float* tv, float* tw, void* stream) {
+  if ((mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || tnn < 0 || tnp < 0 ||
+      (tnp > 0 && (!tnx || !tny || !tnz || !tidx || !tnmx || !tnmy || !tnmz || !tu || !tv || !tw))) {
+    set_error("o3g_panels_affect_panels: bad mem or target surface (nodes, idx, normals, outputs)");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (tnp == 0) return O3G_OK;
+  const float offset = (float)0.0001;   // represent_as_particles(0.0001, -1.0), Influence.h:1231
+  cudaStream_t st = (cudaStream_t)stream;
+  if (mem == O3G_MEM_HOST) {
+    for (int j = 0; j < 3 * tnp; ++j)
+      if (tidx[j] >= (uint32_t)tnn) {
+        set_error("o3g_panels_affect_panels: target panel index out of range");
+        return O3G_ERR_INVALID_ARG;
+      }
+    std::vector<float> p(3 * (size_t)tnp);
+    const float* node[3] = {tnx, tny, tnz};
+    const float* nrm[3] = {tnmx, tnmy, tnmz};
+    for (int i = 0; i < tnp; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const float sum = (node[j][tidx[3 * (size_t)i]] + node[j][tidx[3 * (size_t)i + 1]]) +
+                          node[j][tidx[3 * (size_t)i + 2]];
+        float c = (float)((1. / 3.) * sum);
+        c += offset * nrm[j][i];
+        p[(size_t)j * tnp + i] = c;
+      }
+    for (float* o : {tu, tv, tw}) std::fill(o, o + tnp, 0.0f);
+    return o3g_panels_affect_points(prec, mem, maxlev, nn, nx, ny, nz, np, idx, area, tsx, tsy, tsz, sss, tnp,
+                                    p.data(), p.data() + tnp, p.data() + 2 * (size_t)tnp, tu, tv, tw, nullptr,
+                                    stream);
+  }
+  float* p = nullptr;
+  O3G_CUDA_TRY(cudaMallocAsync((void**)&p, 3 * (size_t)tnp * sizeof(float), st));
+  k_collocation<<<(tnp + 255) / 256, 256, 0, st>>>(tnp, tnx, tny, tnz, tidx, tnmx, tnmy, tnmz, offset, p, p + tnp,
+                                                   p + 2 * (size_t)tnp);
+  note_launch();
+  cudaError_t e = cudaGetLastError();
+  for (float* o : {tu, tv, tw})
+    if (e == cudaSuccess) e = cudaMemsetAsync(o, 0, (size_t)tnp * sizeof(float), st);
+  int32_t rc = O3G_OK;
+  if (e != cudaSuccess) {
+    set_error_cuda("o3g_panels_affect_panels", e);
+    rc = O3G_ERR_CUDA;
+  } else {
+    rc = o3g_panels_affect_points(prec, mem, maxlev, nn, nx, ny, nz, np, idx, area, tsx, tsy, tsz, sss, tnp, p,
+                                  p + tnp, p + 2 * (size_t)tnp, tu, tv, tw, nullptr, stream);
+  }
+  cudaFreeAsync(p, st);
+  return rc;
+}
 
 extern "C" int32_t o3g_represent_as_particles(const o3g_surface_t* surf, float offset, const float* tsx,
                                               const float* tsy, const float* tsz, const float* bc1,

@@ -168,6 +168,12 @@ class InfluenceVisitor:
     def __call__(self, src, targ):
         if isinstance(src, Points) and isinstance(targ, Points):
             return points_affect_points(src, targ, self.restype, self.env)
+        if isinstance(src, Surfaces) and isinstance(targ, Points):
+            return panels_affect_points(src, targ, self.restype, self.env)
+        if isinstance(src, Points) and isinstance(targ, Surfaces):
+            return points_affect_panels(src, targ, self.env)
+        if isinstance(src, Surfaces) and isinstance(targ, Surfaces):
+            return panels_affect_panels(src, targ, self.env)
         raise NotImplementedError("pairing %s -> %s" % (type(src).__name__, type(targ).__name__))
 
 
@@ -282,6 +288,30 @@ def panels_affect_points(src, targ, restype=None, env=None, maxlev=3, arrays=Non
                                           *_rows(a["ts"], 3), sss, targ.n, *_rows(targ.x, 3), *_rows(targ.u, 3),
                                           tug, env.stream_handle(on_dev))
     L.check(st, "o3g_panels_affect_points")
+
+
+def panels_affect_panels(src, targ, env=None, maxlev=3, src_arrays=None, targ_arrays=None, pu=None):
+    """Influence.h:1223: the velocity of the panels of `src` at the collocation points of the
+    panels of `targ` (centroids 0.0001 along the normal), WRITTEN into the target's panel
+    velocities (targ.pu, or the [3, np] tensor `pu` with device arrays), as the reference
+    copies them.  Device arrays when src_arrays / targ_arrays are given."""
+    env = env or ExecEnv()
+    a = src_arrays or {"x": src.x, "idx": src.idx, "area": src.area, "ts": src.ts, "ps": src.ps}
+    t = targ_arrays or {"x": targ.x, "idx": targ.idx, "norm": targ.norm}
+    on_dev = _is_dev(a["x"])
+    if _is_dev(t["x"]) != on_dev:
+        raise ValueError("source and target surfaces must live in the same memory")
+    out = pu if pu is not None else targ.pu
+    if _is_dev(out) != on_dev:
+        raise ValueError("the velocity array must live with the surfaces")
+    sss = _rows(a["ps"], 3)[2] if src.nunk == 3 else None
+    st = L.lib().o3g_panels_affect_panels(_panel_prec(env), L.MEM_DEVICE if on_dev else L.MEM_HOST, maxlev,
+                                          a["x"].shape[1], *_rows(a["x"], 3), a["area"].shape[0], _base(a["idx"]),
+                                          _base(a["area"]), *_rows(a["ts"], 3), sss,
+                                          t["x"].shape[1], *_rows(t["x"], 3), targ.npanels, _base(t["idx"]),
+                                          *_rows(t["norm"], 3), *_rows(out, 3), env.stream_handle(on_dev))
+    L.check(st, "o3g_panels_affect_panels")
+    return out
 
 
 def points_affect_panels(src, targ, env=None, maxlev=3, arrays=None, pu=None):

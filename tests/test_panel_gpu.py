@@ -154,3 +154,36 @@ def test_coefficient_block_into_larger_matrix(cuda):
     bm = big.cpu().numpy().reshape(-1)
     got = np.stack([bm[(n + 5) * (7 + j) + 3:(n + 5) * (7 + j) + 3 + n] for j in range(n)])
     assert np.array_equal(got, ref)
+
+
+def _collocation(s):
+    """Surfaces::represent_as_particles(0.0001, ...) positions (Surfaces.h:991-997) in the
+    reference's float arithmetic: (1/3 in double) * (float sum), then + offset * normal."""
+    i = s.idx.reshape(-1, 3)
+    tot = (s.x[:, i[:, 0]] + s.x[:, i[:, 1]]) + s.x[:, i[:, 2]]
+    c = (np.float64(1.0 / 3.0) * tot.astype(np.float64)).astype(np.float32)
+    return np.ascontiguousarray(c + np.float32(0.0001) * s.norm)
+
+
+@pytest.mark.parametrize("on_device", [True, False])
+@pytest.mark.parametrize("self_influence", [True, False])
+def test_panels_affect_panels_vs_oracle(cuda, on_device, self_influence):
+    """Influence.h:1223-1243: velocity of the source panels at the target panels'
+    collocation points, written (not accumulated) into the target's panel velocities."""
+    import torch
+    s = _sphere(2, nunk=3)
+    t = s if self_influence else _sphere(1, scale=3.2, seed=6, nunk=2)
+    pts = _collocation(t)
+    uo, _ = O.panels_affect_points(s.x, s.idx, s.area, s.ts, pts, s.ps[2], False, "rm", 1)
+    if on_device:
+        sa, ta = s.device_arrays("cuda"), t.device_arrays("cuda")
+        pu = torch.full((3, t.npanels), 7.0, device="cuda")
+        G.panels_affect_panels(s, t, src_arrays=sa, targ_arrays=ta, pu=pu)
+        torch.cuda.synchronize()
+        u = pu.cpu().numpy()
+    else:
+        t.pu[...] = 7.0
+        G.InfluenceVisitor(G.ResultsType("velonly"))(s, t)
+        u = t.pu.copy()
+    assert rel_err(u, uo)[0] <= 1e-5
+    assert np.abs(u).max() > 0
