@@ -408,3 +408,62 @@ def merge_close_particles(x, s, r, overlap=1.5, threshold=0.2, adapt_radii=False
         raise RuntimeError("merge_close_particles failed")
     k = n - rc
     return np.ascontiguousarray(xs[:, :k]), np.ascontiguousarray(ss[:, :k]), rs[:k].copy(), rc
+
+
+def gmres_restarted(A, b, restart=30, tol=None, max_iter=None):
+    """Restated restarted GMRES of Eigen::GMRES, the solver BEM<S,I>::solve uses
+    (BEM.h:182-202, third-party Eigen >= 3.3, not vendored): left diagonal (Jacobi)
+    preconditioner with 1 where the diagonal is zero, restart 30, tolerance = epsilon of the
+    matrix's type, at most 2n iterations, all in the matrix's precision.  A: (n, n) array
+    (any layout numpy can multiply); b: (n,).  Returns (x, iterations, relative residual of
+    the unpreconditioned system).  Timed by bench.py as the CPU baseline of the BEM solve."""
+    dt = A.dtype
+    n = b.shape[0]
+    tol = np.finfo(dt).eps if tol is None else tol
+    max_iter = 2 * n if max_iter is None else max_iter
+    d = np.ascontiguousarray(np.diagonal(A)).astype(dt)
+    inv = np.where(d != 0, 1 / np.where(d != 0, d, 1), 1).astype(dt)
+    b = b.astype(dt)
+    x = np.zeros(n, dt)
+    pb = np.linalg.norm(inv * b)
+    if pb == 0:
+        return x, 0, 0.0
+    it = 0
+    while it < max_iter:
+        r = inv * (b - A @ x)
+        beta = np.linalg.norm(r)
+        if beta / pb <= tol:
+            break
+        m = min(restart, max_iter - it)
+        V = np.zeros((m + 1, n), dt)
+        H = np.zeros((m + 1, m), np.float64)
+        cs, sn = np.zeros(m), np.zeros(m)
+        g = np.zeros(m + 1)
+        g[0] = beta
+        V[0] = r / beta
+        k_done = 0
+        for k in range(m):
+            w = inv * (A @ V[k])
+            for j in range(k + 1):              # modified Gram-Schmidt
+                H[j, k] = float(V[j] @ w)
+                w = w - dt.type(H[j, k]) * V[j]
+            H[k + 1, k] = float(np.linalg.norm(w))
+            if H[k + 1, k] != 0:
+                V[k + 1] = w / dt.type(H[k + 1, k])
+            for j in range(k):                  # previous Givens rotations
+                h0, h1 = H[j, k], H[j + 1, k]
+                H[j, k], H[j + 1, k] = cs[j] * h0 + sn[j] * h1, -sn[j] * h0 + cs[j] * h1
+            den = np.hypot(H[k, k], H[k + 1, k])
+            cs[k], sn[k] = (H[k, k] / den, H[k + 1, k] / den) if den != 0 else (1.0, 0.0)
+            H[k, k], H[k + 1, k] = den, 0.0
+            g[k + 1] = -sn[k] * g[k]
+            g[k] = cs[k] * g[k]
+            it += 1
+            k_done = k + 1
+            if abs(g[k + 1]) / pb <= tol or H[k, k] == 0:
+                break
+        y = np.linalg.solve(np.triu(H[:k_done, :k_done]), g[:k_done])
+        x = x + (V[:k_done].T @ y.astype(dt)).astype(dt)
+    bn = np.linalg.norm(b.astype(np.float64))
+    rel = float(np.linalg.norm(b.astype(np.float64) - A.astype(np.float64) @ x.astype(np.float64)) / bn)
+    return x, it, rel
