@@ -66,6 +66,18 @@ def parse():
     return ap.parse_args()
 
 
+def whole_job(local_step_ms, units_per_rank, world, dist=None, device=None):
+    """Replicas: every rank processes the same number of units; the job's rate is all ranks'
+    units over the slowest rank's step time (all-reduce MAX).  Returns (units/s, max ms)."""
+    step_max = float(local_step_ms)
+    if world > 1:
+        import torch
+        t = torch.tensor([step_max], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_max = float(t.item())
+    return world * units_per_rank / (step_max * 1e-3), step_max
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -678,6 +690,8 @@ def run_ours(args):
             L.check(lib.o3g_last_kernel_ms(ctypes.byref(km)), "o3g_last_kernel_ms")
             kern_ms.append(float(km.value))
         torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
         wall = time.perf_counter() - t0
         launches = L.launch_count() - n0
         lib.o3g_set_timing(0)
@@ -749,12 +763,7 @@ def run_ours(args):
     local_rate = pairs / (comp_step * 1e-3)
 
     # whole-job numbers: max time over ranks, interactions summed
-    step_max = comp_step
-    if world > 1:
-        t = torch.tensor([comp_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_max = float(t.item())
-    value = world * pairs / (step_max * 1e-3)
+    value, step_max = whole_job(comp_step, pairs, world, dist if world > 1 else None, dev)
 
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
