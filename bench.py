@@ -99,8 +99,9 @@ def cpu_reference(args, nthreads=None, ntarg=None, reps=1):
     from omega3d_gb300 import workloads as W
     x, s, r = W.gaussian_cloud(args.n, seed=2)
     nthreads = nthreads or (os.cpu_count() or 1)
-    ntarg = ntarg or min(args.n, 1024)
-    idx = np.linspace(0, args.n - 1, ntarg).astype(np.int64)
+    ntarg = ntarg or min(args.n, 4096)
+    # a seeded subset of the targets, against all sources; scaled to the full count by rate
+    idx = np.sort(np.random.default_rng(7).choice(args.n, ntarg, replace=False)).astype(np.int64)
     tx, tr = np.ascontiguousarray(x[:, idx]), np.ascontiguousarray(r[idx])
     oracle.points_affect_points(x[:, :4096], r[:4096], s[:, :4096], tx[:, :64], tr[:64], True, args.core, 1,
                                 nthreads)
@@ -560,10 +561,27 @@ def bench_bem_cpu(W):
     t2 = time.perf_counter()
     _, it, rel = O.gmres_restarted(C.T, b)
     t3 = time.perf_counter()
-    return {"n": int(b.shape[0]), "rhs_s": t1 - t0, "assemble_s": t2 - t1, "gmres_s": t3 - t2,
+    del C
+    # FP64 LU (numpy / LAPACK on all host cores) of the 10,240-unknown system of the
+    # 4-level sphere, a bounded sample: the full 40,960-unknown factorisation would take
+    # minutes; its time scales as n^3
+    n4, i4 = O.generate_ovoid(4, 2.0, 2.0, 2.0)
+    a1, a2, an, aa = O.compute_bases(n4, i4)
+    C4 = O.panels_on_panels_coeff(dict(nodes=n4, idx=i4, area=aa, x1=a1, x2=a2, norm=an),
+                                  dict(nodes=n4, idx=i4, area=aa, x1=a1, x2=a2, norm=an), 2, True, "rm", 0)
+    A4 = np.ascontiguousarray(C4.T, dtype=np.float64)
+    b4 = np.zeros(A4.shape[0])
+    b4[0::2], b4[1::2] = -a1[0], -a2[0]
+    t4 = time.perf_counter()
+    np.linalg.solve(A4, b4)
+    lu4 = time.perf_counter() - t4
+    n = int(b.shape[0])
+    return {"n": n, "rhs_s": t1 - t0, "assemble_s": t2 - t1, "gmres_s": t3 - t2,
             "gmres_iterations": it, "gmres_relres": rel, "total_s": t3 - t0, "cores": os.cpu_count() or 1,
             "kind": "port",
-            "sample": "the whole workload: oracle loops (OpenMP) + restated Eigen GMRES in numpy FP32"}
+            "sample": "the whole workload: oracle loops (OpenMP) + restated Eigen GMRES in numpy FP32",
+            "fp64_lu": {"n": int(A4.shape[0]), "solve_s": lu4, "scaled_to_n_s": lu4 * (n / A4.shape[0]) ** 3,
+                        "sample": "numpy FP64 LU solve of the 4-level sphere's system, scaled by n^3 to n"}}
 
 
 def bench_splitmerge(args, G, torch, W, reps=3):
