@@ -281,9 +281,17 @@ def bench_ring(args, G, torch, W):
     e1.record()
     torch.cuda.synchronize()
     step_ms = e0.elapsed_time(e1) / 10
+    # CPU baseline, timed in full: the oracle port (float pairs, double sums, OpenMP)
+    import oracle as O
+    nth = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.points_affect_points(x, r, s, x, r, True, "rm", 1, nth)
+    cpu_s = time.perf_counter() - t0
     return {"n": 16384, "core": "rm", "eval_ms": eval_ms,
             "eval_interactions_per_s": 16384.0 ** 2 / (eval_ms * 1e-3), "rk2_step_ms": step_ms,
-            "rk2_steps": 10, "dt": 0.01, "graph": True}
+            "rk2_steps": 10, "dt": 0.01, "graph": True,
+            "cpu_baseline": {"eval_s": cpu_s, "interactions_per_s": 16384.0 ** 2 / cpu_s, "cores": nth,
+                             "kind": "port", "sample": "the whole evaluation (16,384 x 16,384)"}}
 
 
 def bench_batch(args, G, torch, W, flush):
@@ -534,6 +542,19 @@ def bench_coupled(args, G, torch, W):
     out["steps"] = steps
     out["step_ms"] = ms / steps
     out["interactions_per_step"] = 2 * (pairs + float(surf.npanels) * n * 2)
+    # CPU baseline of the particle-particle sums, the step's dominant part: the oracle port
+    # on a seeded 4,096-target subset against all 1,048,576 sources, scaled by rate
+    import oracle as O
+    nth = os.cpu_count() or 1
+    sub = np.sort(np.random.default_rng(7).choice(n, 4096, replace=False))
+    tx_, tr_ = np.ascontiguousarray(px[:, sub]), np.ascontiguousarray(pr[sub])
+    t0 = time.perf_counter()
+    O.points_affect_points(px, pr, ps, tx_, tr_, True, "rm", 1, nth)
+    cpu_rate = 4096.0 * n / (time.perf_counter() - t0)
+    out["cpu_baseline_particle_particle"] = {
+        "interactions_per_s": cpu_rate, "stage_s_scaled": pairs / cpu_rate, "cores": nth, "kind": "port",
+        "sample": "4,096 seeded targets x 1,048,576 sources (RM, float pairs, double sums)",
+        "gpu_stage_speedup": (pairs / cpu_rate) / (pair_ms * 1e-3)}
     out["bem"] = st
     out["finite"] = bool(torch.isfinite(X).all().item())
     del rk, bem
