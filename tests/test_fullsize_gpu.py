@@ -7,10 +7,12 @@ need a CPU sum over all pairs:
 * the 40,960-unknown sphere system (20,480 panels, 100,000 particles): GMRES and the LU path
   both reach 1e-10 and agree with each other;
 * the 1,048,576-particle wake (RM core, compensated): sums against the FP64 path at 1,024
-  seeded targets.
+  seeded targets;
+* the 64 seeded blob systems in one batched launch: 8 systems against the FP64 path.
 
 Bounds (stated per test): compensated L-infinity (max |du| / max |u| over the sample)
-<= 1e-6, per-target relative <= 1e-5; plain L-infinity <= 2e-5."""
+<= 1e-6, per-target relative <= 1e-5 (2e-5 on the strongly cancelling blobs); plain
+L-infinity <= 2e-5."""
 import numpy as np
 import pytest
 
@@ -98,3 +100,33 @@ def test_wake_particles_full_size(cuda):
     uc, gc = _sums(x, s, r, "rm", "compensated")
     assert linf_err(uc[:, sub], u64) <= 1e-6 and linf_err(gc[:, sub], g64) <= 1e-6
     assert rel_err(uc[:, sub], u64)[0] <= 1e-5
+
+
+def test_batch_64_systems_full_size(cuda):
+    """The 64 seeded blob systems (1,024 to 65,536 particles, 4,096 field points each) in one
+    compensated Gaussian launch; 8 of them checked against the FP64 path for that system
+    alone, particles and field points.  These blobs cancel strongly at some targets, where
+    FP32 pair terms alone give up to 6.5e-6 per target, so the per-target bound is 2e-5."""
+    systems = W.batch_systems(64, seed=4)
+    devs = []
+    for x, s, r, f in systems:
+        n, nf = x.shape[1], f.shape[1]
+        devs.append(G.BatchSystem(_t(x), _t(s), _t(r), torch.zeros((3, n), device="cuda"),
+                                  torch.zeros((9, n), device="cuda"), _t(f), torch.zeros((3, nf), device="cuda"),
+                                  torch.zeros((9, nf), device="cuda")))
+    G.Batch(devs, G.ExecEnv("gauss", "compensated"), grads=True).run()
+    torch.cuda.synchronize()
+    for k in range(0, 64, 8):
+        x, s, r, f = systems[k]
+        src = G.Points(_t(x.astype(np.float64)), _t(s.astype(np.float64)), _t(r.astype(np.float64)))
+        tp = G.Points(_t(x.astype(np.float64)), None, _t(r.astype(np.float64)))
+        tf = G.Points(_t(f.astype(np.float64)), None, None, inert=True)
+        for tq in (tp, tf):
+            G.points_affect_points(src, tq, G.ResultsType(), G.ExecEnv("gauss", "fp64"))
+        torch.cuda.synchronize()
+        d = devs[k]
+        for got_u, got_g, ref in ((d.u, d.ug, tp), (d.fu, d.fug, tf)):
+            u, g = got_u.cpu().numpy(), got_g.cpu().numpy()
+            u64, g64 = ref.u.cpu().numpy(), ref.ug.cpu().numpy()
+            assert linf_err(u, u64) <= 1e-6 and linf_err(g, g64) <= 1e-6
+            assert rel_err(u, u64)[0] <= 2e-5 and rel_err(g, g64)[0] <= 2e-5
