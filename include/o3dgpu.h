@@ -51,7 +51,7 @@ enum { O3G_CORE_RM = 0, O3G_CORE_WL = 1, O3G_CORE_EXP = 2, O3G_CORE_GAUSS = 3, O
 /* Arithmetic of the pair sums:
  *  PLAIN       FP32 pair arithmetic and FP32 accumulation (the reference's Vc path);
  *  COMPENSATED FP32 pair arithmetic with a Newton-refined rsqrt and per-tile partial
- *              sums folded into two-sum (hi, lo) accumulators;
+ *              sums folded into compensated (hi, lo) accumulators;
  *  FP64        everything in double (comparator / oracle on the device). */
 enum { O3G_PREC_PLAIN = 0, O3G_PREC_COMPENSATED = 1, O3G_PREC_FP64 = 2 };
 

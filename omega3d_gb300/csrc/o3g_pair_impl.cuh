@@ -124,15 +124,9 @@ __device__ __forceinline__ void fold_grads(T* a) {
   a[10] -= a[12];
 }
 
-// error-free transformation of a + b (Knuth's two-sum): s + e == a + b exactly
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
 // Sweep the staged tile (kBlock sources in shared memory) for TPT targets.  In the
-// compensated mode the plain partial of every FOLD sources is folded into (hi, lo).
+// compensated mode the plain partial of every FOLD sources is folded into (hi, lo) with
+// Fast2Sum.
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, int NA, int NC, int NH, int NS = kBlock>
 __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, const V4<T>* tp, T (*acc)[NA],
                                            float (*hi)[NH], float (*lo)[NH]) {
@@ -157,7 +151,10 @@ __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, con
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           float s, e;
-          two_sum(hi[k][c], (float)acc[k][c], s, e);
+          // Fast2Sum: exact error term when |hi| >= |partial|, the usual case once a few
+          // folds have accumulated; otherwise that fold loses at most its own rounding
+          s = hi[k][c] + (float)acc[k][c];
+          e = (float)acc[k][c] - (s - hi[k][c]);
           hi[k][c] = s;
           lo[k][c] += e;
         }

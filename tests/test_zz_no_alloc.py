@@ -3,8 +3,10 @@ allocate device memory (programs that hand all device memory to their own pool, 
 loops, plugin hosts that forbid allocation after start-up).  Its scratch lives in a fixed
 array inside the library, so the test calls it twice in a row -- the second call finds the
 first call's leftovers in that array -- and checks both results against the allocating
-entry point o3g_points_affect_points.  Tolerances are the parity tests' own: per-target
-relative error <= 1e-5 for PLAIN; L-infinity <= 1e-6 and per-target <= 1e-5 for COMPENSATED.
+entry point o3g_points_affect_points.  The two split the sources differently, so PLAIN
+compares two FP32 summation orders: L-infinity <= 1e-5 and per target <= 3e-5 (orders land
+up to 1.5e-5 apart where a sum cancels strongly, as in the batch tests).  COMPENSATED:
+L-infinity <= 1e-6 and per-target <= 1e-5.
 
 This file is named to be collected last, so a run that stops at the first failure has
 run every other test before it; it also passes on its own in a fresh process.
@@ -66,7 +68,10 @@ def test_noalloc_matches_allocating_entry_point_twice(cuda, core, prec, case):
         torch.cuda.synchronize()
         u, g = U.cpu().numpy(), G.cpu().numpy()
         if prec == "plain":
-            assert rel_err(u, u0)[0] <= 1e-5 and rel_err(g, g0)[0] <= 1e-5
+            # the two entry points split the sources differently: two FP32 summation orders,
+            # which land up to 1.5e-5 apart per target where the sum cancels strongly
+            assert linf_err(u, u0) <= 1e-5 and linf_err(g, g0) <= 1e-5
+            assert rel_err(u, u0)[0] <= 3e-5 and rel_err(g, g0)[0] <= 3e-5
         else:
             assert linf_err(u, u0) <= 1e-6 and linf_err(g, g0) <= 1e-6
             assert rel_err(u, u0)[0] <= 1e-5 and rel_err(g, g0)[0] <= 1e-5
