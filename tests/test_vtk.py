@@ -40,3 +40,27 @@ def test_field_points_have_no_strength_or_radius(tmp_path):
     assert path.endswith("fldpt_00_00007.vtu")
     d = vtk.read_vtu(path)
     assert "circulation" not in d and "radius" not in d and d["velocity"].shape == (3, 5)
+
+
+def test_surface_vtu_round_trip(tmp_path):
+    """Surfaces::write_vtk layout: triangles over the nodes, the vortex sheet vector
+    ps0 x1 + ps1 x2 (float) and the source sheet strength as cell data."""
+    import omega3d_gb300 as G
+    from omega3d_gb300 import vtk
+    x, i = G.generate_ovoid(1, 2.0, 2.0, 2.0)
+    s = G.Surfaces(x, i, nunk=3)
+    rng = np.random.default_rng(4)
+    s.set_sheet_strengths(rng.normal(size=s.npanels).astype(np.float32),
+                          rng.normal(size=s.npanels).astype(np.float32),
+                          rng.normal(size=s.npanels).astype(np.float32))
+    path = vtk.write_surface_vtk(s, 1, 12, 0.25, directory=str(tmp_path))
+    assert path.endswith("panel_01_00012.vtu")
+    d = vtk.read_vtu(path)
+    assert np.array_equal(d["position"], s.x)
+    assert np.array_equal(d["connectivity"], s.idx.astype(np.int32))
+    assert np.array_equal(d["offsets"], 3 * np.arange(1, s.npanels + 1, dtype=np.int32))
+    assert np.all(d["types"] == 5)
+    sheet = (s.ps[0] * s.x1 + s.ps[1] * s.x2).astype(np.float32)
+    assert np.array_equal(d["vortex sheet strength"], sheet)
+    assert np.array_equal(d["source sheet strength"], s.ps[2])
+    assert d["TimeValue"][0] == 0.25
