@@ -4,7 +4,7 @@ Python mirror of its call surface."""
 from ._lib import CORES, PRECS, O3GError, lib, header_symbols  # noqa: F401
 from .influence import (BEM, Batch, BatchRalston, BatchSystem, ExecEnv, Ralston, InfluenceVisitor, Points,  # noqa: F401
                         ResultsType, Surfaces, clear_inner_layer, merge_close_particles, represent_as_particles,
-                        split_elongated,
+                        shed_particles, split_elongated,
                         generate_ovoid, panels_affect_panels, panels_affect_points, panels_on_panels_coeff,
                         points_affect_panels,
                         points_affect_points, solve_bem)
@@ -14,4 +14,4 @@ __all__ = ["CORES", "PRECS", "O3GError", "lib", "header_symbols", "ExecEnv", "In
            "panels_affect_panels",
            "points_affect_panels", "panels_on_panels_coeff", "BEM", "solve_bem", "Ralston", "Batch",
            "BatchSystem", "BatchRalston", "clear_inner_layer",
-           "represent_as_particles", "split_elongated", "merge_close_particles"]
+           "represent_as_particles", "split_elongated", "merge_close_particles", "shed_particles"]

@@ -563,6 +563,32 @@ def solve_bem(fs, vort, bdry, bem, env=None, maxlev=3, tol=1e-10, max_iter=30):
     return xs
 
 
+def shed_particles(fs, vort, bdry, bem, h_nu, vdelta, env=None, bc=None, maxlev=3, tol=1e-10, max_iter=30):
+    """Diffusion's shedding (Diffusion.h:184-224): re-solve the BEM for the current particles
+    (solve_bem), put one particle per panel 0.01 h_nu above the surface carrying the
+    panel's strength (Surfaces::represent_as_particles, Surfaces.h:959-1008; bc = (bc1, bc2)
+    adds the reactive boundary-condition sheet) and append them to the last collection of
+    `vort` (host Points) with core radius vdelta, as Points::add_new does (Points.h:160-200);
+    with no collection a new one is made.  Returns the new particles' (x, s) [3, np]."""
+    solve_bem(fs, vort, bdry, bem, env, maxlev, tol, max_iter)
+    # the reference's offset 0.01*(S)h_nu: double product rounded to the float parameter
+    offset = float(np.float32(0.01 * float(np.float32(h_nu))))
+    px, ps = represent_as_particles(bdry, offset, bc=bc, arrays=bdry.device_arrays("cuda"))
+    x, s = px.cpu().numpy(), ps.cpu().numpy()
+    r = np.full(x.shape[1], np.float32(vdelta), np.float32)
+    if vort:
+        v = vort[-1]
+        v.x = np.ascontiguousarray(np.concatenate([v.x, x], axis=1))
+        v.s = np.ascontiguousarray(np.concatenate([v.s, s], axis=1))
+        v.r = np.ascontiguousarray(np.concatenate([v.r, r]))
+        grads = v.ug is not None
+        v.u = np.zeros((3, v.x.shape[1]), np.float32)
+        v.ug = np.zeros((9, v.x.shape[1]), np.float32) if grads else None
+    else:
+        vort.append(Points(x, s, r))
+    return x, s
+
+
 # ------------------------------------------------------------------------------------
 # convection
 

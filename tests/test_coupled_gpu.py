@@ -213,3 +213,25 @@ def test_represent_as_particles_bit_exact(cuda, with_bc):
     px, ps = G.represent_as_particles(s, 0.0125, bc=(_t(bc1), _t(bc2)) if with_bc else None, arrays=arr)
     po, so = O.represent_as_particles(s.x, s.idx, s.area, s.x1, s.x2, s.norm, 0.0125, s.ts, bc1, bc2)
     assert np.array_equal(px.cpu().numpy(), po) and np.array_equal(ps.cpu().numpy(), so)
+
+
+def test_shed_particles_after_bem_solve(cuda):
+    """Diffusion.h:184-224: solve_bem for the current particles, then one particle per panel
+    0.01 h_nu above the surface with the solved panel strength, appended to the last
+    collection with core radius vdelta; positions and strengths bit-identical to the
+    oracle's represent_as_particles of the solved strengths."""
+    x, i = G.generate_ovoid(2, 2.0, 2.0, 2.0)
+    surf = G.Surfaces(x, i, nunk=2)
+    px, ps, pr = W.shell_particles(2000, seed=31)
+    vort = [G.Points(px, ps, pr)]
+    bem = G.BEM(surf.npanels * 2)
+    h_nu, vdelta = 0.05, 0.02
+    nx, ns = G.shed_particles((1.0, 0.0, 0.0), vort, surf, bem, h_nu, vdelta)
+    assert vort[0].n == 2000 + surf.npanels
+    assert np.array_equal(vort[0].x[:, 2000:], nx) and np.array_equal(vort[0].s[:, 2000:], ns)
+    assert np.all(vort[0].r[2000:] == np.float32(vdelta))
+    off = float(np.float32(0.01 * float(np.float32(h_nu))))
+    ox, os_ = O.represent_as_particles(surf.x, surf.idx, surf.area, surf.x1, surf.x2, surf.norm, off, surf.ts)
+    assert np.array_equal(nx.view(np.uint32), ox.view(np.uint32))
+    assert np.array_equal(ns.view(np.uint32), os_.view(np.uint32))
+    assert np.abs(ns).max() > 0
