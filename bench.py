@@ -670,6 +670,10 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
+        # replicas: the flagship cloud section only; the other workloads are single-GPU
+        # reports and would hold every GPU (and the shared host cores) for minutes
+        args.skip_bem = args.skip_ring = args.skip_batch = args.skip_splitmerge = True
+        args.coupled_steps = 0
     lib = L.lib()
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
