@@ -104,10 +104,13 @@ def fit():
 
 
 def write(table, worst, path):
+    # coefficient-major: entry k of every interval side by side, so the lanes of a warp
+    # reading entry k of their own intervals touch one cache line
+    names = ["s", "o"] + ["%s%d" % (f, k) for k in range(DEG, -1, -1) for f in ("G", "D")]
     lines = []
-    for lo, hi, row in zip(EDGES[:-1], EDGES[1:], table):
-        vals = ", ".join("%.9ef" % np.float32(v) for v in row)
-        lines.append("    // q in [%g, %g]\n    %s," % (lo, hi, vals))
+    for k in range(STRIDE):
+        vals = ", ".join("%.9ef" % np.float32(row[k]) for row in table)
+        lines.append("    // %s\n    %s," % (names[k] if k < len(names) else "pad", vals))
     body = "\n".join(lines)
     txt = f"""// o3g_gauss_poly.h -- GENERATED by gauss_poly_gen.py (do not edit): piecewise polynomials of
 // the FP32 Gaussian core on q in [0, 48]: G(q) (r3 = G / sigma^3) and D(q) = 2 G'(q)
@@ -119,9 +122,11 @@ def write(table, worst, path):
 namespace o3g {{
 
 constexpr int kGaussPolyDeg = {DEG};
-constexpr int kGaussPolyStride = {STRIDE};   // s, o, (G[k], D[k]) for k = {DEG}..0
-constexpr int kGaussPolyLast = {len(table) - 1};       // interval j covers [(j/2)^2, ((j+1)/2)^2)
-__device__ const __align__(16) float kGaussPoly[{len(table)} * {STRIDE}] = {{
+constexpr int kGaussPolyStride = {STRIDE};   // entries per interval: s, o, (G[k], D[k]) for k = {DEG}..0
+constexpr int kGaussPolyN = {len(table)};        // intervals; interval j covers [(j/2)^2, ((j+1)/2)^2)
+constexpr int kGaussPolyLast = {len(table) - 1};
+// entry k of interval j at kGaussPoly[k * kGaussPolyN + j]
+__device__ const __align__(16) float kGaussPoly[{STRIDE} * {len(table)}] = {{
 {body}
 }};
 

@@ -154,27 +154,30 @@ __device__ __forceinline__ int gauss_interval(float q) {
   return min((int)(2.0f * qq * rsqrtf(qq)), kGaussPolyLast);
 }
 
-// G(q) and D(q) by Horner's rule in t; the row holds (s, o), then (G_k, D_k) for k = 9..0 in
-// the order used.  Scalar loads: vector loads of the row made the compiler keep all of it
-// live, which cost the pair kernel a fifth of its occupancy.
+// G(q) and D(q) by Horner's rule in t.  The table is coefficient-major (entry e of interval
+// j at e * kGaussPolyN + j), so the lanes of a warp, whatever their intervals, read each
+// entry from one cache line.  Scalar loads: vector loads of a row made the compiler keep
+// all of it live, which cost the pair kernel a fifth of its occupancy.
 __device__ __forceinline__ void gauss_poly(float q, float& G, float& D) {
-  const float* c = kGaussPoly + gauss_interval(q) * kGaussPolyStride;
-  const float t = fmaf(q, __ldg(c), __ldg(c + 1));
-  float g = __ldg(c + 2), d = __ldg(c + 3);
+  constexpr int N = kGaussPolyN;
+  const float* c = kGaussPoly + gauss_interval(q);   // entry e of this interval: c[e * N]
+  const float t = fmaf(q, __ldg(c), __ldg(c + N));
+  float g = __ldg(c + 2 * N), d = __ldg(c + 3 * N);
 #pragma unroll
   for (int k = 1; k <= kGaussPolyDeg; ++k) {
-    g = fmaf(g, t, __ldg(c + 2 + 2 * k));
-    d = fmaf(d, t, __ldg(c + 3 + 2 * k));
+    g = fmaf(g, t, __ldg(c + (2 + 2 * k) * N));
+    d = fmaf(d, t, __ldg(c + (3 + 2 * k) * N));
   }
   G = g;
   D = d;
 }
 __device__ __forceinline__ float gauss_poly_g(float q) {
-  const float* c = kGaussPoly + gauss_interval(q) * kGaussPolyStride;
-  const float t = fmaf(q, __ldg(c), __ldg(c + 1));
-  float g = __ldg(c + 2);
+  constexpr int N = kGaussPolyN;
+  const float* c = kGaussPoly + gauss_interval(q);
+  const float t = fmaf(q, __ldg(c), __ldg(c + N));
+  float g = __ldg(c + 2 * N);
 #pragma unroll
-  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, __ldg(c + 2 + 2 * k));
+  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, __ldg(c + (2 + 2 * k) * N));
   return g;
 }
 
