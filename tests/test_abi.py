@@ -58,3 +58,33 @@ def test_no_device_is_reported_not_crashed(built_lib):
         pytest.skip("a device is present")
     st = _call(built_lib)
     assert st in (2, 3)
+
+
+def _prototypes():
+    """{name: number of parameters} of every function declared in include/o3dgpu.h."""
+    import re
+    txt = open(L.HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for m in re.finditer(r"\b(o3g_[a-z0-9_]+)\s*\(([^;{}]*?)\)\s*;", txt, flags=re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_bindings_match_header_prototypes(built_lib):
+    """Every entry point the Python binding declares argtypes for takes as many arguments
+    as its C prototype (a miscounted argtypes list would shift every later pointer)."""
+    protos = _prototypes()
+    assert len(protos) >= 40
+    checked, bad = 0, []
+    for name, nargs in protos.items():
+        fn = getattr(built_lib, name)
+        if fn.argtypes is None:
+            continue
+        checked += 1
+        if len(fn.argtypes) != nargs:
+            bad.append((name, nargs, len(fn.argtypes)))
+    assert not bad, "argtypes count differs from the prototype: %s" % bad
+    assert checked >= 30
