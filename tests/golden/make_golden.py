@@ -9,7 +9,7 @@ oracle/ref_splitmerge_driver.cpp):
 
     sh oracle/build_ref.sh && python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py --only reflect                       # reflect.npz alone
-    python tests/golden/make_golden.py --only splitmerge                    # splitmerge.npz alone
+    python tests/golden/make_golden.py --only splitmerge                    # splitmerge*.npz alone
 
 Every fixture holds its seeded inputs and the outputs of the reference build for the
 precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
@@ -104,6 +104,22 @@ def write_splitmerge():
                              "merge": {"merge_vrm": [0.2, False], "merge_core": [0.02, False],
                                        "merge_amr": [0.2, True]},
                              "source": "reference Split.h / Merge.h with lib/nanoflann"},
+          x_in=x, s_in=s, r_in=r, e_in=e, **out)
+    write_splitmerge_tied()
+
+
+def write_splitmerge_tied():
+    """Split of an unjittered 12^3 lattice by the reference's Split.h.  Every particle has
+    neighbours at exactly equal float distances, so the reference's visiting order of those
+    ties comes from its nanoflann kd-tree and std::sort, not from the distances."""
+    x, s, r, e = W.lattice_particles(k=12, seed=40, jitter=0.0)
+    out = {}
+    for core in (0, 1):
+        xs, ss, rs, es, m = O.split_elongated(x, s, r, e, core, 1.5, 1.2, use_ref=True)
+        out.update({"split%d_x" % core: xs, "split%d_s" % core: ss, "split%d_r" % core: rs,
+                    "split%d_e" % core: es})
+    _save("splitmerge_tied.npz", {"pinned": True, "overlap": 1.5, "split_threshold": 1.2,
+                                  "source": "reference Split.h with lib/nanoflann"},
           x_in=x, s_in=s, r_in=r, e_in=e, **out)
 
 

@@ -320,6 +320,36 @@ def test_oracle_split_merge_bit_exact_vs_reference(scale):
             assert all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
 
 
+def _has_equal_distance_neighbours(x, r, overlap=1.5):
+    """True when some particle has two neighbours within the split search radius at exactly
+    the same float distance (the metric and radius of Split.h:127-134)."""
+    p = x[:, 0]
+    d2 = ((x[0] - p[0]) ** 2 + (x[1] - p[1]) ** 2) + (x[2] - p[2]) ** 2
+    rad = np.float32(3.0) * (r[0] / np.float32(overlap))
+    d2 = d2[d2 < rad * rad]
+    return np.unique(d2).size < d2.size
+
+
+def test_oracle_split_tied_lattice_within_tolerance():
+    """An unjittered lattice: neighbours at exactly equal distance.  The oracle visits such
+    ties in increasing index; the reference in the order its nanoflann kd-tree layout and
+    std::sort leave them.  Only the curvature sums (Split.h:148-176) see that order: the
+    count, positions, radii and elongations stay bit-identical, and every strength component
+    is within 1e-7 of the largest strength magnitude (below one FP32 epsilon of it)."""
+    d, meta = _gold("splitmerge_tied.npz")
+    assert meta["pinned"]
+    x, s, r, e = d["x_in"], d["s_in"], d["r_in"], d["e_in"]
+    assert _has_equal_distance_neighbours(x, r, meta["overlap"])
+    for core in (0, 1):
+        got = O.split_elongated(x, s, r, e, core, meta["overlap"], meta["split_threshold"])
+        want = [d["split%d_%s" % (core, k)] for k in "xsre"]
+        assert got[4] == want[0].shape[1] - x.shape[1] > 0
+        for k in (0, 2, 3):
+            assert _bits(got[k], want[k])
+        ds = np.abs(got[1].astype(np.float64) - want[1]).max()
+        assert ds <= 1e-7 * np.abs(want[1]).max(), ds
+
+
 def test_oracle_split_conserves_moments():
     """Split.h's comment: zeroth and first moments kept.  The two halves' strengths add
     back to the parent's (to float rounding) and their strength-weighted centre is the

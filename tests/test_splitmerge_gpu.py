@@ -63,6 +63,25 @@ def test_merge_golden(name, thr, adapt):
         _bits_equal(v, d["%s_%s" % (name, k)])
 
 
+@pytest.mark.parametrize("core", [0, 1])
+def test_split_tied_lattice(core):
+    """Unjittered lattice (neighbours at exactly equal distance).  The kernel and the oracle
+    both visit ties in increasing index: bit-identical.  Against the reference's own output,
+    whose tie order follows its kd-tree: count, positions, radii and elongations
+    bit-identical, strengths within 1e-7 of the largest strength magnitude."""
+    d = np.load(os.path.join(os.path.dirname(GOLDEN), "splitmerge_tied.npz"))
+    x, s, r, e = d["x_in"], d["s_in"], d["r_in"], d["e_in"]
+    got = _split_gpu(x, s, r, e, ["gaussian", "compactg"][core])
+    want = O.split_elongated(x, s, r, e, core, 1.5, 1.2)
+    assert got[4] == want[4] > 0
+    for a, b in zip(got[:4], want[:4]):
+        _bits_equal(a, b)
+    for k in (0, 2, 3):
+        _bits_equal(got[k], d["split%d_%s" % (core, "xsre"[k])])
+    ref_s = d["split%d_s" % core]
+    assert np.abs(got[1].astype(np.float64) - ref_s).max() <= 1e-7 * np.abs(ref_s).max()
+
+
 @pytest.mark.parametrize("k,scale,core", [(40, 0.12, 0), (40, 0.05, 1), (100, 0.12, 0)])
 def test_split_vs_oracle(k, scale, core):
     """64,000 and 1,000,000 particles; with the 0.12 tail 19 % split and the dependency
