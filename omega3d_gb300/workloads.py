@@ -99,3 +99,17 @@ def lattice_particles(k=64, seed=6, spacing=0.01, jitter=0.35, str_scale=1e-4, o
     r = np.full(g.shape[1], overlap * spacing)
     e = 1.0 + rng.exponential(elong_scale, g.shape[1])
     return g.astype(np.float32), s.astype(np.float32), r.astype(np.float32), e.astype(np.float32)
+
+
+def duplicated_particles(k=12, seed=41, every=5, seed_dup=2):
+    """lattice_particles(k, seed) followed by exact copies of a seeded 1/every of its
+    particles (same position, radius and elongation; new strengths N(0,1)*1e-4): neighbours
+    at exactly equal distance, the case where the order of a radius search's ties decides
+    which of two coincident particles a merge keeps."""
+    x, s, r, e = lattice_particles(k=k, seed=seed)
+    rng = np.random.default_rng(seed_dup)
+    n = x.shape[1]
+    d = np.sort(rng.choice(n, n // every, replace=False))
+    sd = (rng.normal(size=(3, d.size)) * 1e-4).astype(np.float32)
+    cat = lambda a, b: np.ascontiguousarray(np.concatenate([a, b], axis=-1))
+    return cat(x, x[:, d]), cat(s, sd), cat(r, r[d]), cat(e, e[d])

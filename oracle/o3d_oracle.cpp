@@ -1154,9 +1154,10 @@ extern "C" int o3o_represent_as_particles(int nn, const float* nodes, int np, co
 // (lib/nanoflann/nanoflann.hpp): d2 = ((q0-p0)^2 + (q1-p1)^2) + (q2-p2)^2 in float
 // (L2_Adaptor::evalMetric, :383-405, query minus point) and d2 < radius (strict,
 // RadiusResultSet::addPoint, :249-253).  Matches are visited in increasing d2
-// (params.sorted, :1285-1286); equal d2 are taken in increasing index here, where the
-// reference's order for such ties depends on its kd-tree layout.  The neighbour search
-// below is a uniform cell list; it finds exactly the same match set.
+// (params.sorted, :1285-1286).  The default search is a uniform cell list that finds the
+// same match set and takes equal d2 in increasing index, as the kernels do; the
+// reference's order for such ties depends on its kd-tree layout, which OracleKdTree
+// restates for the tie_order = 1 variant.
 namespace {
 
 struct OracleCells {
@@ -1226,6 +1227,244 @@ struct OracleCells {
   }
 };
 
+// The reference's own visiting order, for inputs with equal-distance neighbours: a
+// restatement of nanoflann 1.3.1's KDTreeSingleIndexAdaptor as KDTreeEigenMatrixAdaptor
+// instantiates it in Split.h:74-76 / Merge.h:85-87 (3 float dimensions, leaf_max_size 10,
+// Eigen Index = int64 indices, L2_Adaptor metric, eps 0).
+//   build:  vind = 0..n-1 (init_vind, :1308-1315); root box = the points' min/max
+//           (computeBoundingBox, :1317-1336); divideTree (:858-908) with middleSplit_
+//           (:910-957) and planeSplit (:968-1004), which permute vind in place;
+//   search: findNeighbors + searchLevel (:1222-1242, :1346-1408): leaves in best-child-first
+//           depth-first order, in-leaf order of vind, a subtree skipped when its incremental
+//           float lower bound exceeds the radius; then radiusSearch's std::sort by distance
+//           alone (:1279-1288, IndexDist_Sorter :208-214), which leaves ties as the
+//           traversal and this C++ library's sort put them.
+// Without ties the order is the cell list's; with ties only this reproduces the reference.
+struct OracleKdTree {
+  struct Node {
+    int64_t left = 0, right = 0;  // leaf: its vind range
+    int feat = -1;                // internal: divfeat; -1 marks a leaf
+    float divlow = 0.f, divhigh = 0.f;
+    int child1 = -1, child2 = -1;
+  };
+  static constexpr int64_t kLeafMax = 10;
+  const float* pt[3] = {nullptr, nullptr, nullptr};
+  std::vector<int64_t> vind;
+  std::vector<Node> nodes;
+  float root_lo[3] = {0, 0, 0}, root_hi[3] = {0, 0, 0};
+  int root = -1;
+
+  float at(int64_t j, int d) const { return pt[d][j]; }
+
+  void build(int64_t n, const float* x, const float* y, const float* z) {
+    pt[0] = x; pt[1] = y; pt[2] = z;
+    vind.resize((size_t)n);
+    for (int64_t i = 0; i < n; ++i) vind[(size_t)i] = i;
+    nodes.clear();
+    root = -1;
+    if (n == 0) return;
+    for (int d = 0; d < 3; ++d) root_lo[d] = root_hi[d] = at(0, d);
+    for (int64_t k = 1; k < n; ++k)
+      for (int d = 0; d < 3; ++d) {
+        if (at(k, d) < root_lo[d]) root_lo[d] = at(k, d);
+        if (at(k, d) > root_hi[d]) root_hi[d] = at(k, d);
+      }
+    root = divide(0, n, root_lo, root_hi);
+  }
+
+  void min_max(const int64_t* ind, int64_t count, int d, float& mn, float& mx) const {
+    mn = mx = at(ind[0], d);
+    for (int64_t i = 1; i < count; ++i) {
+      const float v = at(ind[i], d);
+      if (v < mn) mn = v;
+      if (v > mx) mx = v;
+    }
+  }
+
+  // two in-place passes: [0, lim1) below cut, [lim1, lim2) equal, [lim2, count) above;
+  // "!right" ends a pass at position 0 as the unsigned-index guard does
+  void plane_split(int64_t* ind, int64_t count, int d, float cut, int64_t& lim1, int64_t& lim2) const {
+    int64_t left = 0, right = count - 1;
+    for (;;) {
+      while (left <= right && at(ind[left], d) < cut) ++left;
+      while (right && left <= right && at(ind[right], d) >= cut) --right;
+      if (left > right || !right) break;
+      std::swap(ind[left], ind[right]);
+      ++left;
+      --right;
+    }
+    lim1 = left;
+    right = count - 1;
+    for (;;) {
+      while (left <= right && at(ind[left], d) <= cut) ++left;
+      while (right && left <= right && at(ind[right], d) > cut) --right;
+      if (left > right || !right) break;
+      std::swap(ind[left], ind[right]);
+      ++left;
+      --right;
+    }
+    lim2 = left;
+  }
+
+  // the cut dimension: among those whose box span is within a factor (1 - 1e-5) of the
+  // largest, the first with the largest point spread; the cut at the box middle clamped
+  // to the points' range; the split index nearest the middle that keeps equal values
+  // together where it can
+  void middle_split(int64_t* ind, int64_t count, int64_t& index, int& feat, float& cut, const float lo[3],
+                    const float hi[3]) const {
+    const float eps = 0.00001f;
+    float max_span = hi[0] - lo[0];
+    for (int d = 1; d < 3; ++d)
+      if (hi[d] - lo[d] > max_span) max_span = hi[d] - lo[d];
+    float max_spread = -1;
+    feat = 0;
+    for (int d = 0; d < 3; ++d) {
+      if (hi[d] - lo[d] > (1 - eps) * max_span) {
+        float mn, mx;
+        min_max(ind, count, d, mn, mx);
+        if (mx - mn > max_spread) {
+          feat = d;
+          max_spread = mx - mn;
+        }
+      }
+    }
+    const float mid = (lo[feat] + hi[feat]) / 2;
+    float mn, mx;
+    min_max(ind, count, feat, mn, mx);
+    cut = mid < mn ? mn : (mid > mx ? mx : mid);
+    int64_t lim1, lim2;
+    plane_split(ind, count, feat, cut, lim1, lim2);
+    index = lim1 > count / 2 ? lim1 : (lim2 < count / 2 ? lim2 : count / 2);
+  }
+
+  // returns the node; lo/hi come in as the box handed down (the parent's, cut at the
+  // split value) and leave as the actual box of the node's points
+  int divide(int64_t left, int64_t right, float lo[3], float hi[3]) {
+    const int id = (int)nodes.size();
+    nodes.emplace_back();
+    if (right - left <= kLeafMax) {
+      for (int d = 0; d < 3; ++d) lo[d] = hi[d] = at(vind[(size_t)left], d);
+      for (int64_t k = left + 1; k < right; ++k)
+        for (int d = 0; d < 3; ++d) {
+          const float v = at(vind[(size_t)k], d);
+          if (lo[d] > v) lo[d] = v;
+          if (hi[d] < v) hi[d] = v;
+        }
+      nodes[id].left = left;
+      nodes[id].right = right;
+      return id;
+    }
+    int64_t idx;
+    int feat;
+    float cut;
+    middle_split(vind.data() + left, right - left, idx, feat, cut, lo, hi);
+    float llo[3], lhi[3], rlo[3], rhi[3];
+    for (int d = 0; d < 3; ++d) { llo[d] = rlo[d] = lo[d]; lhi[d] = rhi[d] = hi[d]; }
+    lhi[feat] = cut;
+    const int c1 = divide(left, left + idx, llo, lhi);
+    rlo[feat] = cut;
+    const int c2 = divide(left + idx, right, rlo, rhi);
+    Node& nd = nodes[id];
+    nd.feat = feat;
+    nd.child1 = c1;
+    nd.child2 = c2;
+    nd.divlow = lhi[feat];
+    nd.divhigh = rlo[feat];
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(llo[d], rlo[d]);
+      hi[d] = std::max(lhi[d], rhi[d]);
+    }
+    return id;
+  }
+
+  void level(const float q[3], float radius, int node, float mindistsq, float dists[3],
+             std::vector<std::pair<int64_t, float>>& out) const {
+    const Node& nd = nodes[node];
+    if (nd.feat < 0) {
+      for (int64_t i = nd.left; i < nd.right; ++i) {
+        const int64_t j = vind[(size_t)i];
+        float dist = 0.f;
+        for (int d = 0; d < 3; ++d) {
+          const float diff = q[d] - at(j, d);
+          dist += diff * diff;
+        }
+        if (dist < radius) out.push_back({j, dist});
+      }
+      return;
+    }
+    const int f = nd.feat;
+    const float val = q[f];
+    const float diff1 = val - nd.divlow, diff2 = val - nd.divhigh;
+    int best, other;
+    float cut_dist;
+    if (diff1 + diff2 < 0) {
+      best = nd.child1;
+      other = nd.child2;
+      cut_dist = (val - nd.divhigh) * (val - nd.divhigh);
+    } else {
+      best = nd.child2;
+      other = nd.child1;
+      cut_dist = (val - nd.divlow) * (val - nd.divlow);
+    }
+    level(q, radius, best, mindistsq, dists, out);
+    const float dst = dists[f];
+    mindistsq = mindistsq + cut_dist - dst;
+    dists[f] = cut_dist;
+    if (mindistsq * 1.0f <= radius) level(q, radius, other, mindistsq, dists, out);
+    dists[f] = dst;
+  }
+
+  struct ByDistance {
+    bool operator()(const std::pair<int64_t, float>& a, const std::pair<int64_t, float>& b) const {
+      return a.second < b.second;
+    }
+  };
+
+  // (d2, j) in the reference's visiting order
+  void search(float qx, float qy, float qz, float radius, std::vector<std::pair<int64_t, float>>& scratch,
+              std::vector<std::pair<float, int>>& out) const {
+    scratch.clear();
+    out.clear();
+    if (root < 0) return;
+    const float q[3] = {qx, qy, qz};
+    float dists[3] = {0.f, 0.f, 0.f};
+    float distsq = 0.f;
+    for (int d = 0; d < 3; ++d) {
+      if (q[d] < root_lo[d]) {
+        dists[d] = (q[d] - root_lo[d]) * (q[d] - root_lo[d]);
+        distsq += dists[d];
+      }
+      if (q[d] > root_hi[d]) {
+        dists[d] = (q[d] - root_hi[d]) * (q[d] - root_hi[d]);
+        distsq += dists[d];
+      }
+    }
+    level(q, radius, root, distsq, dists, scratch);
+    std::sort(scratch.begin(), scratch.end(), ByDistance());
+    for (const auto& m : scratch) out.push_back({m.second, (int)m.first});
+  }
+};
+
+// the neighbour search of both operators: the cell list (ties in increasing index) or the
+// restated kd-tree (ties in the reference's order)
+struct OracleSearch {
+  bool kd = false;
+  OracleCells cells;
+  OracleKdTree tree;
+  mutable std::vector<std::pair<int64_t, float>> scratch;
+
+  void build(int n, const float* x, const float* y, const float* z, double rmax, int tie_order) {
+    kd = tie_order != 0;
+    if (kd) tree.build(n, x, y, z);
+    else cells.build(n, x, y, z, rmax);
+  }
+  void search(float qx, float qy, float qz, float thr, const float* x, const float* y, const float* z,
+              std::vector<std::pair<float, int>>& out) const {
+    if (kd) tree.search(qx, qy, qz, thr, scratch, out);
+    else cells.search(qx, qy, qz, thr, x, y, z, out);
+  }
+};
+
 // get_core_coefficient<float> (Core.h:32-35): CoreType gaussian = 0, compactg = 1
 float core_coefficient(int core) {
   return core == 0 ? (float)(1.0 / (M_PI * std::sqrt(M_PI))) : (float)0.23873241;
@@ -1235,9 +1474,10 @@ float core_coefficient(int core) {
 
 // split_elongated<float> (Split.h:44-270).  Arrays have room for cap particles; the split
 // ones are halved and moved in place and their children appended at [n, n + nsplit).
-// Returns nsplit, or -1 when cap is too small or the arguments are bad.
+// tie_order 0 visits equal-distance neighbours in increasing index, 1 in the reference's
+// kd-tree order.  Returns nsplit, or -1 when cap is too small or the arguments are bad.
 extern "C" int o3o_split_elongated(int n, int cap, float* x, float* y, float* z, float* r, float* elong, float* sx,
-                                   float* sy, float* sz, int core, float overlap, float threshold) {
+                                   float* sy, float* sz, int core, float overlap, float threshold, int tie_order) {
   if (n < 0 || cap < n) return -1;
   int m = 0;
   double rmax = 0.0;
@@ -1251,8 +1491,8 @@ extern "C" int o3o_split_elongated(int n, int cap, float* x, float* y, float* z,
   if (m == 0) return 0;
   // the search runs on the positions before any split (the kd-tree's copy)
   const std::vector<float> px(x, x + n), py(y, y + n), pz(z, z + n);
-  OracleCells cells;
-  cells.build(n, px.data(), py.data(), pz.data(), rmax);
+  OracleSearch cells;
+  cells.build(n, px.data(), py.data(), pz.data(), rmax, tie_order);
   const float coef = core_coefficient(core);
   std::vector<std::pair<float, int>> matches;
   int k = n;
@@ -1323,9 +1563,10 @@ extern "C" int o3o_split_elongated(int n, int cap, float* x, float* y, float* z,
 }
 
 // merge_close_particles<float> (Merge.h:45-218): greedy merge in index order, then the
-// survivors compacted in place.  Returns the number removed, or -1 on bad arguments.
+// survivors compacted in place; tie_order as for the split.  Returns the number removed, or
+// -1 on bad arguments.
 extern "C" int o3o_merge_close_particles(int n, float* x, float* y, float* z, float* sx, float* sy, float* sz,
-                                         float* r, float overlap, float threshold, int adapt_radii) {
+                                         float* r, float overlap, float threshold, int adapt_radii, int tie_order) {
   if (n < 0) return -1;
   if (n == 0) return 0;
   const float initial_thresh = 0.5f;
@@ -1336,8 +1577,8 @@ extern "C" int o3o_merge_close_particles(int n, float* x, float* y, float* z, fl
   double rmax = 0.0;
   for (int i = 0; i < n; ++i) rmax = std::max(rmax, (double)((r[i] / overlap) * initial_thresh));
   const std::vector<float> px(x, x + n), py(y, y + n), pz(z, z + n);
-  OracleCells cells;
-  cells.build(n, px.data(), py.data(), pz.data(), rmax);
+  OracleSearch cells;
+  cells.build(n, px.data(), py.data(), pz.data(), rmax, tie_order);
   std::vector<char> erase((size_t)n, 0);
   std::vector<std::pair<float, int>> matches;
   for (int i = 0; i < n; ++i) {

@@ -371,10 +371,20 @@ def _splitmerge_lib(use_ref):
     return _ref["splitmerge"], "ref_"
 
 
-def split_elongated(x, s, r, elong, core=0, overlap=1.5, threshold=1.2, use_ref=False):
+def _tie_args(use_ref, tie_order):
+    """The oracle's trailing tie_order argument: 0 visits equal-distance neighbours in
+    increasing index (the kernels' order), 1 in the order of the restated nanoflann kd-tree
+    (the reference's).  The reference build has no such argument."""
+    if tie_order not in ("index", "kdtree"):
+        raise ValueError("tie_order must be 'index' or 'kdtree'")
+    return () if use_ref else (ctypes.c_int(int(tie_order == "kdtree")),)
+
+
+def split_elongated(x, s, r, elong, core=0, overlap=1.5, threshold=1.2, use_ref=False, tie_order="index"):
     """split_elongated<float> (Split.h:44-270) on x[3, n], s[3, n], r[n], elong[n]
     (core 0 = gaussian, 1 = compactg, Core.h:27).  Returns new arrays
-    (x, s, r, elong) of n + nsplit particles (children appended in index order) and nsplit."""
+    (x, s, r, elong) of n + nsplit particles (children appended in index order) and nsplit.
+    tie_order: see _tie_args."""
     n = x.shape[1]
     m = int(np.count_nonzero(np.asarray(elong, np.float32) > np.float32(threshold)))
     cap = n + m
@@ -386,16 +396,19 @@ def split_elongated(x, s, r, elong, core=0, overlap=1.5, threshold=1.2, use_ref=
     L, pre = _splitmerge_lib(use_ref)
     rc = getattr(L, pre + "split_elongated")(
         ctypes.c_int(n), ctypes.c_int(cap), _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(rs), _p(es), _p(ss[0]), _p(ss[1]),
-        _p(ss[2]), ctypes.c_int(core), ctypes.c_float(overlap), ctypes.c_float(threshold))
+        _p(ss[2]), ctypes.c_int(core), ctypes.c_float(overlap), ctypes.c_float(threshold),
+        *_tie_args(use_ref, tie_order))
     if rc < 0:
         raise RuntimeError("split_elongated failed")
     assert rc == m
     return xs, ss, rs, es, rc
 
 
-def merge_close_particles(x, s, r, overlap=1.5, threshold=0.2, adapt_radii=False, use_ref=False):
+def merge_close_particles(x, s, r, overlap=1.5, threshold=0.2, adapt_radii=False, use_ref=False,
+                          tie_order="index"):
     """merge_close_particles<float> (Merge.h:45-218) on x[3, n], s[3, n], r[n].  Returns
-    new arrays (x, s, r) of the survivors in their original order and the number removed."""
+    new arrays (x, s, r) of the survivors in their original order and the number removed.
+    tie_order: see _tie_args."""
     n = x.shape[1]
     xs = np.array(x, np.float32, order="C", copy=True)
     ss = np.array(s, np.float32, order="C", copy=True)
@@ -403,7 +416,8 @@ def merge_close_particles(x, s, r, overlap=1.5, threshold=0.2, adapt_radii=False
     L, pre = _splitmerge_lib(use_ref)
     rc = getattr(L, pre + "merge_close_particles")(
         ctypes.c_int(n), _p(xs[0]), _p(xs[1]), _p(xs[2]), _p(ss[0]), _p(ss[1]), _p(ss[2]), _p(rs),
-        ctypes.c_float(overlap), ctypes.c_float(threshold), ctypes.c_int(int(bool(adapt_radii))))
+        ctypes.c_float(overlap), ctypes.c_float(threshold), ctypes.c_int(int(bool(adapt_radii))),
+        *_tie_args(use_ref, tie_order))
     if rc < 0:
         raise RuntimeError("merge_close_particles failed")
     k = n - rc

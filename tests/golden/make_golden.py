@@ -109,18 +109,24 @@ def write_splitmerge():
 
 
 def write_splitmerge_tied():
-    """Split of an unjittered 12^3 lattice by the reference's Split.h.  Every particle has
-    neighbours at exactly equal float distances, so the reference's visiting order of those
-    ties comes from its nanoflann kd-tree and std::sort, not from the distances."""
+    """Inputs with neighbours at exactly equal float distances, where the reference's
+    visiting order of the ties comes from its nanoflann kd-tree and std::sort: the split of
+    an unjittered 12^3 lattice (Split.h) and the merge of a lattice with duplicated particles
+    (Merge.h)."""
     x, s, r, e = W.lattice_particles(k=12, seed=40, jitter=0.0)
     out = {}
     for core in (0, 1):
         xs, ss, rs, es, m = O.split_elongated(x, s, r, e, core, 1.5, 1.2, use_ref=True)
         out.update({"split%d_x" % core: xs, "split%d_s" % core: ss, "split%d_r" % core: rs,
                     "split%d_e" % core: es})
+    xd, sd, rd, _ = W.duplicated_particles(k=12, seed=41, every=5, seed_dup=2)
+    for name, thr in (("merge_vrm", 0.2), ("merge_core", 0.02)):
+        xm, sm, rm, nrem = O.merge_close_particles(xd, sd, rd, 1.5, thr, False, use_ref=True)
+        out.update({name + "_x": xm, name + "_s": sm, name + "_r": rm})
     _save("splitmerge_tied.npz", {"pinned": True, "overlap": 1.5, "split_threshold": 1.2,
-                                  "source": "reference Split.h with lib/nanoflann"},
-          x_in=x, s_in=s, r_in=r, e_in=e, **out)
+                                  "merge": {"merge_vrm": 0.2, "merge_core": 0.02},
+                                  "source": "reference Split.h / Merge.h with lib/nanoflann"},
+          x_in=x, s_in=s, r_in=r, e_in=e, xd_in=xd, sd_in=sd, rd_in=rd, **out)
 
 
 def main():

@@ -308,16 +308,41 @@ def test_oracle_split_merge_bit_exact_vs_reference(scale):
         pytest.skip("oracle/_ref not built (reference sources absent)")
     x, s, r, e = W.lattice_particles(k=30, seed=31, elong_scale=scale)
     for core in (0, 1):
-        a = O.split_elongated(x, s, r, e, core, 1.5, 1.2)
         b = O.split_elongated(x, s, r, e, core, 1.5, 1.2, use_ref=True)
-        assert a[4] == b[4] > 0
-        assert all(_bits(u, v) for u, v in zip(a[:4], b[:4]))
+        for order in ("index", "kdtree"):
+            a = O.split_elongated(x, s, r, e, core, 1.5, 1.2, tie_order=order)
+            assert a[4] == b[4] > 0
+            assert all(_bits(u, v) for u, v in zip(a[:4], b[:4]))
     for thr in (0.2, 0.02):
         for adapt in (False, True):
-            a = O.merge_close_particles(x, s, r, 1.5, thr, adapt)
             b = O.merge_close_particles(x, s, r, 1.5, thr, adapt, use_ref=True)
-            assert a[3] == b[3] > 0
-            assert all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
+            for order in ("index", "kdtree"):
+                a = O.merge_close_particles(x, s, r, 1.5, thr, adapt, tie_order=order)
+                assert a[3] == b[3] > 0
+                assert all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
+
+
+def test_oracle_kdtree_order_bit_exact_vs_reference_on_ties():
+    """The kd-tree restatement against the reference build itself on larger tied inputs:
+    an unjittered 20^3 lattice (split, both cores) and 8,000 lattice particles with 800
+    exact duplicates (split and merge, both thresholds, fixed and adaptive radii)."""
+    if not O.ref_splitmerge_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    x, s, r, e = W.lattice_particles(k=20, seed=40, jitter=0.0)
+    for core in (0, 1):
+        a = O.split_elongated(x, s, r, e, core, 1.5, 1.2, tie_order="kdtree")
+        b = O.split_elongated(x, s, r, e, core, 1.5, 1.2, use_ref=True)
+        assert a[4] == b[4] > 0 and all(_bits(u, v) for u, v in zip(a[:4], b[:4]))
+    xd, sd, rd, ed = W.duplicated_particles(k=20, seed=40, every=10, seed_dup=1)
+    for core in (0, 1):
+        a = O.split_elongated(xd, sd, rd, ed, core, 1.5, 1.2, tie_order="kdtree")
+        b = O.split_elongated(xd, sd, rd, ed, core, 1.5, 1.2, use_ref=True)
+        assert a[4] == b[4] > 0 and all(_bits(u, v) for u, v in zip(a[:4], b[:4]))
+    for thr in (0.2, 0.02):
+        for adapt in (False, True):
+            a = O.merge_close_particles(xd, sd, rd, 1.5, thr, adapt, tie_order="kdtree")
+            b = O.merge_close_particles(xd, sd, rd, 1.5, thr, adapt, use_ref=True)
+            assert a[3] == b[3] > 0 and all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
 
 
 def _has_equal_distance_neighbours(x, r, overlap=1.5):
@@ -348,6 +373,33 @@ def test_oracle_split_tied_lattice_within_tolerance():
             assert _bits(got[k], want[k])
         ds = np.abs(got[1].astype(np.float64) - want[1]).max()
         assert ds <= 1e-7 * np.abs(want[1]).max(), ds
+
+
+def test_oracle_kdtree_order_matches_tied_fixture():
+    """With tie_order="kdtree" the oracle visits neighbours in the order of its restatement
+    of the reference's nanoflann kd-tree and std::sort.  On the tied inputs it then
+    reproduces the reference bit for bit: the split of the unjittered lattice (both cores)
+    and the merge of duplicated particles (both thresholds).  The index-order merge of the
+    duplicates differs from the reference at threshold 0.2 (another partner merges first),
+    while the count and the total strength agree."""
+    d, meta = _gold("splitmerge_tied.npz")
+    x, s, r, e = d["x_in"], d["s_in"], d["r_in"], d["e_in"]
+    for core in (0, 1):
+        got = O.split_elongated(x, s, r, e, core, meta["overlap"], meta["split_threshold"], tie_order="kdtree")
+        for k, v in zip("xsre", got[:4]):
+            assert _bits(v, d["split%d_%s" % (core, k)])
+    xd, sd, rd = d["xd_in"], d["sd_in"], d["rd_in"]
+    for name, thr in meta["merge"].items():
+        want = [d["%s_%s" % (name, k)] for k in "xsr"]
+        got = O.merge_close_particles(xd, sd, rd, meta["overlap"], thr, False, tie_order="kdtree")
+        assert got[3] == xd.shape[1] - want[0].shape[1] > 0
+        for k in range(3):
+            assert _bits(got[k], want[k])
+        idx = O.merge_close_particles(xd, sd, rd, meta["overlap"], thr, False)
+        assert idx[3] == got[3]
+        assert np.allclose(idx[1].astype(np.float64).sum(1), want[1].astype(np.float64).sum(1), rtol=0, atol=1e-7)
+    idx = O.merge_close_particles(xd, sd, rd, meta["overlap"], 0.2, False)
+    assert not all(_bits(a, d["merge_vrm_" + k]) for a, k in zip(idx[:3], "xsr"))
 
 
 def test_oracle_split_conserves_moments():

@@ -82,6 +82,24 @@ def test_split_tied_lattice(core):
     assert np.abs(got[1].astype(np.float64) - ref_s).max() <= 1e-7 * np.abs(ref_s).max()
 
 
+@pytest.mark.parametrize("name,thr", [("merge_vrm", 0.2), ("merge_core", 0.02)])
+def test_merge_duplicated_particles(name, thr):
+    """Lattice particles plus exact copies of a fifth of them.  The kernel and the oracle
+    take equal-distance partners in increasing index: bit-identical.  The reference takes
+    them in its kd-tree order.  It removes the same number and keeps the same total
+    strength, but at threshold 0.2 it keeps other members of some coincident pairs."""
+    d = np.load(os.path.join(os.path.dirname(GOLDEN), "splitmerge_tied.npz"))
+    xd, sd, rd = d["xd_in"], d["sd_in"], d["rd_in"]
+    got = _merge_gpu(xd, sd, rd, 1.5, thr, False)
+    want = O.merge_close_particles(xd, sd, rd, 1.5, thr, False)
+    assert got[3] == want[3] > 0
+    for a, b in zip(got[:3], want[:3]):
+        _bits_equal(a, b)
+    ref_s = d[name + "_s"]
+    assert got[3] == xd.shape[1] - ref_s.shape[1]
+    assert np.allclose(got[1].astype(np.float64).sum(1), ref_s.astype(np.float64).sum(1), rtol=0, atol=1e-7)
+
+
 @pytest.mark.parametrize("k,scale,core", [(40, 0.12, 0), (40, 0.05, 1), (100, 0.12, 0)])
 def test_split_vs_oracle(k, scale, core):
     """64,000 and 1,000,000 particles; with the 0.12 tail 19 % split and the dependency
