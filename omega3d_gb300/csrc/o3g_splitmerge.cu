@@ -51,10 +51,12 @@
 #include "o3g_common.cuh"
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 #include <cub/device/device_segmented_sort.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -1008,6 +1010,32 @@ int32_t build_cells(Scratch& sc, int n, const float* x, const float* y, const fl
   return O3G_OK;
 }
 
+struct Add64 {
+  __host__ __device__ long long operator()(long long a, long long b) const { return a + b; }
+};
+
+// the number of matches over all queries, summed in 64 bits: the match lists are indexed
+// by int offsets (an int exclusive sum of cnt), so a total above INT_MAX is refused before
+// anything is allocated or written
+int32_t match_total(Scratch& sc, const int* cnt, int count, int* total, const char* what) {
+  long long* sum = nullptr;
+  O3G_TRY(sc.get(&sum, 1));
+  size_t tb = 0;
+  O3G_CUDA_TRY(cub::DeviceReduce::Reduce(nullptr, tb, cnt, sum, count, Add64(), 0ll, sc.st));
+  void* tmp = nullptr;
+  O3G_TRY(sc.get((char**)&tmp, tb));
+  O3G_CUDA_TRY(cub::DeviceReduce::Reduce(tmp, tb, cnt, sum, count, Add64(), 0ll, sc.st));
+  long long h = 0;
+  O3G_CUDA_TRY(cudaMemcpyAsync(&h, sum, sizeof(h), cudaMemcpyDeviceToHost, sc.st));
+  O3G_CUDA_TRY(cudaStreamSynchronize(sc.st));
+  if (h < 0 || h > (long long)INT_MAX) {
+    set_error(what);
+    return O3G_ERR_INVALID_ARG;
+  }
+  *total = (int)h;
+  return O3G_OK;
+}
+
 int32_t sort_matches(Scratch& sc, uint64_t* keys, uint64_t** sorted, int total, int nseg, const int* off) {
   uint64_t* out = nullptr;
   O3G_TRY(sc.get(&out, total));
@@ -1070,7 +1098,8 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   note_launch(1);
   O3G_TRY(exclusive_sum(sc, cnt, off, m + 1));
   int total = 0;
-  O3G_TRY(read_int(off + m, &total, st));
+  O3G_TRY(match_total(sc, cnt, m, &total,
+                      "o3g_split_elongated: more than 2^31 - 1 neighbour matches in all (coincident particles?)"));
   uint64_t *ukeys = nullptr, *keys = nullptr;
   float4* terms = nullptr;
   int *code = nullptr, *dep = nullptr, *ndep = nullptr;
@@ -1224,7 +1253,8 @@ int32_t merge_run(int n, float* x, float* y, float* z, float* sx, float* sy, flo
   note_launch(1);
   O3G_TRY(exclusive_sum(sc, cnt, off, n + 1));
   int total = 0;
-  O3G_TRY(read_int(off + n, &total, st));
+  O3G_TRY(match_total(sc, cnt, n, &total,
+                      "o3g_merge_close_particles: more than 2^31 - 1 neighbour matches in all (coincident particles?)"));
   *nremoved = 0;
   if (total == 0) return O3G_OK;
   uint64_t *keys = nullptr, *sorted = nullptr;

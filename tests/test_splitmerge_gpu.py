@@ -191,6 +191,36 @@ def test_split_merge_edges():
     _bits_equal(got[0], xf)
 
 
+def test_too_many_matches_refused():
+    """48,000 coincident particles: every one matches every other, 2.3e9 matches in all,
+    more than the int offsets of the match lists can index.  Both operators refuse with
+    INVALID_ARG before writing anything, and the arrays come back unchanged."""
+    G = _g()
+    from omega3d_gb300._lib import O3GError
+    n = 48000
+    x = np.full((3, n), 0.25, np.float32)
+    s = np.zeros((3, n), np.float32)
+    s[0] = 1e-4
+    r = np.full(n, 0.015, np.float32)
+    e = np.full(n, 2.0, np.float32)
+    tx, ts, tr, te = _dev(x), _dev(s), _dev(r), _dev(e)
+    for call in (lambda: G.split_elongated(tx, ts, tr, te), lambda: G.merge_close_particles(tx, ts, tr)):
+        with pytest.raises(O3GError, match="2\\^31") as ex:
+            call()
+        assert ex.value.status == 1
+    torch.cuda.synchronize()
+    for a, b in ((tx, x), (ts, s), (tr, r), (te, e)):
+        _bits_equal(a.cpu().numpy(), b)
+    # the library stays usable
+    xs, ss, rs, es, m = _split_gpu(*_small_lattice(), "gaussian")
+    assert m > 0
+
+
+def _small_lattice():
+    from omega3d_gb300 import workloads as W
+    return W.lattice_particles(k=8, seed=26)
+
+
 def test_split_merge_deterministic():
     from omega3d_gb300 import workloads as W
     x, s, r, e = W.lattice_particles(k=40, seed=26)
