@@ -605,14 +605,32 @@ def bench_bem_cpu(W):
                         "sample": "numpy FP64 LU solve of the 4-level sphere's system, scaled by n^3 to n"}}
 
 
-def bench_splitmerge(args, G, torch, W, reps=3):
+def cpu_splitmerge(x, s, r, e):
+    """The oracle port of Split.h / Merge.h on the host, single thread (the reference's loops
+    are sequential), run twice: with the restated nanoflann kd-tree, the reference's own
+    search structure, timed as the CPU baseline; and with the cell list, which takes
+    equal-distance neighbours in increasing index like the kernels, for the bit-for-bit
+    check.  Returns {order: (split result, split ms, merge result, merge ms)}."""
+    import oracle as O
+    res = {}
+    for order in ("kdtree", "index"):
+        t0 = time.perf_counter()
+        sp = O.split_elongated(x, s, r, e, 0, 1.5, 1.2, tie_order=order)
+        t_sp = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        mg = O.merge_close_particles(x, s, r, 1.5, 0.2, False, tie_order=order)
+        t_mg = (time.perf_counter() - t0) * 1e3
+        res[order] = (sp, t_sp, mg, t_mg)
+    return res
+
+
+def bench_splitmerge(args, G, torch, W, reps=3, k=100):
     """Particle split (Split.h:44-270) and merge (Merge.h:45-218) of 1,000,000 particles on
     a jittered lattice (19 % elongated past the split threshold, 9 % with a neighbour within
     half a separation).  Each call is timed end to end (both wait for their result) on fresh
-    device copies; the oracle port of the reference's sequential loops runs once on the host
-    for the CPU figure and to confirm the device results bit for bit."""
-    import oracle as O
-    x, s, r, e = W.lattice_particles(k=100, seed=41)
+    device copies; the oracle port of the reference's sequential loops runs on the host for
+    the CPU figure and to confirm the device results bit for bit (cpu_splitmerge)."""
+    x, s, r, e = W.lattice_particles(k=k, seed=41)
     n = x.shape[1]
     dev = torch.device("cuda", torch.cuda.current_device())
     X, S, R, E = (torch.from_numpy(a).to(dev) for a in (x, s, r, e))
@@ -633,26 +651,29 @@ def bench_splitmerge(args, G, torch, W, reps=3):
 
     sp_ms, sp = timed(lambda a, b, c, d: G.split_elongated(a, b, c, d, "gaussian", 1.5, 1.2))
     mg_ms, mg = timed(lambda a, b, c, d: G.merge_close_particles(a, b, c, 1.5, 0.2, False))
-    t0 = time.perf_counter()
-    osp = O.split_elongated(x, s, r, e, 0, 1.5, 1.2)
-    cpu_sp = (time.perf_counter() - t0) * 1e3
-    t0 = time.perf_counter()
-    omg = O.merge_close_particles(x, s, r, 1.5, 0.2, False)
-    cpu_mg = (time.perf_counter() - t0) * 1e3
+    cpu = cpu_splitmerge(x, s, r, e)
+    osp, cell_sp, omg, cell_mg = cpu["index"]
+    _, cpu_sp, _, cpu_mg = cpu["kdtree"]
 
     def same(dev_arrs, host_arrs):
         return all(np.array_equal(a.cpu().numpy().view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
                    for a, b in zip(dev_arrs, host_arrs))
 
+    kd_sp, kd_mg = cpu["kdtree"][0], cpu["kdtree"][2]
     out["split"] = {"ms": sp_ms, "particles_per_s": n / (sp_ms * 1e-3), "nsplit": sp[4],
-                    "cpu_port_ms": cpu_sp, "speedup_vs_cpu_port": cpu_sp / sp_ms,
-                    "bit_identical_to_port": bool(sp[4] == osp[4] and same(sp[:4], osp[:4]))}
+                    "cpu_port_ms": cpu_sp, "speedup_vs_cpu_port": cpu_sp / sp_ms, "cpu_port_cell_list_ms": cell_sp,
+                    "bit_identical_to_port": bool(sp[4] == osp[4] and same(sp[:4], osp[:4])),
+                    "port_kdtree_equals_cell_list": bool(kd_sp[4] == osp[4] and all(
+                        np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in zip(kd_sp[:4], osp[:4])))}
     out["merge"] = {"ms": mg_ms, "particles_per_s": n / (mg_ms * 1e-3), "nremoved": mg[3],
-                    "cpu_port_ms": cpu_mg, "speedup_vs_cpu_port": cpu_mg / mg_ms,
-                    "bit_identical_to_port": bool(mg[3] == omg[3] and same(mg[:3], omg[:3]))}
+                    "cpu_port_ms": cpu_mg, "speedup_vs_cpu_port": cpu_mg / mg_ms, "cpu_port_cell_list_ms": cell_mg,
+                    "bit_identical_to_port": bool(mg[3] == omg[3] and same(mg[:3], omg[:3])),
+                    "port_kdtree_equals_cell_list": bool(kd_mg[3] == omg[3] and all(
+                        np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in zip(kd_mg[:3], omg[:3])))}
     out["cpu_port"] = {"cores": 1, "kind": "port",
                        "sample": "the whole 1,000,000-particle operator, single thread (the reference's loops are "
-                                 "sequential)"}
+                                 "sequential), neighbours found with the restated nanoflann kd-tree the reference "
+                                 "uses; cpu_port_cell_list_ms is the same port with the cell list"}
     return out
 
 
