@@ -322,6 +322,30 @@ def test_oracle_split_merge_bit_exact_vs_reference(scale):
                 assert all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
 
 
+@pytest.mark.parametrize("overlap", [1.0, 1.5, 2.0])
+def test_oracle_split_merge_mixed_radii_vs_reference(overlap):
+    """Particles of different core radii (uniform lattice radius times U[0.7, 1.3]), so
+    every r[i] * r[iother] (Split.h:157), min(r[iother], r[i]) and r[iother]-based test
+    (Merge.h:137-147) sees unequal radii; several overlaps and thresholds, fixed and
+    adaptive radii, both visiting orders: bit for bit against the reference build."""
+    if not O.ref_splitmerge_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    x, s, r, e = W.lattice_particles(k=16, seed=34, overlap=overlap, elong_scale=0.2)
+    r = (r * np.random.default_rng(35).uniform(0.7, 1.3, r.size)).astype(np.float32)
+    for core in (0, 1):
+        for thr in (1.05, 1.5):
+            b = O.split_elongated(x, s, r, e, core, overlap, thr, use_ref=True)
+            for order in ("index", "kdtree"):
+                a = O.split_elongated(x, s, r, e, core, overlap, thr, tie_order=order)
+                assert a[4] == b[4] > 0 and all(_bits(u, v) for u, v in zip(a[:4], b[:4]))
+    for thr in (0.05, 0.2, 0.5):
+        for adapt in (False, True):
+            b = O.merge_close_particles(x, s, r, overlap, thr, adapt, use_ref=True)
+            for order in ("index", "kdtree"):
+                a = O.merge_close_particles(x, s, r, overlap, thr, adapt, tie_order=order)
+                assert a[3] == b[3] > 0 and all(_bits(u, v) for u, v in zip(a[:3], b[:3]))
+
+
 def test_oracle_kdtree_order_bit_exact_vs_reference_on_ties():
     """The kd-tree restatement against the reference build itself on larger tied inputs:
     an unjittered 20^3 lattice (split, both cores) and 8,000 lattice particles with 800

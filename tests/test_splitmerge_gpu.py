@@ -113,6 +113,28 @@ def test_split_vs_oracle(k, scale, core):
         _bits_equal(a, b)
 
 
+@pytest.mark.parametrize("overlap", [1.0, 2.0])
+def test_split_merge_mixed_radii_vs_oracle(overlap):
+    """Unequal core radii (lattice radius times U[0.7, 1.3]) and other overlaps and
+    thresholds: the cell size follows the largest search radius, every match test and
+    weight the pair's own radii."""
+    from omega3d_gb300 import workloads as W
+    x, s, r, e = W.lattice_particles(k=16, seed=34, overlap=overlap, elong_scale=0.2)
+    r = (r * np.random.default_rng(35).uniform(0.7, 1.3, r.size)).astype(np.float32)
+    for core in (0, 1):
+        want = O.split_elongated(x, s, r, e, core, overlap, 1.05)
+        got = _split_gpu(x, s, r, e, ["gaussian", "compactg"][core], overlap, 1.05)
+        assert got[4] == want[4] > 0
+        for a, b in zip(got[:4], want[:4]):
+            _bits_equal(a, b)
+    for thr, adapt in ((0.05, False), (0.5, True)):
+        want = O.merge_close_particles(x, s, r, overlap, thr, adapt)
+        got = _merge_gpu(x, s, r, overlap, thr, adapt)
+        assert got[3] == want[3] > 0
+        for a, b in zip(got[:3], want[:3]):
+            _bits_equal(a, b)
+
+
 def test_split_every_particle_elongated():
     """Every particle split: the longest dependency chain the operator can have here."""
     from omega3d_gb300 import workloads as W
