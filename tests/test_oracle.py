@@ -99,15 +99,21 @@ def test_oracle_bit_exact_vs_reference_pairs(core, prec):
 
 
 @pytest.mark.parametrize("core", list(O.REF_CORES))
-def test_oracle_bit_exact_vs_reference_panels(core):
+@pytest.mark.parametrize("shape", [(2.0, 2.0, 2.0), (2.0, 1.0, 0.5)])
+def test_oracle_bit_exact_vs_reference_panels(core, shape):
+    """A sphere and an elongated ovoid (panels of unequal area and aspect), with targets in
+    a shell and just outside the surface, where the adaptive kernels subdivide."""
     _need_ref(core)
-    nodes, idx = O.generate_ovoid(1, 2.0, 2.0, 2.0)
+    nodes, idx = O.generate_ovoid(1, *shape)
     x1, x2, nm, area = O.compute_bases(nodes, idx)
     rng = np.random.default_rng(5)
     ts = O.sheet_to_panel_strength(rng.normal(size=80).astype(np.float32), rng.normal(size=80).astype(np.float32),
                                    x1, x2, area)
     sss = rng.normal(size=80).astype(np.float32)
     tx, ps, _ = W.shell_particles(50, seed=23, rin=1.01, rout=1.3)
+    near = (nodes[:, :30] * np.float32(1.03)).astype(np.float32)
+    tx = np.ascontiguousarray(np.concatenate([tx, near], axis=1))
+    ps = np.ascontiguousarray(np.concatenate([ps, (rng.normal(size=(3, 30)) * 1e-3).astype(np.float32)], axis=1))
     for prec in (0, 1, 2):
         a = O.panels_affect_points(nodes, idx, area, ts, tx, sss, True, core, prec)
         b = O.panels_affect_points(nodes, idx, area, ts, tx, sss, True, core, prec, use_ref=True)
