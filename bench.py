@@ -677,6 +677,24 @@ def bench_splitmerge(args, G, torch, W, reps=3, k=100):
     return out
 
 
+def guarded(fn):
+    """Runs one secondary section of the line.  An exception there is reported in the line as
+    that section's {"error": ...} instead of losing the headline."""
+    try:
+        return fn()
+    except Exception as ex:
+        return {"error": "%s: %s" % (type(ex).__name__, str(ex)[:500])}
+
+
+def bem_section(args, G, torch, W, rank):
+    bem = bench_bem(args, G, torch, W, fp64=not args.skip_bem_fp64)
+    if rank == 0:
+        bem["cpu_baseline_nunk2"] = cpu = bench_bem_cpu(W)
+        g = bem["nunk2"]["gmres"]["total_ms_with_rhs_and_assembly"] * 1e-3
+        cpu["gpu_gmres_speedup"] = cpu["total_s"] / g
+    return bem
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -841,23 +859,19 @@ def run_ours(args):
 
     bem = None
     if not args.skip_bem:
-        bem = bench_bem(args, G, torch, W, fp64=not args.skip_bem_fp64)
-        if rank == 0:
-            bem["cpu_baseline_nunk2"] = cpu = bench_bem_cpu(W)
-            g = bem["nunk2"]["gmres"]["total_ms_with_rhs_and_assembly"] * 1e-3
-            cpu["gpu_gmres_speedup"] = cpu["total_s"] / g
+        bem = guarded(lambda: bem_section(args, G, torch, W, rank))
     ring = None
     if not args.skip_ring:
-        ring = bench_ring(args, G, torch, W)
+        ring = guarded(lambda: bench_ring(args, G, torch, W))
     batch = None
     if not args.skip_batch:
-        batch = bench_batch(args, G, torch, W, flush)
+        batch = guarded(lambda: bench_batch(args, G, torch, W, flush))
     coupled = None
     if args.coupled_steps > 0:
-        coupled = bench_coupled(args, G, torch, W)
+        coupled = guarded(lambda: bench_coupled(args, G, torch, W))
     splitmerge = None
     if not args.skip_splitmerge:
-        splitmerge = bench_splitmerge(args, G, torch, W)
+        splitmerge = guarded(lambda: bench_splitmerge(args, G, torch, W))
 
     if rank == 0:
         cpu_v, cpu_cores, cpu_sample, _ = cpu_reference(args)

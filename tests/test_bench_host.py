@@ -87,3 +87,15 @@ def test_cpu_splitmerge_orders_agree_without_ties():
     assert ks[4] == cs[4] > 0 and km[3] == cm[3] > 0
     for a, b in zip(ks[:4] + km[:3], cs[:4] + cm[:3]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_guarded_section_reports_errors_in_the_line():
+    import bench
+    assert bench.guarded(lambda: {"ms": 1.0}) == {"ms": 1.0}
+
+    def broken():
+        raise RuntimeError("o3g_batch_run failed: timeout")
+
+    out = bench.guarded(broken)
+    assert out == {"error": "RuntimeError: o3g_batch_run failed: timeout"}
+    json.dumps(out)
