@@ -16,7 +16,14 @@
 # and oracle/_ref/libo3dref_splitmerge.so from the reference's Split.h and Merge.h (each
 # streamed up to its *_operation wrapper, which needs the element classes) with the
 # vendored lib/nanoflann/nanoflann.hpp, oracle/eigen_shim (a stand-in for the few Eigen
-# members they use), oracle/splitmerge_prelude.h and oracle/ref_splitmerge_driver.cpp.
+# members they use), oracle/splitmerge_prelude.h and oracle/ref_splitmerge_driver.cpp,
+# and oracle/_ref/libo3dref_ovoid.so from the reference's icosahedral sphere:
+# src/GeomHelper.cpp streamed up to generate_cuboid (generate_ovoid alone),
+# src/IglRefine.cpp, and the vendored lib/igl upsample.cpp,
+# triangle_triangle_adjacency.cpp, vertex_triangle_adjacency.cpp and cumsum.cpp, each
+# streamed up to its explicit-instantiation block and compiled with IGL_STATIC_LIBRARY
+# (so the igl headers do not pull in the rest of igl), against oracle/eigen_shim_igl (a
+# stand-in for the Eigen members they use), with oracle/ref_ovoid_driver.cpp.
 #
 # The reference location defaults to /root/reference/src; set O3D_REFERENCE_SRC to
 # override.  When the sources are absent (e.g. on a machine without the reference) the
@@ -69,4 +76,18 @@ if [ -f "$REF/Split.h" ] && [ -f "$REF/Merge.h" ] && [ -f "$NANOFLANN/nanoflann/
   } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fPIC -shared -w -I"$REF" -I"$NANOFLANN" \
         -I"$HERE/eigen_shim" -x c++ - -o "$OUT/libo3dref_splitmerge.so"
   echo "build_ref: built $OUT/libo3dref_splitmerge.so"
+fi
+IGL="$NANOFLANN/igl"
+if [ -f "$REF/GeomHelper.cpp" ] && [ -f "$REF/IglRefine.cpp" ] && [ -f "$IGL/upsample.cpp" ]; then
+  {
+    printf '#define IGL_STATIC_LIBRARY\n#define IGL_PARALLEL_FOR_FORCE_SERIAL\n'
+    for f in cumsum vertex_triangle_adjacency triangle_triangle_adjacency upsample; do
+      sed -n '/^#ifdef IGL_STATIC_LIBRARY/q;p' "$IGL/$f.cpp"
+    done
+    cat "$REF/IglRefine.cpp"
+    sed -n '/^ElementPacket<float> generate_cuboid/q;p' "$REF/GeomHelper.cpp"
+    cat "$HERE/ref_ovoid_driver.cpp"
+  } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fPIC -shared -w -I"$REF" -I"$NANOFLANN" -I"$IGL" \
+        -I"$HERE/eigen_shim_igl" -x c++ - -o "$OUT/libo3dref_ovoid.so"
+  echo "build_ref: built $OUT/libo3dref_ovoid.so"
 fi

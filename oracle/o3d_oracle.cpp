@@ -6,8 +6,15 @@
 //
 // Every function restates the reference algorithm in the reference's own arithmetic
 // order so that, compiled with -ffp-contract=off, it is bit-identical to the
-// reference's Kernels.h/CoreFunc.h/MathHelper.h compiled the same way (the pinning
-// test builds those reference headers into oracle/_ref/ and compares).
+// reference's own code compiled the same way.  oracle/build_ref.sh builds that code
+// into oracle/_ref/ and the pinning tests compare:
+//   Kernels.h/CoreFunc.h/MathHelper.h: the pair and panel kernels;
+//   Reflect.h: clear_inner_layer;
+//   Split.h/Merge.h with nanoflann: split and merge;
+//   GeomHelper.cpp/IglRefine.cpp with igl upsample: the sphere.
+// Parity unpinned: the Gaussian core, which the reference does not have (checked against
+// an independent closed form instead); and the BEM solve, whose Eigen GMRES is absent
+// (checked against an FP64 LU of the same matrix instead).
 //
 // Template parameters follow the reference: S = storage/arithmetic type,
 // A = accumulator type (Influence.h:67 `template <class S, class A>`).

@@ -226,10 +226,27 @@ def points_move_rk2(x, s, elong, u1, ug1, u2, ug2, dt, wt1=0.25, wt2=0.75):
         raise RuntimeError("oracle points_move_rk2 failed")
 
 
-def generate_ovoid(levels, rx=1.0, ry=1.0, rz=1.0):
+def ref_ovoid_available():
+    return os.path.exists(os.path.join(REF_DIR, "libo3dref_ovoid.so"))
+
+
+def generate_ovoid(levels, rx=1.0, ry=1.0, rz=1.0, use_ref=False):
+    """The icosahedral sphere of generate_ovoid (GeomHelper.cpp:41-91) refined `levels`
+    times with igl upsample numbering (IglRefine.cpp, lib/igl/upsample.cpp), scaled by
+    (rx, ry, rz): nodes (3, 10*4^L+2) float32 and panel node triples (3*20*4^L,) uint32.
+    use_ref runs the reference's own code (oracle/_ref/libo3dref_ovoid.so)."""
     nn, np_ = 10 * 4 ** levels + 2, 20 * 4 ** levels
-    x = np.zeros((3, nn), np.float32)
     idx = np.zeros(3 * np_, np.uint32)
+    if use_ref:
+        if "ovoid" not in _ref:
+            _ref["ovoid"] = ctypes.CDLL(os.path.join(REF_DIR, "libo3dref_ovoid.so"))
+        xi = np.zeros(3 * nn, np.float32)
+        rc = _ref["ovoid"].ref_generate_ovoid(ctypes.c_int(levels), ctypes.c_float(rx), ctypes.c_float(ry),
+                                              ctypes.c_float(rz), _p(xi), _p(idx))
+        if rc != 0:
+            raise RuntimeError("reference generate_ovoid failed")
+        return np.ascontiguousarray(xi.reshape(nn, 3).T), idx
+    x = np.zeros((3, nn), np.float32)
     rc = lib().o3o_generate_ovoid(ctypes.c_int(levels), ctypes.c_float(rx), ctypes.c_float(ry),
                                   ctypes.c_float(rz), _p(x), _p(idx))
     if rc != 0:

@@ -14,9 +14,9 @@ oracle/ref_splitmerge_driver.cpp):
 Every fixture holds its seeded inputs and the outputs of the reference build for the
 precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
 The Gaussian core has no reference implementation; its fixture comes from the oracle
-restatement and is marked "pinned": False.  The sphere fixture comes from the oracle's
-restatement of generate_ovoid + igl::upsample (the reference's version needs Eigen and
-cannot be built here) and is also marked unpinned.
+restatement and is marked "pinned": False.  The sphere fixture comes from the reference's
+generate_ovoid + igl upsample, built against oracle/eigen_shim_igl
+(python tests/golden/make_golden.py --only sphere writes it alone).
 """
 import json
 import os
@@ -136,6 +136,9 @@ def main():
     if "--only" in sys.argv and sys.argv[-1] == "splitmerge":
         write_splitmerge()
         return
+    if "--only" in sys.argv and sys.argv[-1] == "sphere":
+        write_sphere()
+        return
     for core in O.REF_CORES:
         if not O.ref_available(core):
             raise SystemExit("oracle/_ref/libo3dref_%s.so missing: run sh oracle/build_ref.sh" % core)
@@ -180,14 +183,23 @@ def main():
         _save("coeff_%s.npz" % core, {"core": core, "pinned": True, "maxlev": 3, "is_self": True,
                                       "source": "reference kernels"}, **geo, **out)
 
-    arrays = {}
-    for lev in range(4):
-        n, i = O.generate_ovoid(lev, 2.0, 2.0, 2.0)
-        arrays["nodes_L%d" % lev], arrays["idx_L%d" % lev] = n, i
-    _save("sphere.npz", {"pinned": False, "scale": 2.0, "source": "oracle restatement of generate_ovoid"},
-          **arrays)
+    write_sphere()
     write_reflect()
     write_splitmerge()
+
+
+def write_sphere():
+    """The icosahedral sphere (levels 0-3, scale 2) from the reference's own generate_ovoid
+    (src/GeomHelper.cpp) with refine_geometry (src/IglRefine.cpp) and the vendored igl
+    upsample (oracle/_ref/libo3dref_ovoid.so)."""
+    if not O.ref_ovoid_available():
+        raise SystemExit("oracle/_ref/libo3dref_ovoid.so missing: run sh oracle/build_ref.sh")
+    arrays = {}
+    for lev in range(4):
+        n, i = O.generate_ovoid(lev, 2.0, 2.0, 2.0, use_ref=True)
+        arrays["nodes_L%d" % lev], arrays["idx_L%d" % lev] = n, i
+    _save("sphere.npz", {"pinned": True, "scale": 2.0,
+                         "source": "reference generate_ovoid + refine_geometry + igl upsample"}, **arrays)
 
 
 if __name__ == "__main__":

@@ -61,6 +61,7 @@ def test_oracle_matches_golden_coefficients(core):
 
 def test_sphere_fixture_and_topology():
     d, meta = _gold("sphere.npz")
+    assert meta["pinned"]
     for lev in range(4):
         n, i = O.generate_ovoid(lev, 2.0, 2.0, 2.0)
         assert n.shape == (3, 10 * 4 ** lev + 2) and i.shape == (3 * 20 * 4 ** lev,)
@@ -127,6 +128,19 @@ def test_oracle_bit_exact_vs_reference_panels(core, shape):
             a = O.panels_on_panels_coeff(geo, geo, nunk, True, core, prec)
             b = O.panels_on_panels_coeff(geo, geo, nunk, True, core, prec, use_ref=True)
             assert _exact(a, b)
+
+
+@pytest.mark.parametrize("shape", [(2.0, 2.0, 2.0), (1.0, 1.0, 1.0), (2.0, 1.0, 0.5), (3.3, 0.7, 1.9)])
+def test_oracle_generate_ovoid_bit_exact_vs_reference(shape):
+    """The restated sphere against the reference's own generate_ovoid (GeomHelper.cpp:41-91)
+    with refine_geometry (IglRefine.cpp) and the vendored igl upsample, levels 0-5 (up to
+    the 20,480-panel sphere): node coordinates and panel numbering bit for bit."""
+    if not O.ref_ovoid_available():
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    for lev in range(6):
+        xa, ia = O.generate_ovoid(lev, *shape)
+        xb, ib = O.generate_ovoid(lev, *shape, use_ref=True)
+        assert np.array_equal(xa.view(np.uint32), xb.view(np.uint32)) and np.array_equal(ia, ib)
 
 
 # ---- known answers ----------------------------------------------------------------
