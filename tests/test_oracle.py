@@ -100,6 +100,30 @@ def test_oracle_bit_exact_vs_reference_pairs(core, prec):
 
 
 @pytest.mark.parametrize("core", list(O.REF_CORES))
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_oracle_bit_exact_vs_reference_at_branch_edges(core, prec):
+    """Targets placed at distances where the cores switch form: d^3/sigma^3 just below, at
+    and above 0.001 and 16 (the exponential core's three branches, CoreFunc.h:119-132; with
+    target radii sigma^3 = sigma_s^3 + sigma_t^3), d = 0, and d^3/sigma^3 from 1e-12 to 1e9,
+    in random directions."""
+    _need_ref(core)
+    rng = np.random.default_rng(36)
+    sig = np.float32(0.05)
+    rel = np.array([0.0] + [v * f for v in (1e-3, 16.0) for f in (0.999, 1.0, 1.001)] + [1e-12, 1e-9, 1e-6, 1e3, 1e9])
+    d = rng.normal(size=(3, rel.size))
+    d /= np.linalg.norm(d, axis=0)
+    sx = np.zeros((3, 1), np.float32)
+    ss = np.array([[0.3], [-0.2], [0.5]], np.float32)
+    sr = np.array([sig], np.float32)
+    tr = np.full(rel.size, sig, np.float32)
+    for trr, sig3 in ((tr, 2.0 * float(sig) ** 3), (None, float(sig) ** 3)):
+        tx = (d * np.cbrt(rel * sig3)).astype(np.float32)
+        a = O.points_affect_points(sx, sr, ss, tx, trr, True, core, prec)
+        b = O.points_affect_points(sx, sr, ss, tx, trr, True, core, prec, use_ref=True)
+        assert _exact(a[0], b[0]) and _exact(a[1], b[1])
+
+
+@pytest.mark.parametrize("core", list(O.REF_CORES))
 @pytest.mark.parametrize("shape", [(2.0, 2.0, 2.0), (2.0, 1.0, 0.5)])
 def test_oracle_bit_exact_vs_reference_panels(core, shape):
     """A sphere and an elongated ovoid (panels of unequal area and aspect), with targets in
