@@ -81,11 +81,33 @@ int32_t o3g_set_timing(int32_t enable);
 int32_t o3g_last_kernel_ms(float* ms);
 /* Cumulative number of CUDA kernels this thread has launched through the library. */
 int32_t o3g_launch_count(uint64_t* n);
+/* Cumulative number of device allocations (cudaMalloc / cudaMallocAsync) the library has
+ * made in this process, from any thread: its per-stream workspaces, BEM, RK2 and batch
+ * handles, and the scratch of split, merge, reflection and shedding. */
+int32_t o3g_alloc_count(uint64_t* n);
+
+/* Wait test.  Some kernels wait on the device for one another's progress, each wait
+ * bounded: the grid barriers of the BEM panel factorisation and triangular solves, and the
+ * dependency waits of the particle split.  A wait that runs out sets an error word, every
+ * other wait then returns at once, the kernels end, and the call returns O3G_ERR_TIMEOUT
+ * with the device still usable.  With enable != 0 (process-wide, until called with 0)
+ * those waits are given a condition that nothing fulfils (a barrier count one above the
+ * number of blocks, a flag nothing sets) and a limit of about a millisecond, so that tests
+ * can see them run out.  A split that runs out leaves the particles unchanged. */
+int32_t o3g_debug_wait_test(int32_t enable);
 
 /* Measures the FP32 FMA throughput of the current device (TFLOP/s, counting an FMA as
  * 2 flops) with a register-resident FMA-chain kernel: the measured denominator of the
  * pair kernels' roofline.  No counterpart in the reference. */
 int32_t o3g_fp32_peak_probe(int32_t iters, void* stream, double* tflops, float* ms);
+
+/* y[i] = exp(x[i]) (device arrays, n >= 0, asynchronous on `stream`) by the float exp the
+ * plain FP32 exponential core uses in 1 - exp(-x) (CoreFunc.h:127-128), made for its
+ * arguments, -16 < x < -0.001 (accurate for -20 <= x <= 0): rounded once from a float-float
+ * value, so it is the correctly rounded float but for rare arguments within about 2^-12 ulp
+ * of a rounding boundary, and 1 ulp from it there.  For tests and
+ * measurement; no counterpart in the reference, which calls its host library's expf. */
+int32_t o3g_exp_probe(int32_t n, const float* x, float* y, void* stream);
 
 /* ---- points_affect_points -------------------------------------------------------
  * Replaces points_affect_points<float,A>(src, targ, restype, env), Influence.h:67-551,
@@ -113,6 +135,41 @@ int32_t o3g_points_affect_points_d(int32_t core, int32_t mem,
                                    const double* tr,
                                    double* tu, double* tv, double* tw, double* const* tug,
                                    void* stream);
+
+/* ---- the reference's own external-solver hook -------------------------------------
+ * Exactly the prototypes a reference built with EXTERNAL_VEL_SOLVE declares and calls
+ * (Influence.h:33-48; call site :88-113), so that build links against this library with
+ * no source change.  Arguments, in the reference's order: source count (by pointer),
+ * source x, y, z, strengths sx, sy, sz, core radii; target count (by pointer), target
+ * x, y, z; velocity u, v, w; the nine gradient arrays (Kernels.h:184-192 order).  All
+ * arrays are host memory.  The targets carry no radius, so each is summed as a point
+ * (the kernel_0v_0pg form, Kernels.h:253-290); results are ADDED (+=) to u, v, w and
+ * the gradients, the caller zeroes them (Convection.h:161).  Nine NULL gradient
+ * pointers give velocity only.  Synchronous on the legacy default stream.
+ * Return: the flops of the call at the reference's own accounting,
+ * nt (12 + flops_0v_0pg ns) (Influence.h:310), or -1 on an error (o3g_last_error).
+ * The float hook uses the core and precision set by o3g_external_set_method, else the
+ * environment (O3G_EXTERNAL_CORE = rm|wl|exp|gauss|v2, O3G_EXTERNAL_PREC =
+ * plain|compensated), else WL and PLAIN: the reference's compiled-in core
+ * (CoreFunc.h:37) and its float arithmetic.  The double hook computes in FP64. */
+float external_vel_solver_f_(int* ns, const float* sx, const float* sy, const float* sz,
+                             const float* ssx, const float* ssy, const float* ssz, const float* sr,
+                             int* nt, const float* tx, const float* ty, const float* tz,
+                             float* tu, float* tv, float* tw,
+                             float* tux, float* tvx, float* twx, float* tuy, float* tvy, float* twy,
+                             float* tuz, float* tvz, float* twz);
+float external_vel_solver_d_(int* ns, const double* sx, const double* sy, const double* sz,
+                             const double* ssx, const double* ssy, const double* ssz, const double* sr,
+                             int* nt, const double* tx, const double* ty, const double* tz,
+                             double* tu, double* tv, double* tw,
+                             double* tux, double* tvx, double* twx, double* tuy, double* tvy, double* twy,
+                             double* tuz, double* tvz, double* twz);
+/* Core (O3G_CORE_*, or -1 for the environment / default) and precision (PLAIN or
+ * COMPENSATED, or -1) of the float hook above, process-wide.  No counterpart in the
+ * reference, which fixes the core at compile time (CoreFunc.h:35-39). */
+int32_t o3g_external_set_method(int32_t core, int32_t prec);
+/* The core and precision the float hook would use now. */
+int32_t o3g_external_get_method(int32_t* core, int32_t* prec);
 
 /* ---- surfaces ---------------------------------------------------------------------
  * A triangulated surface in the reference's Surfaces<S> layout (Surfaces.h:1463-1489):
@@ -405,12 +462,14 @@ int32_t o3g_merge_close_particles(int32_t n, float* x, float* y, float* z, float
  * device-resident arrays (mem is always device; prec PLAIN or COMPENSATED), with every
  * scratch byte taken from one fixed 64 MiB array in the library's device image.
  *  - The first call on a device resolves that array's address (cudaGetSymbolAddress);
- *    make it before capturing a stream into a graph.
+ *    make it before capturing a stream into a graph.  The address is looked up again
+ *    when the device's context changes (e.g. after cudaDeviceReset).
  *  - All calls share the array: calls that overlap on the GPU race; use one stream.
  *  - Problems whose packed tiles do not fit (about 1.3 million sources + targets) return
  *    O3G_ERR_INVALID_ARG before any work is queued.
- * Sources are not Morton-sorted, so the Gaussian and exponential cores run without the
- * far-tile fast path. */
+ * Sources are not Morton-sorted: the Gaussian and exponential cores still test each
+ * source tile against each warp's targets, but with unsorted points the test almost
+ * never finds a far tile, so nearly every pair takes the full core. */
 int32_t o3g_points_affect_points_noalloc(int32_t core, int32_t prec,
                                          int32_t ns, const float* sx, const float* sy, const float* sz,
                                          const float* sr, const float* ssx, const float* ssy, const float* ssz,

@@ -77,10 +77,24 @@ def _declare(l):
     l.o3g_last_kernel_ms.argtypes = [P]
     l.o3g_launch_count.restype = c_i32
     l.o3g_launch_count.argtypes = [P]
+    l.o3g_alloc_count.restype = c_i32
+    l.o3g_alloc_count.argtypes = [P]
+    l.o3g_debug_wait_test.restype = c_i32
+    l.o3g_debug_wait_test.argtypes = [c_i32]
     l.o3g_fp32_peak_probe.restype = c_i32
     l.o3g_fp32_peak_probe.argtypes = [c_i32, P, P, P]
+    l.o3g_exp_probe.restype = c_i32
+    l.o3g_exp_probe.argtypes = [c_i32, P, P, P]
     l.o3g_points_affect_points.restype = c_i32
     l.o3g_points_affect_points.argtypes = [c_i32, c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
+    for name in ("external_vel_solver_f_", "external_vel_solver_d_"):
+        fn = getattr(l, name)
+        fn.argtypes = [P] * 24
+        fn.restype = c_f
+    l.o3g_external_set_method.argtypes = [c_i32, c_i32]
+    l.o3g_external_set_method.restype = c_i32
+    l.o3g_external_get_method.argtypes = [P, P]
+    l.o3g_external_get_method.restype = c_i32
     l.o3g_ovoid_size.restype = c_i32
     l.o3g_ovoid_size.argtypes = [c_i32, P, P]
     l.o3g_generate_ovoid.restype = c_i32
@@ -199,4 +213,4 @@ def header_symbols():
     import re
     txt = open(HEADER).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(o3g_[a-z0-9_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(o3g_[a-z0-9_]+|external_vel_solver_[fd]_)\s*\(", txt)))

@@ -1,6 +1,10 @@
 // o3g_api_pair.cu -- extern "C" points_affect_points entry points (float and double).
 #include "o3g_pair_impl.cuh"
 
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+
 namespace o3g {
 
 template <class I>
@@ -149,4 +153,107 @@ extern "C" int32_t o3g_points_affect_points_d(int32_t core, int32_t mem, int32_t
                                               double* tv, double* tw, double* const* tug, void* stream) {
   return o3g::ptpt_entry<double>(core, o3g::MODE_FP64, mem, ns, sx, sy, sz, sr, ssx, ssy, ssz, nt, tx, ty, tz, tr,
                                  tu, tv, tw, tug, stream);
+}
+
+// ---------------------------------------------------------------------------------------
+// The reference's own external-solver hook (Influence.h:33-48, called at :88-113 when the
+// reference is built with EXTERNAL_VEL_SOLVE): Fortran-style by-pointer counts, source
+// positions, strengths, radii, target positions (no target radius: the targets are taken as
+// points, the kernel_0v_0pg form), velocity and nine gradient arrays in host memory, summed
+// into (+=).  Returns the flops of the call at the reference's accounting,
+// nt (12 + flops_0v_0pg ns) (Influence.h:310), or -1 on an error (o3g_last_error).
+namespace {
+std::atomic<int> g_ext_core{-1};
+std::atomic<int> g_ext_prec{-1};
+
+int ext_parse(const char* v, const char* const* names, int n, int dflt) {
+  if (!v || !*v) return dflt;
+  for (int k = 0; k < n; ++k)
+    if (!strcmp(v, names[k])) return k;
+  if (v[0] >= '0' && v[0] < '0' + n && v[1] == 0) return v[0] - '0';
+  return dflt;
+}
+void ext_method(int* core, int* prec) {
+  static const char* const cores[5] = {"rm", "wl", "exp", "gauss", "v2"};
+  static const char* const precs[2] = {"plain", "compensated"};
+  int c = g_ext_core.load(), p = g_ext_prec.load();
+  if (c < 0) c = ext_parse(getenv("O3G_EXTERNAL_CORE"), cores, 5, O3G_CORE_WL);
+  if (p < 0) p = ext_parse(getenv("O3G_EXTERNAL_PREC"), precs, 2, O3G_PREC_PLAIN);
+  *core = c;
+  *prec = p;
+}
+template <class I>
+float ext_call(int core, int prec, const int* ns, const I* sx, const I* sy, const I* sz, const I* ssx, const I* ssy,
+               const I* ssz, const I* sr, const int* nt, const I* tx, const I* ty, const I* tz, I* tu, I* tv, I* tw,
+               I* g0, I* g1, I* g2, I* g3, I* g4, I* g5, I* g6, I* g7, I* g8) {
+  if (!ns || !nt) {
+    o3g::set_error("external_vel_solver: null count pointer");
+    return -1.0f;
+  }
+  I* g[9] = {g0, g1, g2, g3, g4, g5, g6, g7, g8};
+  int nnull = 0;
+  for (int k = 0; k < 9; ++k) nnull += (g[k] == nullptr);
+  if (nnull != 0 && nnull != 9) {
+    o3g::set_error("external_vel_solver: some gradient arrays are null and some are not");
+    return -1.0f;
+  }
+  const bool grads = (nnull == 0);
+  int32_t st;
+  if (std::is_same<I, float>::value)
+    st = o3g_points_affect_points(core, prec, O3G_MEM_HOST, *ns, (const float*)sx, (const float*)sy,
+                                  (const float*)sz, (const float*)sr, (const float*)ssx, (const float*)ssy,
+                                  (const float*)ssz, *nt, (const float*)tx, (const float*)ty, (const float*)tz,
+                                  nullptr, (float*)tu, (float*)tv, (float*)tw,
+                                  grads ? (float* const*)g : nullptr, nullptr);
+  else
+    st = o3g_points_affect_points_d(core, O3G_MEM_HOST, *ns, (const double*)sx, (const double*)sy,
+                                    (const double*)sz, (const double*)sr, (const double*)ssx, (const double*)ssy,
+                                    (const double*)ssz, *nt, (const double*)tx, (const double*)ty,
+                                    (const double*)tz, nullptr, (double*)tu, (double*)tv, (double*)tw,
+                                    grads ? (double* const*)g : nullptr, nullptr);
+  if (st != O3G_OK) return -1.0f;
+  const double fpp = (double)o3g_flops_per_pair(core, grads ? 1 : 0, 0);
+  return (float)((double)(*nt) * (12.0 + fpp * (double)(*ns)));
+}
+}  // namespace
+
+extern "C" int32_t o3g_external_set_method(int32_t core, int32_t prec) {
+  if (core < -1 || core > 4 || prec < -1 || prec > 1) {
+    o3g::set_error("o3g_external_set_method: core must be -1..4 and prec -1..1");
+    return O3G_ERR_INVALID_ARG;
+  }
+  g_ext_core.store(core);
+  g_ext_prec.store(prec);
+  return O3G_OK;
+}
+
+extern "C" int32_t o3g_external_get_method(int32_t* core, int32_t* prec) {
+  if (!core || !prec) return O3G_ERR_INVALID_ARG;
+  int c, p;
+  ext_method(&c, &p);
+  *core = c;
+  *prec = p;
+  return O3G_OK;
+}
+
+extern "C" float external_vel_solver_f_(int* ns, const float* sx, const float* sy, const float* sz, const float* ssx,
+                                        const float* ssy, const float* ssz, const float* sr, int* nt, const float* tx,
+                                        const float* ty, const float* tz, float* tu, float* tv, float* tw, float* tux,
+                                        float* tvx, float* twx, float* tuy, float* tvy, float* twy, float* tuz,
+                                        float* tvz, float* twz) {
+  int core, prec;
+  ext_method(&core, &prec);
+  return ext_call<float>(core, prec, ns, sx, sy, sz, ssx, ssy, ssz, sr, nt, tx, ty, tz, tu, tv, tw, tux, tvx, twx,
+                         tuy, tvy, twy, tuz, tvz, twz);
+}
+
+extern "C" float external_vel_solver_d_(int* ns, const double* sx, const double* sy, const double* sz,
+                                        const double* ssx, const double* ssy, const double* ssz, const double* sr,
+                                        int* nt, const double* tx, const double* ty, const double* tz, double* tu,
+                                        double* tv, double* tw, double* tux, double* tvx, double* twx, double* tuy,
+                                        double* tvy, double* twy, double* tuz, double* tvz, double* twz) {
+  int core, prec;
+  ext_method(&core, &prec);
+  return ext_call<double>(core, O3G_PREC_FP64, ns, sx, sy, sz, ssx, ssy, ssz, sr, nt, tx, ty, tz, tu, tv, tw, tux,
+                          tvx, twx, tuy, tvy, twy, tuz, tvz, twz);
 }

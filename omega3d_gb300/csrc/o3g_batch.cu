@@ -710,7 +710,7 @@ int32_t batch_create(int core, int prec, bool grads, int nsys, const BatchSysDev
     add(h->cub_bytes);
   }
   add((size_t)12 * std::max(h->cap_tpad, 1LL) * sizeof(float));   // tuning sink
-  cudaError_t e = cudaMalloc((void**)&h->arena, bytes);
+  cudaError_t e = o3g::dev_alloc((void**)&h->arena, bytes);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error_cuda("batched pair sums: cudaMalloc", e);

@@ -38,11 +38,23 @@ constexpr int kPanelThreads = 256;
 constexpr int kSolveThreads = 1024;
 constexpr unsigned long long kSpinLimit = 1ull << 25;
 
+constexpr unsigned long long kTestSpinLimit = 1ull << 14;   // the wait test's limit (~1 ms)
+
 struct Barrier {
   unsigned* count;
   unsigned* gen;
   int* err;
+  unsigned long long limit;   // polls before giving up
+  unsigned extra;             // 0; 1 in the wait test: one more arrival than blocks, never met
 };
+
+// the barrier over the handle's flag words (count, generation, error), with the spin limit,
+// or in the wait test the unreachable count and the short limit
+inline Barrier make_barrier(int* flags) {
+  const bool test = wait_test_on();
+  return Barrier{(unsigned*)(flags + 2), (unsigned*)(flags + 3), flags, test ? kTestSpinLimit : kSpinLimit,
+                 test ? 1u : 0u};
+}
 
 // grid-wide barrier with a bounded spin; returns false (in every thread) once the error
 // flag is set, by a timeout here or anywhere else
@@ -54,7 +66,7 @@ __device__ bool grid_sync(const Barrier& b) {
     const unsigned g = *gen;
     __threadfence();
     const unsigned arrived = atomicAdd(b.count, 1u) + 1u;
-    if (arrived == gridDim.x) {
+    if (arrived == gridDim.x + b.extra) {
       atomicExch(b.count, 0u);
       __threadfence();
       atomicAdd(b.gen, 1u);
@@ -62,7 +74,7 @@ __device__ bool grid_sync(const Barrier& b) {
       unsigned long long it = 0;
       while (*gen == g) {
         if (*(volatile int*)b.err) break;
-        if (++it > kSpinLimit) {
+        if (++it > b.limit) {
           atomicExch(b.err, 1);
           break;
         }
@@ -662,12 +674,12 @@ extern "C" int32_t o3g_bem_create(int64_t n, o3g_bem_t** out) {
   h->n = (int)n;
   h->ld = (n + 31) / 32 * 32;
   const size_t mat = (size_t)h->ld * n * sizeof(float);
-  cudaError_t e = cudaMalloc((void**)&h->A, mat);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->LU, mat);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->piv, n * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->perm, n * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->flags, 64 * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&h->dinv, (size_t)((n + kNb - 1) / kNb) * 2 * kNb * kNb * sizeof(float));
+  cudaError_t e = o3g::dev_alloc((void**)&h->A, mat);
+  if (e == cudaSuccess) e = o3g::dev_alloc((void**)&h->LU, mat);
+  if (e == cudaSuccess) e = o3g::dev_alloc((void**)&h->piv, n * sizeof(int));
+  if (e == cudaSuccess) e = o3g::dev_alloc((void**)&h->perm, n * sizeof(int));
+  if (e == cudaSuccess) e = o3g::dev_alloc((void**)&h->flags, 64 * sizeof(int));
+  if (e == cudaSuccess) e = o3g::dev_alloc((void**)&h->dinv, (size_t)((n + kNb - 1) / kNb) * 2 * kNb * kNb * sizeof(float));
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error_cuda("o3g_bem_create: cudaMalloc", e);
@@ -731,7 +743,7 @@ static int32_t bem_scratch(o3g_bem_t* h, size_t bytes) {
   cudaFree(h->scratch);
   h->scratch = nullptr;
   h->scratch_bytes = 0;
-  cudaError_t e = cudaMalloc((void**)&h->scratch, bytes);
+  cudaError_t e = o3g::dev_alloc((void**)&h->scratch, bytes);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error_cuda("o3g_bem: scratch", e);
@@ -853,7 +865,7 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
       pa.A = h->LU; pa.ld = ld; pa.n = n; pa.k0 = k0; pa.jb = jb; pa.R = r;
       pa.piv = h->piv; pa.cval = cval; pa.crow = crow; pa.crows = crows; pa.drow = drow;
       pa.singular = h->flags + 1;
-      pa.bar = Barrier{(unsigned*)(h->flags + 2), (unsigned*)(h->flags + 3), h->flags};
+      pa.bar = make_barrier(h->flags);
       void* args[] = {&pa};
       const size_t sm = ((size_t)jb * r + jb + 32) * sizeof(float);
       O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_panel_lu, dim3(g), dim3(kPanelThreads), args, sm, st));
@@ -962,7 +974,7 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   if (per_sm < 1) return O3G_ERR_CUDA;
   TrsvArgs ta;
   ta.LU = h->LU; ta.dinv = h->dinv; ta.ld = ld; ta.n = n; ta.y = y;
-  ta.bar = Barrier{(unsigned*)(h->flags + 2), (unsigned*)(h->flags + 3), h->flags};
+  ta.bar = make_barrier(h->flags);
   void* targs[] = {&ta};
   std::vector<double> hn((size_t)nrb);
   double rel = 1.0, bnorm = 0.0;

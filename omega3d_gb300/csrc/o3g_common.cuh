@@ -81,6 +81,16 @@ KernelTimer& thread_timer();
 // count of kernels this thread has launched through the library
 void note_launch(int n = 1);
 
+// device allocations: every cudaMalloc / cudaMallocAsync the library makes goes through
+// these, which count the successful ones for o3g_alloc_count
+cudaError_t dev_alloc(void** p, size_t bytes);
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st);
+
+// wait test (o3g_debug_wait_test): when on, the bounded device-side waits of the BEM
+// factorisation and solves and of the particle split wait for a condition nothing fulfils,
+// with a short limit, so that they run out and the call returns O3G_ERR_TIMEOUT
+bool wait_test_on();
+
 // ------------------------------------------------------------------------------
 // vector types
 template <class T> struct V4;
@@ -131,6 +141,74 @@ __device__ __forceinline__ float rsq(float x) {
 }
 template <bool ACC>
 __device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+
+// exp(x) for float x in [-20, 0], rounded once from a float-float value accurate to about
+// 2^-35 relative: so it is the correctly rounded float in all but about 5 of 100,000
+// arguments, and 1 ulp from it otherwise (beyond |x| = 22, n hi(ln2/32) below is no longer
+// exact and the accuracy drops).  The plain FP32 exponential core evaluates the
+// reference's 1 - exp(-x) with it: that form magnifies a difference of one ulp in exp(-x)
+// by exp(-x) / (1 - exp(-x)) (1000x at x = 0.001), so the result tracks the host library's
+// float exp (glibc's is within 0.502 ulp) only if this one is as close to correct rounding.
+// Method: Tang's table-driven exponential (ACM TOMS 15(2), 1989): x = (32 k + j) ln2/32 + r
+// with |r| <= ln2/64, exp(x) = 2^k 2^(j/32) exp(r); 2^(j/32) as a (hi, lo) float pair,
+// ln2/32 split so that n hi is exact, exp(r) - 1 = r + r^2/2 + r^3/6 + r^4/24.
+__device__ const __align__(16) float2 kExp2Frac[32] = {
+    {1.000000000e+00f, 0.000000000e+00f},
+    {1.021897197e+00f, -4.811559862e-08f},
+    {1.044273734e+00f, 4.833470157e-08f},
+    {1.067140460e+00f, -5.933751979e-08f},
+    {1.090507746e+00f, -1.307753994e-08f},
+    {1.114386797e+00f, -5.435540018e-08f},
+    {1.138788581e+00f, 5.386222313e-08f},
+    {1.163724899e+00f, -4.051441493e-08f},
+    {1.189207077e+00f, 3.797635273e-08f},
+    {1.215247393e+00f, -3.267394888e-08f},
+    {1.241857767e+00f, 4.496838102e-08f},
+    {1.269050956e+00f, 1.419333318e-09f},
+    {1.296839595e+00f, -4.018999533e-08f},
+    {1.325236678e+00f, -3.496373324e-08f},
+    {1.354255557e+00f, -1.012334927e-08f},
+    {1.383909941e+00f, -5.875577358e-08f},
+    {1.414213538e+00f, 2.420323497e-08f},
+    {1.445180774e+00f, 3.324199938e-08f},
+    {1.476826191e+00f, -4.500898854e-08f},
+    {1.509164453e+00f, -2.495937323e-08f},
+    {1.542210817e+00f, 8.070904833e-09f},
+    {1.575980902e+00f, -5.661025426e-08f},
+    {1.610490322e+00f, 9.836217174e-09f},
+    {1.645755529e+00f, -5.124972091e-08f},
+    {1.681792855e+00f, -2.475532668e-08f},
+    {1.718619347e+00f, -4.849617596e-08f},
+    {1.756252170e+00f, -9.235770371e-09f},
+    {1.794709086e+00f, -1.141504491e-08f},
+    {1.834008098e+00f, -1.123927795e-08f},
+    {1.874167681e+00f, -4.663005626e-08f},
+    {1.915206552e+00f, 9.845328108e-09f},
+    {1.957144141e+00f, -1.702180441e-08f}
+};
+__device__ __forceinline__ float exp_tang(float x) {
+  const float nf = rintf(x * 4.616624069e+01f);        // 32 / ln2
+  const int n = (int)nf;
+  const float rh = fmaf(-nf, 2.166175842e-02f, x);     // x - n hi(ln2/32): exact
+  const float rl = -nf * -9.090303479e-07f;            // - n lo(ln2/32)
+  const float r = rh + rl;
+  const float q = (r * r) * fmaf(r, fmaf(r, 4.166666791e-02f, 1.666666716e-01f), 0.5f);
+  const float slo = rl + q;                            // exp(r) - 1 = rh + slo
+  const float2 T = __ldg(&kExp2Frac[n & 31]);
+  const float p = __fmul_rn(T.x, rh);                  // (no contraction: the error terms
+  const float pe = fmaf(T.x, rh, -p);                  //  below need p and h rounded)
+  const float h = __fadd_rn(T.x, p);                   // T.x rh = p + pe exactly; |p| < T.x:
+  const float l0 = __fadd_rn(__fsub_rn(T.x, h), p);    // Fast2Sum, T.x + p = h + l0
+  const float tail = fmaf(T.x, slo, T.y + T.y * rh);
+  const float res = h + ((l0 + pe) + tail);
+  return res * __int_as_float((127 + (n >> 5)) << 23);  // times 2^k, exact for normal results
+}
+
+// dx dx + dy dy + dz dz with every product and sum rounded, left to right: the reference's
+// expression (Kernels.h:167-170) as an uncontracted float build evaluates it
+__device__ __forceinline__ float dist2_ref(float dx, float dy, float dz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
 
 __device__ __forceinline__ float dev_erf(float x) { return erff(x); }
 __device__ __forceinline__ double dev_erf(double x) { return erf(x); }
@@ -276,8 +354,12 @@ __device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
     r3 = d2top * dn5;
     bbb = fma(T(-5.0) * r3, rs2, T(2.0) * dn5);
   } else if (C == CORE_EXP) {
-    // CoreFunc.h:226-236 with the branches of exp_cond / exp_bbb (:119-174)
-    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    // CoreFunc.h:226-236 with the branches of exp_cond / exp_bbb (:119-174).  The core
+    // jumps by reld3/2 (5e-4) where it switches form at reld3 = 0.001, so plain FP32 forms
+    // distsq and the bbb difference in the reference's operation order, each operation
+    // rounded (Kernels.h:167-170), and takes each branch exactly where the reference does.
+    constexpr bool REF = !ACC && std::is_same<T, float>::value;
+    const T distsq = REF ? (T)dist2_ref((float)dx, (float)dy, (float)dz) : fma(dx, dx, fma(dy, dy, dz * dz));
     const T dist = dev_sqrt(distsq);
     const T corefac = T(1.0) / cst;
     const T d3 = distsq * dist;
@@ -289,8 +371,16 @@ __device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
     } else if (reld3 < T(0.001)) {
       r3 = corefac;
       bbb = T(-1.5) * dist * r3 * r3;
+    } else if (REF) {
+      // plain FP32: the reference's own float arithmetic, 1 - exp(-x) and corefac exp(-x)
+      // (exp_cond / exp_bbb, CoreFunc.h:127-128, :175-177), exp nearly correctly rounded
+      const float e = exp_tang((float)-reld3);
+      const float r3f = __fmul_rn((float)ood3, __fsub_rn(1.0f, e));
+      r3 = (T)r3f;
+      bbb = (T)(__fdiv_rn(__fmul_rn(3.0f, __fsub_rn(__fmul_rn((float)corefac, e), r3f)), (float)distsq));
     } else {
-      // 1 - exp(-x) through expm1: the reference's float 1.0f - exp(-x) loses ~eps/x here
+      // compensated and FP64: 1 - exp(-x) through expm1, which keeps the digits that
+      // float 1 - exp(-x) loses (about eps/x) near the core
       const T em1 = dev_expm1(-reld3);
       r3 = ood3 * (-em1);
       bbb = T(3.0) * (corefac * (em1 + T(1.0)) - r3) / distsq;
@@ -322,13 +412,15 @@ __device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst) {
     const T rs2 = rs * rs;
     return fma(T(2.5), cst, distsq) * (rs2 * rs2 * rs);
   } else if (C == CORE_EXP) {
-    const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
+    constexpr bool REF = !ACC && std::is_same<T, float>::value;   // as in core_g
+    const T distsq = REF ? (T)dist2_ref((float)dx, (float)dy, (float)dz) : fma(dx, dx, fma(dy, dy, dz * dz));
     const T dist = dev_sqrt(distsq);
     const T ood3 = T(1.0) / (distsq * dist);
     const T corefac = T(1.0) / cst;
     const T reld3 = corefac / ood3;
     if (reld3 > T(16.0)) return ood3;
     if (reld3 < T(0.001)) return corefac;
+    if (REF) return (T)__fmul_rn((float)ood3, __fsub_rn(1.0f, exp_tang((float)-reld3)));
     return ood3 * (-dev_expm1(-reld3));
   } else if (C == CORE_V2) {
     const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));

@@ -13,17 +13,24 @@
 //  * The array holds O3G_NOALLOC_SCRATCH_BYTES (64 MiB).  Every GPU on which the library
 //    is loaded keeps it until the process exits.
 //  * The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current).  Make that first
-//    call before capturing any stream into a CUDA graph.
+//    cudaGetSymbolAddress (with that device current) and keeps it for that device's
+//    context.  Make that first call before capturing any stream into a CUDA graph.  Each
+//    later call compares the current context's unique id (cuCtxGetId) with the one the
+//    address was taken in, and looks the address up again when it differs: after a
+//    cudaDeviceReset the library image, and with it the array, is loaded anew.
 //  * Every call uses the same array.  Calls whose work overlaps on the GPU (different
 //    streams, or several host threads) race on it: issue them on one stream.
 //  * Nothing in the array has to start at zero: every byte a call reads was written
 //    earlier in the same call, so the contents left by the previous call do no harm.
 //  * Problems too large for the array are rejected with O3G_ERR_INVALID_ARG before any
 //    work is queued; the message (o3g_last_error) gives the bytes needed.
-// Sources are not Morton-sorted here (the sort needs scratch proportional to N twice over),
-// so the Gaussian and compact-exponential cores run without the far-tile fast path.
+// Sources are not Morton-sorted here (the sort needs scratch proportional to N twice over).
+// The Gaussian and compact-exponential cores still bound each source tile and test it
+// against each warp's targets, but unsorted tiles and targets spread over the whole set,
+// so the test almost never finds a far tile: nearly every pair takes the full core.
 #include "o3g_pair_impl.cuh"
+
+#include <cuda.h>
 
 #include <cstdio>
 #include <mutex>
@@ -33,9 +40,36 @@ namespace o3g {
 static constexpr size_t kNoAllocBytes = (size_t)64 << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
+// Unique id of the calling thread's current context (0 when none is current), through the
+// driver entry points the runtime hands out (no link against the driver library).
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+    (void)cudaGetLastError();
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 static int32_t noalloc_base(char** base) {
   static std::mutex mu;
   static char* addr[64] = {nullptr};
+  static unsigned long long ctx[64] = {0};
   int dev = -1;
   O3G_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) {
@@ -43,7 +77,8 @@ static int32_t noalloc_base(char** base) {
     return O3G_ERR_NO_DEVICE;
   }
   std::lock_guard<std::mutex> lk(mu);
-  if (!addr[dev]) {
+  const unsigned long long id = current_context_id();
+  if (!addr[dev] || id == 0 || id != ctx[dev]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -51,6 +86,7 @@ static int32_t noalloc_base(char** base) {
       return O3G_ERR_CUDA;
     }
     addr[dev] = (char*)p;
+    ctx[dev] = current_context_id();   // the lookup made the device's context current
   }
   *base = addr[dev];
   return O3G_OK;

@@ -55,3 +55,25 @@ extern "C" int32_t o3g_fp32_peak_probe(int32_t iters, void* stream, double* tflo
   O3G_CUDA_TRY(cudaGetLastError());
   return O3G_OK;
 }
+
+namespace o3g {
+__global__ void k_exp_probe(int n, const float* __restrict__ x, float* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = exp_tang(x[i]);
+}
+}  // namespace o3g
+
+extern "C" int32_t o3g_exp_probe(int32_t n, const float* x, float* y, void* stream) {
+  using namespace o3g;
+  if (n < 0 || (n > 0 && (!x || !y))) {
+    set_error("o3g_exp_probe: n must be >= 0 and x, y non-null");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (n == 0) return O3G_OK;
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+  k_exp_probe<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(n, x, y);
+  note_launch();
+  O3G_CUDA_TRY(cudaGetLastError());
+  return O3G_OK;
+}

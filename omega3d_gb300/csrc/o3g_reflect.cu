@@ -195,7 +195,7 @@ extern "C" int32_t o3g_clear_inner_layer(int32_t n, float* x, float* y, float* z
   if (npushed) {
     *npushed = 0;
     if (n == 0) return O3G_OK;
-    O3G_CUDA_TRY(cudaMallocAsync((void**)&counter, sizeof(int), st));
+    O3G_CUDA_TRY(o3g::dev_alloc_async((void**)&counter, sizeof(int), st));
     O3G_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
   }
   // the cutoff height is the reference's float product _cutoff_mult * _ips (Reflect.h:553)

@@ -359,7 +359,7 @@ static int32_t rk2_alloc(int32_t core, int32_t prec, int32_t n, float* const* x,
   h->na = na;
   h->fa = fa;
   const size_t total = na * (3 + 9 + 3 + 9 + 3 + 3 + 1) + fa * (3 + 9 + 3 + 9 + 3);
-  cudaError_t e = cudaMalloc((void**)&h->buf, total);
+  cudaError_t e = o3g::dev_alloc((void**)&h->buf, total);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error_cuda("o3g_rk2_create: cudaMalloc", e);
@@ -561,7 +561,7 @@ extern "C" int32_t o3g_rk2_attach_body(o3g_rk2_t* h, const o3g_surface_t* surf, 
   b->max_iter = max_iter;
   const size_t pa = align_up((size_t)surf->np * sizeof(float));
   const size_t ua = align_up((size_t)surf->np * nunk * sizeof(float));
-  cudaError_t e = cudaMalloc((void**)&b->buf, 7 * pa + 2 * ua + 256);
+  cudaError_t e = o3g::dev_alloc((void**)&b->buf, 7 * pa + 2 * ua + 256);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     delete b;

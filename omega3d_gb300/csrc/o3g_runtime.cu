@@ -1,6 +1,8 @@
 // o3g_runtime.cu -- errors, device facts, per-stream workspaces, kernel timing.
 #include "o3g_common.cuh"
 
+#include <atomic>
+
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -69,10 +71,10 @@ int32_t workspace_get(cudaStream_t stream, size_t bytes, Workspace** out) {
       w.cap = 0;
     }
     const size_t want = align_up(bytes + bytes / 4, 1 << 20);
-    cudaError_t e = cudaMalloc((void**)&w.base, want);
+    cudaError_t e = dev_alloc((void**)&w.base, want);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
-      e = cudaMalloc((void**)&w.base, align_up(bytes, 1 << 20));
+      e = dev_alloc((void**)&w.base, align_up(bytes, 1 << 20));
       if (e != cudaSuccess) {
         (void)cudaGetLastError();
         set_error_cuda("cudaMalloc(workspace)", e);
@@ -109,6 +111,21 @@ int32_t occupancy_blocks(const void* kernel, int block, int* nb) {
 static thread_local bool g_timing = false;
 static thread_local unsigned long long g_launches = 0;
 void note_launch(int n) { g_launches += (unsigned long long)n; }
+
+static std::atomic<int> g_wait_test{0};
+bool wait_test_on() { return g_wait_test.load() != 0; }
+
+static std::atomic<unsigned long long> g_allocs{0};
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) g_allocs.fetch_add(1);
+  return e;
+}
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st) {
+  const cudaError_t e = cudaMallocAsync(p, bytes, st);
+  if (e == cudaSuccess) g_allocs.fetch_add(1);
+  return e;
+}
 static thread_local KernelTimer g_timer;
 
 KernelTimer& thread_timer() { return g_timer; }
@@ -169,6 +186,17 @@ int32_t o3g_flops_per_pair(int32_t core, int32_t grads, int32_t have_tr) {
   if (core < 0 || core > 4) return -1;
   if (grads) return 54 + (have_tr ? tvg[core] : tpg[core]);
   return 23 + (have_tr ? tv[core] : tp[core]);
+}
+
+int32_t o3g_debug_wait_test(int32_t enable) {
+  o3g::g_wait_test.store(enable != 0 ? 1 : 0);
+  return O3G_OK;
+}
+
+int32_t o3g_alloc_count(uint64_t* n) {
+  if (!n) return O3G_ERR_INVALID_ARG;
+  *n = (uint64_t)o3g::g_allocs.load();
+  return O3G_OK;
 }
 
 int32_t o3g_launch_count(uint64_t* n) {

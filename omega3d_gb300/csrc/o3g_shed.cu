@@ -114,7 +114,7 @@ extern "C" int32_t o3g_panels_affect_panels(int32_t prec, int32_t mem, int32_t m
                                     stream);
   }
   float* p = nullptr;
-  O3G_CUDA_TRY(cudaMallocAsync((void**)&p, 3 * (size_t)tnp * sizeof(float), st));
+  O3G_CUDA_TRY(o3g::dev_alloc_async((void**)&p, 3 * (size_t)tnp * sizeof(float), st));
   k_collocation<<<(tnp + 255) / 256, 256, 0, st>>>(tnp, tnx, tny, tnz, tidx, tnmx, tnmy, tnmz, offset, p, p + tnp,
                                                    p + 2 * (size_t)tnp);
   note_launch();

@@ -68,6 +68,9 @@ constexpr int64_t kMaxCell = (1 << 21) - 1;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kReadySpin = 1u << 28;
 constexpr uint64_t kReadyNs = 10ull * 1000 * 1000 * 1000;   // 10 s
+// the wait test's limits (o3g_debug_wait_test): the waits then read a word nothing sets
+constexpr uint32_t kTestSpin = 1u << 14;
+constexpr uint64_t kTestNs = 20ull * 1000 * 1000;   // 20 ms
 // pause between polls of a flag: thousands of waiting threads polling back to back load
 // the L2 enough to slow the stores they wait for
 constexpr unsigned kPollNs = 128;
@@ -471,6 +474,9 @@ struct LevelArgs {
   int* claim;
   int* err;
   int spread;    // 1: every particle has its own resident thread (no claiming)
+  uint32_t spin; // polls before a wait gives up
+  uint64_t ns;   // wall time before a wait gives up
+  const int* never;   // the wait test: wait on this word (never set) instead
 };
 
 __global__ void k_split_levels(LevelArgs a) {
@@ -495,12 +501,13 @@ __global__ void k_split_levels(LevelArgs a) {
       int lv = 0;
       for (int q = 0; q < nd; ++q) {
         const int pj = a.dep[b + q];
+        const int* flag = a.never ? a.never : a.lvl1 + pj;
         const uint64_t t0 = global_ns();
         int v = 0;
-        for (uint32_t it = 0; it < kReadySpin; ++it) {
-          asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(a.lvl1 + pj) : "memory");
+        for (uint32_t it = 0; it < a.spin; ++it) {
+          asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
           if (v) break;
-          if ((it & 1023u) == 1023u && (*(volatile int*)a.err || global_ns() - t0 > kReadyNs)) break;
+          if ((it & 1023u) == 1023u && (*(volatile int*)a.err || global_ns() - t0 > a.ns)) break;
           __nanosleep(kPollNs);
         }
         if (!v) {
@@ -539,19 +546,22 @@ struct SplitArgs {
   int* ready;
   int* claim;
   int* err;
+  uint32_t spin;                // polls before a wait gives up
+  uint64_t ns;                  // wall time before a wait gives up
+  const int* never;             // the wait test: wait on this word (never set) instead
 };
 
-// waits for a ready flag; gives up (setting the error word) after kReadyNs of wall time or
-// kReadySpin polls, or at once when another wait already gave up
-__device__ __forceinline__ bool wait_ready(const int* flag, int* err) {
+// waits for a ready flag; gives up (setting the error word) after `ns` of wall time or
+// `spin` polls, or at once when another wait already gave up
+__device__ __forceinline__ bool wait_ready(const int* flag, int* err, uint32_t spin, uint64_t ns) {
   const uint64_t t0 = global_ns();
-  for (uint32_t it = 0; it < kReadySpin; ++it) {
+  for (uint32_t it = 0; it < spin; ++it) {
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
     if (v) return true;
     if ((it & 1023u) == 1023u) {
       if (*(volatile int*)err) return false;
-      if (global_ns() - t0 > kReadyNs) break;
+      if (global_ns() - t0 > ns) break;
     }
     __nanosleep(kPollNs);
   }
@@ -598,7 +608,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) k_split_chain(SplitArgs a) {
       for (int r = 0; r < kPre; ++r) rj[r] = cd[r] >= 0 ? a.r[(int)(uint32_t)kv[r]] : 0.0f;
 #pragma unroll
       for (int r = 0; r < kPre; ++r)
-        if (cd[r] >= 0) wait_ready(&a.ready[cd[r]], a.err);
+        if (cd[r] >= 0) wait_ready(a.never ? a.never : &a.ready[cd[r]], a.err, a.spin, a.ns);
       float4 px[kPre], ps[kPre];
 #pragma unroll
       for (int r = 0; r < kPre; ++r)
@@ -671,12 +681,14 @@ __global__ void __launch_bounds__(kChainWarps * 32) k_split_chain(SplitArgs a) {
   }
 }
 
+// writes the split's results; nothing when a wait of the chain gave up (the error word is
+// set), so that a failed call leaves the particles as they were
 __global__ void k_split_write(int m, int n, const int* __restrict__ list, const float4* __restrict__ post_x,
                               const float4* __restrict__ post_s, const float4* __restrict__ child_x,
                               const float4* __restrict__ child_s, float* x, float* y, float* z, float* r, float* elong,
-                              float* sx, float* sy, float* sz) {
+                              float* sx, float* sy, float* sz, const int* __restrict__ err) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= m) return;
+  if (k >= m || *err) return;
   const int i = list[k], c = n + k;
   const float4 px = post_x[k], ps = post_s[k], cx = child_x[k], cs = child_s[k];
   x[c] = cx.x; y[c] = cx.y; z[c] = cx.z; r[c] = r[i]; elong[c] = px.w;
@@ -942,10 +954,10 @@ struct Scratch {
   template <class T>
   int32_t get(T** p, size_t count) {
     if (count == 0) count = 1;
-    const cudaError_t e = cudaMallocAsync((void**)p, count * sizeof(T), st);
+    const cudaError_t e = o3g::dev_alloc_async((void**)p, count * sizeof(T), st);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
-      set_error_cuda("cudaMallocAsync(split/merge scratch)", e);
+      set_error_cuda("o3g::dev_alloc_async(split/merge scratch)", e);
       return O3G_ERR_ALLOC;
     }
     ptrs.push_back(*p);
@@ -1064,10 +1076,14 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   int *lo_ord = nullptr, *rmax = nullptr, *flag = nullptr, *rank = nullptr, *err = nullptr;
   O3G_TRY(sc.get(&lo_ord, 6));
   O3G_TRY(sc.get(&rmax, 1));
-  O3G_TRY(sc.get(&err, 3));   // error word, chain claim counter, level claim counter
+  O3G_TRY(sc.get(&err, 4));   // error word, chain and level claim counters, a word never set
   O3G_TRY(sc.get(&flag, (size_t)n + 1));
   O3G_TRY(sc.get(&rank, (size_t)n + 1));
-  O3G_CUDA_TRY(cudaMemsetAsync(err, 0, 3 * sizeof(int), st));
+  O3G_CUDA_TRY(cudaMemsetAsync(err, 0, 4 * sizeof(int), st));
+  const bool wtest = wait_test_on();
+  const uint32_t wspin = wtest ? kTestSpin : kReadySpin;
+  const uint64_t wns = wtest ? kTestNs : kReadyNs;
+  const int* never = wtest ? err + 3 : nullptr;
   k_sm_init<<<1, 32, 0, st>>>(lo_ord, rmax);
   k_split_flag<<<blocks(n), 256, 0, st>>>(n, elong, r, overlap, threshold, flag, rmax);
   O3G_CUDA_TRY(cudaMemsetAsync(flag + n, 0, sizeof(int), st));
@@ -1140,7 +1156,7 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
     // with a thread for every particle all of them are in flight at once, so any mapping is
     // deadlock-free; otherwise they are claimed in rank order
     const int spread = (long long)lgrid * 256 >= (long long)m ? 1 : 0;
-    LevelArgs la{m, off, dep, ndep, lvl1, err + 2, err, spread};
+    LevelArgs la{m, off, dep, ndep, lvl1, err + 2, err, spread, wspin, wns, never};
     void* largs[] = {&la};
     O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_split_levels, dim3(lgrid), dim3(256), largs, 0, st));
   }
@@ -1169,6 +1185,7 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   a.coef = coef;
   a.post_x = post_x; a.post_s = post_s; a.child_x = child_x; a.child_s = child_s;
   a.ready = ready; a.claim = err + 1; a.err = err;
+  a.spin = wspin; a.ns = wns; a.never = never;
   int nb = 0;
   O3G_TRY(occupancy_blocks((const void*)k_split_chain, kChainWarps * 32, &nb));
   int grid = std::max(1, nb) * f.num_sms;
@@ -1177,7 +1194,7 @@ int32_t split_run(int n, int cap, float* x, float* y, float* z, float* r, float*
   O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_split_chain, dim3(grid), dim3(kChainWarps * 32), args, 0,
                                            st));
   k_split_write<<<blocks(m), 256, 0, st>>>(m, n, list, post_x, post_s, child_x, child_s, x, y, z, r, elong, sx, sy,
-                                           sz);
+                                           sz, err);
   note_launch(2);
   O3G_CUDA_TRY(cudaGetLastError());
   return check_err(err, st, "o3g_split_elongated: a device-side check failed (ready-flag wait or match count)");

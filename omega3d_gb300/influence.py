@@ -78,6 +78,24 @@ def _rows(a, k):
     return [b + i * n * item for i in range(k)]
 
 
+class _DeviceArray:
+    """A device buffer described by __cuda_array_interface__ (torch wraps it without a copy)."""
+
+    def __init__(self, ptr, shape, strides, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "strides": tuple(strides), "typestr": typestr,
+                                         "data": (int(ptr), False), "version": 2}
+
+
+def device_matrix_view(base, ld, nrows, ncols=None):
+    """The column-major FP32 matrix at device address `base` (leading dimension ld), e.g. the
+    BEM handle's (BEM.matrix()), as a torch tensor M of shape (ncols, nrows) whose row j is
+    column j of the matrix.  A view of that memory: no copy, no allocation."""
+    if torch is None:
+        raise RuntimeError("device_matrix_view needs torch")
+    ncols = nrows if ncols is None else ncols
+    return torch.as_tensor(_DeviceArray(base, (ncols, nrows), (4 * ld, 4), "<f4"), device="cuda")
+
+
 class Points:
     """Points<S> (Points.h:50-140): positions x[3,n], strengths s[3,n], core radii r[n],
     velocities u[3,n] and optional gradients ug[9,n].  `inert` marks field points

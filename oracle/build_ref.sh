@@ -25,12 +25,14 @@
 # (so the igl headers do not pull in the rest of igl), against oracle/eigen_shim_igl (a
 # stand-in for the Eigen members they use), with oracle/ref_ovoid_driver.cpp.
 #
-# The reference location defaults to /root/reference/src; set O3D_REFERENCE_SRC to
-# override.  When the sources are absent (e.g. on a machine without the reference) the
-# script prints a note and exits 0: the ref libraries are a checker, not the product.
+# The reference is looked for in a checkout named `reference` beside this repository's
+# checkout (../reference/src relative to the repository root); set O3D_REFERENCE_SRC to
+# its src/ directory to use another location.  When the sources are absent (e.g. on a
+# machine without the reference) the script prints a note and exits 0: the ref libraries
+# are a checker, not the product.
 set -e
-REF="${O3D_REFERENCE_SRC:-/root/reference/src}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${O3D_REFERENCE_SRC:-$(dirname "$(dirname "$HERE")")/reference/src}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/Kernels.h" ] || [ ! -f "$REF/CoreFunc.h" ] || [ ! -f "$REF/MathHelper.h" ]; then
   echo "build_ref: reference sources not found under $REF; oracle/_ref not built"

@@ -10,6 +10,7 @@ oracle/ref_splitmerge_driver.cpp):
     sh oracle/build_ref.sh && python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py --only reflect                       # reflect.npz alone
     python tests/golden/make_golden.py --only splitmerge                    # splitmerge*.npz alone
+    python tests/golden/make_golden.py --only edges                         # branch_edges.npz alone
 
 Every fixture holds its seeded inputs and the outputs of the reference build for the
 precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
@@ -129,7 +130,55 @@ def write_splitmerge_tied():
           x_in=x, s_in=s, r_in=r, e_in=e, xd_in=xd, sd_in=sd, rd_in=rd, **out)
 
 
+def branch_edge_inputs():
+    """One source at the origin and targets where the cores switch form: d^3/sigma^3 just
+    below, at and above 0.001 and 16 (the exponential core's branches, CoreFunc.h:119-177)
+    and 332.55 (q = d^2/sigma^2 = 48, the Gaussian core's far-field switch), d = 0, and
+    d^3/sigma^3 from 1e-12 to 1e9, each in 4 random directions.  Particle targets carry
+    sigma_t = sigma_s, so their combined core is 2 sigma^3 (EXP) or 2 sigma^2; field points
+    have sigma_s alone.  Returns the inputs and, per target kind, the d^3/sigma^3 values."""
+    rng = np.random.default_rng(37)
+    sig = np.float32(0.05)
+    rel = np.array([0.0] + [v * f for v in (1e-3, 16.0, 332.55) for f in (0.999, 1.0, 1.001)]
+                   + [1e-12, 1e-9, 1e-6, 0.1, 1.0, 4.0, 1e3, 1e9])
+    rel = np.repeat(rel, 4)
+    d = rng.normal(size=(3, rel.size))
+    d /= np.linalg.norm(d, axis=0)
+    sx = np.zeros((3, 1), np.float32)
+    ss = np.array([[0.3], [-0.2], [0.5]], np.float32)
+    sr = np.array([sig], np.float32)
+    tr = np.full(rel.size, sig, np.float32)
+    tx_p = (d * np.cbrt(rel * 2.0 * float(sig) ** 3)).astype(np.float32)
+    tx_f = (d * np.cbrt(rel * float(sig) ** 3)).astype(np.float32)
+    return dict(sx=sx, ss=ss, sr=sr, tr=tr, tx_p=tx_p, tx_f=tx_f, rel=rel)
+
+
+def write_branch_edges():
+    """Per-pair outputs at the cores' branch edges from the reference kernels (RM, WL, EXP,
+    V2; the Gaussian core from the oracle restatement) at prec 0 and 2."""
+    for core in O.REF_CORES:
+        if not O.ref_available(core):
+            raise SystemExit("oracle/_ref/libo3dref_%s.so missing: run sh oracle/build_ref.sh" % core)
+    inp = branch_edge_inputs()
+    out = {}
+    for core in ("rm", "wl", "exp", "v2", "gauss"):
+        use_ref = core != "gauss"
+        for prec in (0, 2):
+            for tag, tx, tr in (("pg", inp["tx_p"], inp["tr"]), ("fg", inp["tx_f"], None)):
+                u, g = O.points_affect_points(inp["sx"], inp["sr"], inp["ss"], tx, tr, True, core, prec,
+                                              use_ref=use_ref)
+                out["%s_%s_u_p%d" % (core, tag, prec)], out["%s_%s_g_p%d" % (core, tag, prec)] = u, g
+            u, _ = O.points_affect_points(inp["sx"], inp["sr"], inp["ss"], inp["tx_p"], inp["tr"], False, core,
+                                          prec, use_ref=use_ref)
+            out["%s_pv_u_p%d" % (core, prec)] = u
+    _save("branch_edges.npz", {"pinned": {c: c != "gauss" for c in ("rm", "wl", "exp", "v2", "gauss")},
+                               "source": "reference kernels (gauss: oracle restatement)"}, **inp, **out)
+
+
 def main():
+    if "--only" in sys.argv and sys.argv[-1] == "edges":
+        write_branch_edges()
+        return
     if "--only" in sys.argv and sys.argv[-1] == "reflect":
         write_reflect()
         return
@@ -186,6 +235,7 @@ def main():
     write_sphere()
     write_reflect()
     write_splitmerge()
+    write_branch_edges()
 
 
 def write_sphere():

@@ -67,7 +67,7 @@ def _prototypes():
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     txt = re.sub(r"//[^\n]*", "", txt)
     out = {}
-    for m in re.finditer(r"\b(o3g_[a-z0-9_]+)\s*\(([^;{}]*?)\)\s*;", txt, flags=re.S):
+    for m in re.finditer(r"\b(o3g_[a-z0-9_]+|external_vel_solver_[fd]_)\s*\(([^;{}]*?)\)\s*;", txt, flags=re.S):
         args = m.group(2).strip()
         out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
     return out
@@ -88,3 +88,59 @@ def test_bindings_match_header_prototypes(built_lib):
             bad.append((name, nargs, len(fn.argtypes)))
     assert not bad, "argtypes count differs from the prototype: %s" % bad
     assert checked >= 30
+
+
+def test_external_hook_method_and_validation(built_lib):
+    """The reference's hook symbols: method selection, and the checks made before any
+    device is touched (null counts; an empty source set adds nothing and still returns the
+    reference's per-target flop count)."""
+    c, p = ctypes.c_int32(), ctypes.c_int32()
+    assert built_lib.o3g_external_set_method(-1, -1) == 0
+    assert built_lib.o3g_external_get_method(ctypes.byref(c), ctypes.byref(p)) == 0
+    import os
+    if "O3G_EXTERNAL_CORE" not in os.environ and "O3G_EXTERNAL_PREC" not in os.environ:
+        assert (c.value, p.value) == (1, 0)          # WL, PLAIN: CoreFunc.h:37 and the float path
+    assert built_lib.o3g_external_set_method(0, 1) == 0
+    assert built_lib.o3g_external_get_method(ctypes.byref(c), ctypes.byref(p)) == 0
+    assert (c.value, p.value) == (0, 1)
+    assert built_lib.o3g_external_set_method(7, 0) == 1
+    assert built_lib.o3g_external_set_method(-1, -1) == 0
+    nul = [None] * 22
+    assert built_lib.external_vel_solver_f_(None, *nul, None) == -1.0
+    ns, nt = ctypes.c_int(0), ctypes.c_int(5)
+    t = np.zeros(5, np.float32)
+    args = [ctypes.byref(ns)] + [None] * 7 + [ctypes.byref(nt)] + [t.ctypes.data] * 15
+    assert built_lib.external_vel_solver_f_(*args) == 5 * 12.0
+    td = np.zeros(5, np.float64)
+    args = [ctypes.byref(ns)] + [None] * 7 + [ctypes.byref(nt)] + [td.ctypes.data] * 15
+    assert built_lib.external_vel_solver_d_(*args) == 5 * 12.0
+
+
+def test_reference_hook_declarations_compile_against_the_header(built_lib, tmp_path):
+    """The reference's own EXTERNAL_VEL_SOLVE declarations (Influence.h:33-48), compiled in
+    one C++ translation unit with include/o3dgpu.h and linked with libo3dgpu.so: a
+    declaration whose types differed from the library's would not compile (two extern "C"
+    declarations of one name must agree).  Needs the reference sources beside this checkout."""
+    import os
+    import re
+    import subprocess
+    src = os.environ.get("O3D_REFERENCE_SRC") or os.path.join(
+        os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(L.HEADER)))), "reference", "src")
+    path = os.path.join(src, "Influence.h")
+    if not os.path.exists(path):
+        pytest.skip("reference sources not present")
+    txt = open(path).read()
+    m = re.search(r"#ifdef EXTERNAL_VEL_SOLVE\n(.*?)#endif", txt, flags=re.S)
+    assert m and "external_vel_solver_f_" in m.group(1)
+    tu = tmp_path / "hook.cpp"
+    tu.write_text('#include "o3dgpu.h"\n' + m.group(1) + '''
+int main() {
+  int ns = 0, nt = 0;
+  float* p = nullptr;
+  return (int)external_vel_solver_f_(&ns, p, p, p, p, p, p, p, &nt, p, p, p,
+                                     p, p, p, p, p, p, p, p, p, p, p, p);
+}
+''')
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.dirname(L.HEADER), str(tu), "-o", str(tmp_path / "hook"),
+                        L.LIB_PATH, "-Wl,--unresolved-symbols=ignore-in-shared-libs"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

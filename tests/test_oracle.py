@@ -36,6 +36,19 @@ def test_oracle_matches_golden_pairs(core):
         assert _exact(u, d["pv_u_p%d" % prec])
 
 
+@pytest.mark.parametrize("core", ["rm", "wl", "exp", "v2", "gauss"])
+def test_oracle_matches_golden_branch_edges(core):
+    """The per-pair fixture at the cores' branch edges (from the reference kernels), bit for bit."""
+    d, meta = _gold("branch_edges.npz")
+    assert meta["pinned"][core] == (core != "gauss")
+    for prec in (0, 2):
+        for tag, tx, tr in (("pg", d["tx_p"], d["tr"]), ("fg", d["tx_f"], None)):
+            u, g = O.points_affect_points(d["sx"], d["sr"], d["ss"], tx, tr, True, core, prec)
+            assert _exact(u, d["%s_%s_u_p%d" % (core, tag, prec)]) and _exact(g, d["%s_%s_g_p%d" % (core, tag, prec)])
+        u, _ = O.points_affect_points(d["sx"], d["sr"], d["ss"], d["tx_p"], d["tr"], False, core, prec)
+        assert _exact(u, d["%s_pv_u_p%d" % (core, prec)])
+
+
 @pytest.mark.parametrize("core", ["rm", "wl", "exp"])
 def test_oracle_matches_golden_panels(core):
     d, meta = _gold("panel_%s.npz" % core)
