@@ -23,7 +23,9 @@
 # triangle_triangle_adjacency.cpp, vertex_triangle_adjacency.cpp and cumsum.cpp, each
 # streamed up to its explicit-instantiation block and compiled with IGL_STATIC_LIBRARY
 # (so the igl headers do not pull in the rest of igl), against oracle/eigen_shim_igl (a
-# stand-in for the Eigen members they use), with oracle/ref_ovoid_driver.cpp.
+# stand-in for the Eigen members they use), with oracle/ref_ovoid_driver.cpp,
+# and oracle/_ref/libo3dref_vtk.so from the reference's src/VtkXmlWriter.h with the vendored
+# lib/tinyxml2 (tinyxml2.cpp compiled) and lib/cppcodec, driven by oracle/ref_vtk_driver.cpp.
 #
 # The reference is looked for in a checkout named `reference` beside this repository's
 # checkout (../reference/src relative to the repository root); set O3D_REFERENCE_SRC to
@@ -92,4 +94,9 @@ if [ -f "$REF/GeomHelper.cpp" ] && [ -f "$REF/IglRefine.cpp" ] && [ -f "$IGL/ups
   } | "$CXX" -std=c++17 -O2 -ffp-contract=off -fPIC -shared -w -I"$REF" -I"$NANOFLANN" -I"$IGL" \
         -I"$HERE/eigen_shim_igl" -x c++ - -o "$OUT/libo3dref_ovoid.so"
   echo "build_ref: built $OUT/libo3dref_ovoid.so"
+fi
+if [ -f "$REF/VtkXmlWriter.h" ] && [ -f "$NANOFLANN/tinyxml2/tinyxml2.cpp" ] && [ -d "$NANOFLANN/cppcodec" ]; then
+  "$CXX" -std=c++17 -O2 -fPIC -shared -w -I"$REF" -I"$NANOFLANN" "$NANOFLANN/tinyxml2/tinyxml2.cpp" \
+        "$HERE/ref_vtk_driver.cpp" -o "$OUT/libo3dref_vtk.so"
+  echo "build_ref: built $OUT/libo3dref_vtk.so"
 fi

@@ -498,3 +498,59 @@ def gmres_restarted(A, b, restart=30, tol=None, max_iter=None):
     bn = np.linalg.norm(b.astype(np.float64))
     rel = float(np.linalg.norm(b.astype(np.float64) - A.astype(np.float64) @ x.astype(np.float64)) / bn)
     return x, it, rel
+
+
+# ---- the reference's VTU writer (oracle/_ref/libo3dref_vtk.so) -------------------------
+def ref_vtk_available():
+    return os.path.exists(os.path.join(REF_DIR, "libo3dref_vtk.so"))
+
+
+def _vtk_lib():
+    if "vtk" not in _ref:
+        path = os.path.join(REF_DIR, "libo3dref_vtk.so")
+        if not os.path.exists(path):
+            raise RuntimeError("oracle/_ref/libo3dref_vtk.so missing: run sh oracle/build_ref.sh")
+        _ref["vtk"] = ctypes.CDLL(path)
+    return _ref["vtk"]
+
+
+def ref_write_points_vtu(path, x, u, s=None, r=None, time=0.0):
+    """The reference's VtkXmlWriter driven as Points::write_vtk drives it (Points.h:851-1039):
+    particles with strengths s[3, n] and radii r[n], or field points (s, r None)."""
+    f = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    x, u = f(x), f(u)
+    n = x.shape[1]
+    if s is not None:
+        s, r = f(s), f(r)
+        sp = [_p(s[0]), _p(s[1]), _p(s[2])]
+        rp = _p(r)
+    else:
+        sp, rp = [None] * 3, None
+    rc = _vtk_lib().ref_write_points_vtu(path.encode(), ctypes.c_int(n), _p(x[0]), _p(x[1]), _p(x[2]), *sp, rp,
+                                         _p(u[0]), _p(u[1]), _p(u[2]), ctypes.c_double(time))
+    if rc != 0:
+        raise RuntimeError("reference VTU writer failed")
+    return path
+
+
+def ref_write_panels_vtu(path, nodes, idx, sheet=None, src=None, time=0.0):
+    """The reference's VtkXmlWriter driven as Surfaces::write_vtk drives it
+    (Surfaces.h:1301-1458): triangles over the nodes, the vortex sheet vector per panel and
+    the source sheet strength as cell data when given."""
+    f = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    x = f(nodes)
+    ix = np.ascontiguousarray(idx, np.uint32).reshape(-1)
+    npan = ix.size // 3
+    tp = [None] * 3
+    if sheet is not None:
+        sheet = f(sheet)
+        tp = [_p(sheet[0]), _p(sheet[1]), _p(sheet[2])]
+    sp = None
+    if src is not None:
+        src = f(src)
+        sp = _p(src)
+    rc = _vtk_lib().ref_write_panels_vtu(path.encode(), ctypes.c_int(x.shape[1]), _p(x[0]), _p(x[1]), _p(x[2]),
+                                         ctypes.c_int(npan), _p(ix), *tp, sp, ctypes.c_double(time))
+    if rc != 0:
+        raise RuntimeError("reference VTU writer failed")
+    return path

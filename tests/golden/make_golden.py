@@ -11,6 +11,7 @@ oracle/ref_splitmerge_driver.cpp):
     python tests/golden/make_golden.py --only reflect                       # reflect.npz alone
     python tests/golden/make_golden.py --only splitmerge                    # splitmerge*.npz alone
     python tests/golden/make_golden.py --only edges                         # branch_edges.npz alone
+    python tests/golden/make_golden.py --only vtk                           # vtk_files.npz alone
 
 Every fixture holds its seeded inputs and the outputs of the reference build for the
 precisions named in it:  prec 0 = S=A=float (Vc build semantics), prec 2 = S=A=double.
@@ -175,7 +176,48 @@ def write_branch_edges():
                                "source": "reference kernels (gauss: oracle restatement)"}, **inp, **out)
 
 
+def vtk_inputs():
+    """Seeded particles, field points and a level-1 sphere's panels with sheet strengths."""
+    rng = np.random.default_rng(38)
+    n, nf = 37, 11
+    x = rng.normal(size=(3, n)).astype(np.float32)
+    s = rng.normal(size=(3, n)).astype(np.float32)
+    r = rng.uniform(0.01, 0.05, n).astype(np.float32)
+    u = rng.normal(size=(3, n)).astype(np.float32)
+    fx = rng.normal(size=(3, nf)).astype(np.float32)
+    fu = rng.normal(size=(3, nf)).astype(np.float32)
+    nodes, idx = O.generate_ovoid(1, 2.0, 2.0, 2.0)
+    npan = idx.size // 3
+    sheet = rng.normal(size=(3, npan)).astype(np.float32)
+    src = rng.normal(size=npan).astype(np.float32)
+    return dict(x=x, s=s, r=r, u=u, fx=fx, fu=fu, nodes=nodes, idx=idx, sheet=sheet, src=src)
+
+
+def write_vtk_golden():
+    """Files written by the reference's own VtkXmlWriter (oracle/_ref/libo3dref_vtk.so),
+    driven as Points::write_vtk and Surfaces::write_vtk drive it, stored as bytes."""
+    import tempfile
+    if not O.ref_vtk_available():
+        raise SystemExit("oracle/_ref/libo3dref_vtk.so missing: run sh oracle/build_ref.sh")
+    d = vtk_inputs()
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, "f.vtu")
+        for name, call in (("part", lambda: O.ref_write_points_vtu(f, d["x"], d["u"], d["s"], d["r"], 2.5)),
+                           ("fldpt", lambda: O.ref_write_points_vtu(f, d["fx"], d["fu"], None, None, 0.125)),
+                           ("panel3", lambda: O.ref_write_panels_vtu(f, d["nodes"], d["idx"], d["sheet"], d["src"],
+                                                                    1.0)),
+                           ("panel2", lambda: O.ref_write_panels_vtu(f, d["nodes"], d["idx"], d["sheet"], None, 1.0))):
+            call()
+            out[name] = np.frombuffer(open(f, "rb").read(), np.uint8)
+    _save("vtk_files.npz", {"pinned": True, "source": "reference VtkXmlWriter.h with lib/tinyxml2, lib/cppcodec",
+                            "times": {"part": 2.5, "fldpt": 0.125, "panel3": 1.0, "panel2": 1.0}}, **d, **out)
+
+
 def main():
+    if "--only" in sys.argv and sys.argv[-1] == "vtk":
+        write_vtk_golden()
+        return
     if "--only" in sys.argv and sys.argv[-1] == "edges":
         write_branch_edges()
         return
@@ -236,6 +278,7 @@ def main():
     write_reflect()
     write_splitmerge()
     write_branch_edges()
+    write_vtk_golden()
 
 
 def write_sphere():
