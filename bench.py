@@ -93,25 +93,35 @@ def config(args):
 
 
 # ------------------------------------------------------------------------------------
-def cpu_reference(args, nthreads=None, ntarg=None, reps=1):
-    """Times the oracle port on a bounded sample: `ntarg` targets against all sources."""
+def cpu_reference(args, nthreads=None, ntarg=None, reps=1, build=None):
+    """Times the oracle port on a bounded sample: `ntarg` targets against all sources.
+    build: "o3" (the reference's Release optimisation), "o2" (the bit-exact checker build),
+    or None: both are timed on a first sample and the faster one is used."""
     import oracle
     from omega3d_gb300 import workloads as W
     x, s, r = W.gaussian_cloud(args.n, seed=2)
     nthreads = nthreads or (os.cpu_count() or 1)
-    ntarg = ntarg or min(args.n, 4096)
+    ntarg = ntarg or min(args.n, 8192)
     # a seeded subset of the targets, against all sources; scaled to the full count by rate
     idx = np.sort(np.random.default_rng(7).choice(args.n, ntarg, replace=False)).astype(np.int64)
     tx, tr = np.ascontiguousarray(x[:, idx]), np.ascontiguousarray(r[idx])
-    oracle.points_affect_points(x[:, :4096], r[:4096], s[:, :4096], tx[:, :64], tr[:64], True, args.core, 1,
-                                nthreads)
-    times = []
-    for _ in range(reps):
+
+    def once(fast):
         t0 = time.perf_counter()
-        oracle.points_affect_points(x, r, s, tx, tr, True, args.core, 1, nthreads)
-        times.append(time.perf_counter() - t0)
+        oracle.points_affect_points(x, r, s, tx, tr, True, args.core, 1, nthreads, fast=fast)
+        return time.perf_counter() - t0
+
+    for fast in (False, True):
+        oracle.points_affect_points(x[:, :4096], r[:4096], s[:, :4096], tx[:, :64], tr[:64], True, args.core, 1,
+                                    nthreads, fast=fast)
+    if build is None:
+        build = "o3" if once(True) < once(False) else "o2"
+    times = [once(build == "o3") for _ in range(reps)]
     pairs = float(ntarg) * args.n
-    return pairs / statistics.median(times), nthreads, "%d targets x %d sources per sample" % (ntarg, args.n), times
+    flags = "-O3" if build == "o3" else "-O2 -ffp-contract=off"
+    return (pairs / statistics.median(times), nthreads,
+            "%d targets x %d sources per sample (%.1f%% of the targets); port built %s" % (
+                ntarg, args.n, 100.0 * ntarg / args.n, flags), times)
 
 
 def run_reference(args):
@@ -119,8 +129,10 @@ def run_reference(args):
     if rank != 0:
         return
     samples = []
+    build = None
     for k in range(args.warmup + args.steps):
-        v, cores, sample, _ = cpu_reference(args)
+        v, cores, sample, _ = cpu_reference(args, build=build)
+        build = "o3" if "-O3" in sample else "o2"
         if k >= args.warmup:
             samples.append(v)
     v = statistics.median(samples)
@@ -226,6 +238,8 @@ def bench_bem(args, G, torch, W, fp64=True):
             res["gmres"] = {"solve_ms": e[5].elapsed_time(e[6]), "iterations": bem.iters, "relres": bem.relres,
                             "total_ms_with_rhs_and_assembly": e[0].elapsed_time(e[2]) + e[5].elapsed_time(e[6]),
                             "strengths_vs_lu_max_rel": float(((xg - xs).abs().max() / xs.abs().max()).item())}
+            if nunk == 2 and rep == 1:
+                res["many_rhs"] = bench_many_rhs(bem, rhs, torch, ev)
         if fp64 and nunk == 2:
             A = torch.empty((n, n), device="cuda")
             G.panels_on_panels_coeff(arr, arr, nunk, True, A)
@@ -250,6 +264,39 @@ def bench_bem(args, G, torch, W, fp64=True):
         out["nunk%d" % nunk] = res
         del bem
         torch.cuda.empty_cache()
+    return out
+
+
+def bench_many_rhs(bem, rhs, torch, ev):
+    """Several right-hand sides per matrix pass (o3g_bem_solve_many / _gmres_many) on the
+    factorised sphere system: k = 1, 2, 4, 8 right-hand sides (the sphere's own RHS scaled
+    and perturbed by seeded noise of 1e-3 of its size), each solved to 1e-10; time per
+    right-hand side against one single-vector solve."""
+    g = torch.Generator(device="cuda").manual_seed(5)
+    out = {}
+    single = {}
+    for method, iters in (("lu", 30), ("gmres", 300)):
+        e0, e1 = ev(), ev()
+        e0.record()
+        bem.solve(rhs, tol=1e-10, max_iter=iters, method=method)
+        e1.record()
+        torch.cuda.synchronize()
+        single[method] = e0.elapsed_time(e1)
+    for k in (1, 2, 4, 8):
+        B = torch.stack([rhs * (1.0 + 0.1 * c) + 1e-3 * rhs.abs().max() *
+                         torch.randn(rhs.shape[0], device="cuda", generator=g) for c in range(k)])
+        row = {}
+        for method, iters in (("lu", 30), ("gmres", 300)):
+            e0, e1 = ev(), ev()
+            e0.record()
+            bem.solve_many(B, tol=1e-10, max_iter=iters, method=method)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            row[method] = {"ms": ms, "ms_per_rhs": ms / k, "per_rhs_vs_single": (ms / k) / single[method],
+                           "max_relres": float(bem.relres_many.max()), "iterations": bem.iters_many.tolist()}
+        out["k%d" % k] = row
+    out["single_ms"] = single
     return out
 
 

@@ -109,6 +109,14 @@ int32_t o3g_fp32_peak_probe(int32_t iters, void* stream, double* tflops, float* 
  * measurement; no counterpart in the reference, which calls its host library's expf. */
 int32_t o3g_exp_probe(int32_t n, const float* x, float* y, void* stream);
 
+/* C -= A B on the tensor cores (tcgen05, TF32 products, FP32 sums): the update of the BEM
+ * factorisation (o3g_bem_factor), callable on its own.  Device arrays, column-major:
+ * A m x k (leading dimension lda >= m), B k x n (ldb >= k, a multiple of 4, B 16-byte
+ * aligned), C m x n (ldc >= m).  Synchronises the stream.  No counterpart in the
+ * reference, which leaves the factorisation to Eigen on the host (BEM.h:182-195). */
+int32_t o3g_gemm_tf32_sub(int32_t m, int32_t n, int32_t k, const float* A, int64_t lda, const float* B, int64_t ldb,
+                          float* C, int64_t ldc, void* stream);
+
 /* ---- points_affect_points -------------------------------------------------------
  * Replaces points_affect_points<float,A>(src, targ, restype, env), Influence.h:67-551,
  * and generalises the external solver hook external_vel_solver_f_, Influence.h:33-40.
@@ -289,6 +297,23 @@ int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double* x64, int32
  * assembled matrix (o3g_bem_matrix / o3g_bem_set_block). */
 int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
                             int32_t max_iter, int32_t restart, int32_t* iters, double* relres, void* stream);
+/* Several right-hand sides at once: B holds nrhs vectors of n floats back to back (column c
+ * at B + c n, an n x nrhs column-major block), X (float) and X64 (double, nullable) the
+ * solutions in the same layout, iters and relres (nullable) nrhs entries.  Each refinement
+ * sweep (o3g_bem_solve_many, after o3g_bem_factor) or GMRES iteration
+ * (o3g_bem_solve_gmres_many, restart as for o3g_bem_solve_gmres) streams the matrix once for
+ * up to 8 right-hand sides, where o3g_bem_solve / o3g_bem_solve_gmres stream it once per
+ * right-hand side; larger nrhs go in groups of 8.  Every column is solved as by the
+ * single-vector entry points (refinements or GMRES iterations counted per column, converged
+ * columns frozen) until ||b_c - A x_c|| / ||b_c|| <= tol.  The reference solves one b per
+ * BEM::solve (BEM.h:200-203) and solves again per RK stage (Convection.h:197) and per
+ * diffusion step (Diffusion.h:184-187); these take all of those right-hand sides in one call.
+ * O3G_ERR_NOT_CONVERGED when any column misses tol (its relres says which). */
+int32_t o3g_bem_solve_many(o3g_bem_t* h, int32_t nrhs, const float* B, float* X, double* X64, int32_t mem,
+                           double tol, int32_t max_iter, int32_t* iters, double* relres, void* stream);
+int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const float* B, float* X, double* X64, int32_t mem,
+                                 double tol, int32_t max_iter, int32_t restart, int32_t* iters, double* relres,
+                                 void* stream);
 /* finalize_vels of panel velocities (u = fs + u/(4 pi), ElementBase.h:187-193) and
  * vels_to_rhs_panels (RHS.h:92-110) in one pass; device arrays; rhs has np*nunk entries */
 int32_t o3g_panel_vels_to_rhs(int32_t np, int32_t nunk, const double* fs, float* pu, float* pv, float* pw,

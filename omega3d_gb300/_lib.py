@@ -67,6 +67,7 @@ def _declare(l):
     l.o3g_last_error.restype = ctypes.c_char_p
     l.o3g_last_error.argtypes = []
     l.o3g_version.restype = c_i32
+    l.o3g_version.argtypes = []
     l.o3g_device_info.restype = c_i32
     l.o3g_device_info.argtypes = [P, P, P, P]
     l.o3g_flops_per_pair.restype = c_i32
@@ -85,6 +86,8 @@ def _declare(l):
     l.o3g_fp32_peak_probe.argtypes = [c_i32, P, P, P]
     l.o3g_exp_probe.restype = c_i32
     l.o3g_exp_probe.argtypes = [c_i32, P, P, P]
+    l.o3g_gemm_tf32_sub.restype = c_i32
+    l.o3g_gemm_tf32_sub.argtypes = [c_i32, c_i32, c_i32, P, ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64, P]
     l.o3g_points_affect_points.restype = c_i32
     l.o3g_points_affect_points.argtypes = [c_i32, c_i32, c_i32, c_i32] + [P] * 7 + [c_i32] + [P] * 4 + [P] * 3 + [P, P]
     for name in ("external_vel_solver_f_", "external_vel_solver_d_"):
@@ -125,6 +128,10 @@ def _declare(l):
     l.o3g_bem_solve.argtypes = [P, P, P, P, c_i32, c_d, c_i32, P, P, P]
     l.o3g_bem_solve_gmres.restype = c_i32
     l.o3g_bem_solve_gmres.argtypes = [P, P, P, P, c_i32, c_d, c_i32, c_i32, P, P, P]
+    l.o3g_bem_solve_many.restype = c_i32
+    l.o3g_bem_solve_many.argtypes = [P, c_i32, P, P, P, c_i32, c_d, c_i32, P, P, P]
+    l.o3g_bem_solve_gmres_many.restype = c_i32
+    l.o3g_bem_solve_gmres_many.argtypes = [P, c_i32, P, P, P, c_i32, c_d, c_i32, c_i32, P, P, P]
     l.o3g_panel_vels_to_rhs.restype = c_i32
     l.o3g_panel_vels_to_rhs.argtypes = [c_i32, c_i32, P, P, P, P, P, P, P]
     l.o3g_points_finalize.restype = c_i32

@@ -59,9 +59,16 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
   constexpr int NH = ACC ? NC : 1;
   constexpr int NP = ACC ? 2 * NC : NC;
   constexpr int TB = kBlock * TPT;
-  __shared__ V4<T> sp[kBlock];
-  __shared__ V4<T> sw[kBlock];
+  static_assert(std::is_same<T, float>::value, "the batched sums are FP32 (packed pair arithmetic)");
+  __shared__ float4 Q[5][kBlock / 2];   // the staged tile as source pairs (stage_pair)
   __shared__ int s_item, s_last;
+  // the Gaussian core's polynomial table, read from shared memory by the near-field pairs
+  __shared__ float gsh[C == CORE_GAUSS && std::is_same<T, float>::value ? kGaussPolyStride * kGaussPolyN : 1];
+  const float* gtab = nullptr;
+  if constexpr (C == CORE_GAUSS && std::is_same<T, float>::value) {
+    stage_gauss_table(gsh);   // visible after the first __syncthreads of the item loop
+    gtab = gsh;
+  }
   const int tid = threadIdx.x;
   // lane l of warp w handles slots wbase + 32 k (k < TPT) of the target block
   const int wbase = (tid >> 5) * (32 * TPT) + (tid & 31);
@@ -79,22 +86,27 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
     V4<T> tp[TPT];
     int tm[TPT];
     bool real[TPT];
+    float2 tt[TPT][4];
 #pragma unroll
     for (int k = 0; k < TPT; ++k) {
       tp[k] = a.tpos[tbase + 32 * k];
       tm[k] = a.tmap[tbase + 32 * k];
       real[k] = tm[k] >= 0;
+      tt[k][0] = make_float2(tp[k].x, tp[k].x);
+      tt[k][1] = make_float2(tp[k].y, tp[k].y);
+      tt[k][2] = make_float2(tp[k].z, tp[k].z);
+      tt[k][3] = make_float2(tp[k].w, tp[k].w);
     }
 
     float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
     bool live = true;
     if (CLASSIFY) live = warp_box<TPT, T>(tp, real, blo, bhi, bw);
 
-    T acc[TPT][NA];
+    float2 acc2[TPT][NA];
 #pragma unroll
     for (int k = 0; k < TPT; ++k)
 #pragma unroll
-      for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
+      for (int c = 0; c < NA; ++c) acc2[k][c] = make_float2(0.f, 0.f);
     float hi[TPT][NH], lo[TPT][NH];
 #pragma unroll
     for (int k = 0; k < TPT; ++k)
@@ -103,8 +115,7 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
 
     for (int tile = item.y; tile < item.z; ++tile) {
       __syncthreads();
-      sp[tid] = a.spos[(size_t)tile * kBlock + tid];
-      sw[tid] = a.sstr[(size_t)tile * kBlock + tid];
+      stage_pair(a.spos[(size_t)tile * kBlock + tid], a.sstr[(size_t)tile * kBlock + tid], Q, tid);
       __syncthreads();
       if constexpr (CLASSIFY) {
         if (!live) continue;
@@ -112,16 +123,22 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
         for (int hf = 0; hf < kBlock / kHalf; ++hf) {
           const int u = tile * (kBlock / kHalf) + hf;
           if (half_is_far<C, true>(a.tile_lo[u], a.tile_hi[u], blo, bhi, bw))
-            sweep_tile<CORE_SING, MODE, GRADS, true, TPT, T, NA, NC, NH, kHalf>(sp + hf * kHalf, sw + hf * kHalf, tp,
-                                                                             acc, hi, lo);
+            sweep_pairs<CORE_SING, MODE, GRADS, true, TPT, NA, NC, NH, kHalf / 2>(Q, hf * (kHalf / 2), tt, acc2, hi,
+                                                                                lo, gtab);
           else
-            sweep_tile<C, MODE, GRADS, true, TPT, T, NA, NC, NH, kHalf>(sp + hf * kHalf, sw + hf * kHalf, tp, acc,
-                                                                     hi, lo);
+            sweep_pairs<C, MODE, GRADS, true, TPT, NA, NC, NH, kHalf / 2>(Q, hf * (kHalf / 2), tt, acc2, hi, lo,
+                                                                        gtab);
         }
       } else {
-        sweep_tile<C, MODE, GRADS, true, TPT, T, NA, NC, NH>(sp, sw, tp, acc, hi, lo);
+        sweep_pairs<C, MODE, GRADS, true, TPT, NA, NC, NH, kBlock / 2>(Q, 0, tt, acc2, hi, lo, gtab);
       }
     }
+    // the two lanes of the plain sums are added here, as the last step of the sums
+    float acc[TPT][NA];
+#pragma unroll
+    for (int k = 0; k < TPT; ++k)
+#pragma unroll
+      for (int c = 0; c < NA; ++c) acc[k][c] = acc2[k][c].x + acc2[k][c].y;
     if (!ACC && GRADS) {
 #pragma unroll
       for (int k = 0; k < TPT; ++k) fold_grads(acc[k]);

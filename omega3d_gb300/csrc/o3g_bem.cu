@@ -42,43 +42,39 @@ constexpr unsigned long long kTestSpinLimit = 1ull << 14;   // the wait test's l
 
 struct Barrier {
   unsigned* count;
-  unsigned* gen;
   int* err;
   unsigned long long limit;   // polls before giving up
   unsigned extra;             // 0; 1 in the wait test: one more arrival than blocks, never met
 };
 
-// the barrier over the handle's flag words (count, generation, error), with the spin limit,
+// the barrier over the handle's flag words (arrival counter, error), with the spin limit,
 // or in the wait test the unreachable count and the short limit
 inline Barrier make_barrier(int* flags) {
   const bool test = wait_test_on();
-  return Barrier{(unsigned*)(flags + 2), (unsigned*)(flags + 3), flags, test ? kTestSpinLimit : kSpinLimit,
-                 test ? 1u : 0u};
+  return Barrier{(unsigned*)(flags + 2), flags, test ? kTestSpinLimit : kSpinLimit, test ? 1u : 0u};
 }
 
-// grid-wide barrier with a bounded spin; returns false (in every thread) once the error
-// flag is set, by a timeout here or anywhere else
+// Grid-wide barrier on one arrival counter that only grows.  The host zeroes the counter
+// before each cooperative launch (zero_barrier); the k-th barrier of the launch is passed
+// when the counter reaches k * gridDim.x.  One atomic per block and acquire loads of one
+// word: no reset or generation step on the critical path.  Bounded: returns false (in every
+// thread) once the error flag is set, by a timeout here or anywhere else.
 __device__ bool grid_sync(const Barrier& b) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* gen = b.gen;
-    const unsigned g = *gen;
     __threadfence();
     const unsigned arrived = atomicAdd(b.count, 1u) + 1u;
-    if (arrived == gridDim.x + b.extra) {
-      atomicExch(b.count, 0u);
-      __threadfence();
-      atomicAdd(b.gen, 1u);
-    } else {
-      unsigned long long it = 0;
-      while (*gen == g) {
-        if (*(volatile int*)b.err) break;
-        if (++it > b.limit) {
-          atomicExch(b.err, 1);
-          break;
-        }
-        __nanosleep(64);
+    const unsigned target = (arrived + gridDim.x - 1u) / gridDim.x * gridDim.x + b.extra;
+    unsigned long long it = 0;
+    for (;;) {
+      unsigned c;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(b.count) : "memory");
+      if (c >= target) break;
+      if ((it & 63ull) == 63ull && *(volatile int*)b.err) break;
+      if (++it > b.limit) {
+        atomicExch(b.err, 1);
+        break;
       }
     }
     __threadfence();
@@ -87,6 +83,9 @@ __device__ bool grid_sync(const Barrier& b) {
   __syncthreads();
   return ok != 0;
 }
+
+// zeroes the arrival counter of make_barrier(flags) before a cooperative launch
+inline cudaError_t zero_barrier(int* flags, cudaStream_t st) { return cudaMemsetAsync(flags + 2, 0, sizeof(int), st); }
 
 // global -> shared copy of a column-major rows x cols block (leading dimension ld), with 8
 // loads in flight per thread before the stores (a plain load->store loop is latency-bound)
@@ -307,6 +306,39 @@ __global__ void k_eye(float* E, int jb) {
   if (e < jb * jb) E[e] = (e % jb == e / jb) ? 1.f : 0.f;
 }
 
+// C[:, j] = L T[:, j] for j < ncols in FP32: L jb x jb (leading dimension jb, jb <= kNb), T
+// jb x ncols (leading dimension jb), C with leading dimension ldc.  L stays in shared memory;
+// 32 columns of T at a time, thread (r, g) sums row r of 16 of them, k in order.
+constexpr int kLeftCols = 32;
+__global__ void __launch_bounds__(256) k_left_gemm(const float* __restrict__ L, int jb, const float* __restrict__ T,
+                                                   int ncols, float* __restrict__ C, long long ldc) {
+  extern __shared__ float lsm[];
+  float* Ls = lsm;                   // [jb][jb]
+  float* Ts = lsm + (size_t)jb * jb; // [kLeftCols][jb]
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) Ls[e] = L[e];
+  const int r = threadIdx.x & (kNb - 1), g = threadIdx.x / kNb;
+  for (int c0 = blockIdx.x * kLeftCols; c0 < ncols; c0 += gridDim.x * kLeftCols) {
+    const int nc = min(kLeftCols, ncols - c0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < kLeftCols * jb; e += blockDim.x)
+      Ts[e] = (e / jb) < nc ? T[(size_t)(c0 + e / jb) * jb + e % jb] : 0.f;
+    __syncthreads();
+    if (r < jb) {
+      float acc[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] = 0.f;
+      for (int kk = 0; kk < jb; ++kk) {
+        const float l = Ls[(size_t)kk * jb + r];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[c] = fmaf(l, Ts[(size_t)(g * 16 + c) * jb + kk], acc[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (g * 16 + c < nc) C[(size_t)(c0 + g * 16 + c) * ldc + r] = acc[c];
+    }
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // solves with the factors: y = P b (gather), L y = y (unit lower), U x = y (upper)
 __global__ void k_permute_to_float(const double* r, const int* perm, float* y, int n) {
@@ -440,12 +472,15 @@ struct TrsvArgs {
   const float* dinv;
   long long ld;
   int n;
-  float* y;
+  float* y;     // right-hand side, overwritten by the partial updates
+  float* out;   // the solution: each segment, once final (never read by the kernel)
   Barrier bar;
 };
 
 // forward substitution with the unit lower factor: per block column, every block applies
-// the block's inverse to the (final) y segment, then updates its share of the rows below
+// the block's inverse to the (final) y segment, then updates its share of the rows below;
+// block 0 stores the solved segment in `out`, which no block reads, so it cannot overtake
+// another block still reading that segment of y
 __global__ void __launch_bounds__(kSolveThreads) k_trsv_lower(TrsvArgs a) {
   __shared__ float yd[kNb], yin[kNb];
   __shared__ float part[kSolveThreads];
@@ -457,7 +492,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_trsv_lower(TrsvArgs a) {
     const int chunk = (rest + G - 1) / G;
     const int i0 = k0 + jb + blockIdx.x * chunk, i1 = min(a.n, i0 + chunk);
     update_rows(a.LU, a.ld, k0, jb, i0, i1, yd, a.y, part);
-    if (blockIdx.x == 0 && threadIdx.x < jb) a.y[k0 + threadIdx.x] = yd[threadIdx.x];
+    if (blockIdx.x == 0 && threadIdx.x < jb) a.out[k0 + threadIdx.x] = yd[threadIdx.x];
     if (!grid_sync(a.bar)) return;
   }
 }
@@ -474,7 +509,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_trsv_upper(TrsvArgs a) {
     const int chunk = (k0 + G - 1) / G;
     const int i0 = blockIdx.x * chunk, i1 = min(k0, i0 + chunk);
     update_rows(a.LU, a.ld, k0, jb, i0, i1, yd, a.y, part);
-    if (blockIdx.x == 0 && threadIdx.x < jb) a.y[k0 + threadIdx.x] = yd[threadIdx.x];
+    if (blockIdx.x == 0 && threadIdx.x < jb) a.out[k0 + threadIdx.x] = yd[threadIdx.x];
     if (!grid_sync(a.bar)) return;
   }
 }
@@ -633,7 +668,9 @@ struct o3g_bem {
   float* dinv = nullptr;  // inverses of the diagonal blocks of L and U
   char* scratch = nullptr;
   size_t scratch_bytes = 0;
-  int* flags = nullptr;   // [0] barrier error, [1] singular column + 1, [2..3] barrier count/gen
+  int* flags = nullptr;   // [0] barrier error, [1] singular column + 1, [2] barrier arrivals,
+                          // [4] tensor-core update error
+  float* tcw = nullptr;   // K-major copies of the update's left operand (n x 512)
   cublasHandle_t cublas = nullptr;
   bool factored = false;
   int panel_blocks = 0, solve_blocks = 0;
@@ -694,7 +731,6 @@ extern "C" int32_t o3g_bem_create(int64_t n, o3g_bem_t** out) {
     delete h;
     return O3G_ERR_CUDA;
   }
-  cublasSetMathMode(h->cublas, CUBLAS_TF32_TENSOR_OP_MATH);
   *out = h;
   return O3G_OK;
 }
@@ -704,6 +740,7 @@ extern "C" int32_t o3g_bem_destroy(o3g_bem_t* h) {
   cudaDeviceSynchronize();
   cudaFree(h->A); cudaFree(h->LU); cudaFree(h->piv); cudaFree(h->perm); cudaFree(h->flags); cudaFree(h->scratch);
   cudaFree(h->dinv);
+  cudaFree(h->tcw);
   if (h->cublas) cublasDestroy(h->cublas);
   h->A = nullptr;
   delete h;
@@ -790,23 +827,23 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   O3G_CUDA_TRY(cudaMemsetAsync(h->flags, 0, 64 * sizeof(int), st));
   O3G_CUDA_TRY(cudaMemcpy2DAsync(h->LU, ld * sizeof(float), h->A, ld * sizeof(float), n * sizeof(float), n,
                                  cudaMemcpyDeviceToDevice, st));
-  cublasSetStream(h->cublas, st);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
-  const float minus1 = -1.f, one = 1.f;
   const size_t tsm = (size_t)kNb * kNb * sizeof(float);
   O3G_CUDA_TRY(cudaFuncSetAttribute(k_trsm_unit_lower, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-  // C = C - A B with TF32 tensor cores (all operands column-major in LU)
-  auto gemm = [&](int m, int nn, int kk, const float* Am, const float* Bm, float* Cm) -> int32_t {
-    if (m <= 0 || nn <= 0 || kk <= 0) return O3G_OK;
-    const cublasStatus_t cs = cublasGemmEx(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, nn, kk, &minus1, Am, CUDA_R_32F,
-                                           (int)ld, Bm, CUDA_R_32F, (int)ld, &one, Cm, CUDA_R_32F, (int)ld,
-                                           CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT);
-    if (cs != CUBLAS_STATUS_SUCCESS) {
-      set_error("o3g_bem_factor: cublasGemmEx (TF32 update) failed");
-      return O3G_ERR_CUDA;
+  // C = C - A B on the tensor cores (o3g_tcgemm.cu: tcgen05, TF32 products, FP32 sums; all
+  // operands column-major in LU); the error word of its pipeline waits is flags[4]
+  if (!h->tcw) {
+    const cudaError_t e = o3g::dev_alloc((void**)&h->tcw, tc_gemm_scratch_floats(n, 512) * sizeof(float));
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      h->tcw = nullptr;
+      set_error_cuda("o3g_bem_factor: tensor-core scratch", e);
+      return O3G_ERR_ALLOC;
     }
-    return O3G_OK;
+  }
+  auto gemm = [&](int m, int nn, int kk, const float* Am, const float* Bm, float* Cm) -> int32_t {
+    return tc_gemm_sub(m, nn, kk, Am, ld, Bm, ld, Cm, ld, h->tcw, h->flags + 4, st);
   };
   auto trsm = [&](int k0, int jb, int c0, int ncols) {
     if (ncols <= 0) return;
@@ -817,8 +854,10 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
     note_launch();
   };
   // the same solve for a wide right-hand side: Linv = L11^-1 once (TRSM on the identity),
-  // then B <- Linv B as an FP32 GEMM through a scratch copy
+  // then B <- Linv B as an FP32 product (k_left_gemm) through a scratch copy
   float* linv = cv.take<float>((size_t)kNb * kNb);
+  const size_t lsm_bytes = ((size_t)kNb * kNb + (size_t)kLeftCols * kNb) * sizeof(float);
+  O3G_CUDA_TRY(cudaFuncSetAttribute(k_left_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm_bytes));
   float* tmp = cv.take<float>((size_t)kNb * n);
   auto trsm_wide = [&](int k0, int jb, int c0, int ncols) -> int32_t {
     if (ncols <= 0) return O3G_OK;
@@ -829,14 +868,9 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
     float* B = h->LU + (size_t)c0 * ld + k0;
     O3G_CUDA_TRY(cudaMemcpy2DAsync(tmp, (size_t)jb * sizeof(float), B, ld * sizeof(float), (size_t)jb * sizeof(float),
                                    ncols, cudaMemcpyDeviceToDevice, st));
-    const float zero = 0.f;
-    const cublasStatus_t cs = cublasGemmEx(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, jb, ncols, jb, &one, linv, CUDA_R_32F,
-                                           jb, tmp, CUDA_R_32F, jb, &zero, B, CUDA_R_32F, (int)ld,
-                                           CUBLAS_COMPUTE_32F_PEDANTIC, CUBLAS_GEMM_DEFAULT);
-    if (cs != CUBLAS_STATUS_SUCCESS) {
-      set_error("o3g_bem_factor: cublasGemmEx (triangular solve) failed");
-      return O3G_ERR_CUDA;
-    }
+    const int lb = std::min((ncols + kLeftCols - 1) / kLeftCols, 2 * df.num_sms);
+    k_left_gemm<<<lb, 256, lsm_bytes, st>>>(linv, jb, tmp, ncols, B, ld);
+    note_launch();
     return O3G_OK;
   };
   auto laswp = [&](int p0, int p1, int c0, int c1, int s0, int s1) {
@@ -868,6 +902,7 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
       pa.bar = make_barrier(h->flags);
       void* args[] = {&pa};
       const size_t sm = ((size_t)jb * r + jb + 32) * sizeof(float);
+      O3G_CUDA_TRY(zero_barrier(h->flags, st));
       O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_panel_lu, dim3(g), dim3(kPanelThreads), args, sm, st));
       note_launch();
       // interchanges inside the outer panel; the other columns get them once per outer panel
@@ -896,13 +931,17 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   }
   tm.end(st);
   O3G_CUDA_TRY(cudaGetLastError());
-  int fl[2] = {0, 0};
-  O3G_CUDA_TRY(cudaMemcpyAsync(fl, h->flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  int fl[5] = {0, 0, 0, 0, 0};
+  O3G_CUDA_TRY(cudaMemcpyAsync(fl, h->flags, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
   std::vector<int> piv(n);
   O3G_CUDA_TRY(cudaMemcpyAsync(piv.data(), h->piv, n * sizeof(int), cudaMemcpyDeviceToHost, st));
   O3G_CUDA_TRY(cudaStreamSynchronize(st));
   if (fl[0]) {
     set_error("o3g_bem_factor: a grid barrier timed out");
+    return O3G_ERR_TIMEOUT;
+  }
+  if (fl[4]) {
+    set_error("o3g_bem_factor: a wait of the tensor-core update timed out");
     return O3G_ERR_TIMEOUT;
   }
   // compose the interchanges into one gather permutation
@@ -972,10 +1011,14 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   const size_t dsm = 0;
   O3G_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower, kSolveThreads, dsm));
   if (per_sm < 1) return O3G_ERR_CUDA;
-  TrsvArgs ta;
-  ta.LU = h->LU; ta.dinv = h->dinv; ta.ld = ld; ta.n = n; ta.y = y;
+  // L w = P r (y -> w; xh is free between the products), then U y = w (w -> y)
+  TrsvArgs ta, tb;
+  ta.LU = h->LU; ta.dinv = h->dinv; ta.ld = ld; ta.n = n; ta.y = y; ta.out = xh;
   ta.bar = make_barrier(h->flags);
+  tb = ta;
+  tb.y = xh; tb.out = y;
   void* targs[] = {&ta};
+  void* tbargs[] = {&tb};
   std::vector<double> hn((size_t)nrb);
   double rel = 1.0, bnorm = 0.0;
   int it = 0;
@@ -998,8 +1041,10 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
     rel = bnorm > 0.0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
     if (rel <= tol || it == max_iter) break;
     k_permute_to_float<<<nrb, 256, 0, st>>>(rd, h->perm, y, n);
+    O3G_CUDA_TRY(zero_barrier(h->flags, st));
     O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_lower, dim3(G), dim3(kSolveThreads), targs, dsm, st));
-    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_upper, dim3(G), dim3(kSolveThreads), targs, dsm, st));
+    O3G_CUDA_TRY(zero_barrier(h->flags, st));
+    O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_upper, dim3(G), dim3(kSolveThreads), tbargs, dsm, st));
     k_axpy_f2d<<<nrb, 256, 0, st>>>(xd, y, n);
     note_launch(4);
   }
@@ -1194,6 +1239,650 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
     std::snprintf(msg, sizeof(msg), "o3g_bem_solve_gmres: relative residual %.3e after %d iterations (tol %.1e)", rel,
                   total, tol);
     set_error(msg);
+    return O3G_ERR_NOT_CONVERGED;
+  }
+  return O3G_OK;
+}
+
+// =====================================================================================
+// Several right-hand sides per pass over the matrix.  Each refinement sweep and each
+// GMRES iteration of one right-hand side streams the n^2 FP32 matrix once (6.7 GB at
+// n = 40,960): the products, the triangular solves and the Krylov steps below serve up to
+// kMaxRhs right-hand sides with that one pass.  BEM::solve takes one b (BEM.h:200-203); the
+// reference solves again per RK stage (Convection.h:197) and per diffusion step
+// (Diffusion.h:184-187), and these entry points let a caller hand all of them over at once.
+namespace o3g {
+
+constexpr int kMaxRhs = 8;
+constexpr int kMvChunkM = 512;   // columns per block of the multi-vector product
+
+struct DIn { const double* p[kMaxRhs]; };
+struct DOut { double* p[kMaxRhs]; };
+
+// xh/xl[c][.] = the float split of src.p[c] (K vectors of n)
+__global__ void k_split_f64_multi(DIn src, float* xh, float* xl, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (i >= n) return;
+  const double v = src.p[c][i];
+  const float h = (float)v;
+  xh[(size_t)c * n + i] = h;
+  xl[(size_t)c * n + i] = (float)(v - (double)h);
+}
+
+// part[cb][c][i] = sum over the columns of chunk cb of A[i, j] x_c[j], double-single as in
+// k_matvec_ds: every matrix element is loaded once for the K vectors
+template <int K>
+__global__ void __launch_bounds__(256) k_matvec_ds_multi(const float* __restrict__ A, long long ld, int n,
+                                                         const float* __restrict__ xh, const float* __restrict__ xl,
+                                                         double* __restrict__ part) {
+  __shared__ float sh[K][kMvChunkM], sl[K][kMvChunkM];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cb = blockIdx.y;
+  const int j0 = cb * kMvChunkM, m = min(n - j0, kMvChunkM);
+#pragma unroll
+  for (int c = 0; c < K; ++c)
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+      sh[c][k] = xh[(size_t)c * n + j0 + k];
+      sl[c][k] = xl[(size_t)c * n + j0 + k];
+    }
+  __syncthreads();
+  if (i >= n) return;
+  const float* a = A + (size_t)j0 * ld + i;
+  float hi[K], lo[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
+  int k = 0;
+  for (; k + 8 <= m; k += 8) {
+    float av[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) av[q] = __ldg(a + (size_t)(k + q) * ld);
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+#pragma unroll
+      for (int c = 0; c < K; ++c) ds_add_product(av[q], sh[c][k + q], sl[c][k + q], hi[c], lo[c]);
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      const float s2 = __fadd_rn(hi[c], lo[c]);
+      lo[c] = __fsub_rn(lo[c], __fsub_rn(s2, hi[c]));
+      hi[c] = s2;
+    }
+  }
+  for (; k < m; ++k) {
+    const float av = __ldg(a + (size_t)k * ld);
+#pragma unroll
+    for (int c = 0; c < K; ++c) ds_add_product(av, sh[c][k], sl[c][k], hi[c], lo[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < K; ++c) part[((size_t)cb * K + c) * n + i] = (double)hi[c] + (double)lo[c];
+}
+
+// y_c = b_c - sum_cb part (b given) or y_c = sum_cb part, c = blockIdx.y < K; per-block sums
+// of y_c^2 into nrm[c][blockIdx.x]
+__global__ void k_matvec_finish_multi(const double* __restrict__ part, int ncb, int K, int n, DIn b, DOut y,
+                                      double* __restrict__ nrm) {
+  __shared__ double s1[8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  double yy = 0.0;
+  if (i < n) {
+    double s = 0.0;
+    for (int k = 0; k < ncb; ++k) s += part[((size_t)k * K + c) * n + i];
+    const double v = b.p[c] ? b.p[c][i] - s : s;
+    y.p[c][i] = v;
+    yy = v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) yy += __shfl_xor_sync(0xffffffffu, yy, o);
+  if ((threadIdx.x & 31) == 0) s1[threadIdx.x >> 5] = yy;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a1 += s1[w];
+    nrm[(size_t)c * gridDim.x + blockIdx.x] = a1;
+  }
+}
+
+// y[c][i] = r[c][perm[i]] for the columns in `mask`, 0 for the others (no correction)
+__global__ void k_permute_to_float_multi(const double* r, const int* perm, float* y, int n, unsigned mask) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (i < n) y[(size_t)c * n + i] = ((mask >> c) & 1u) ? (float)r[(size_t)c * n + perm[i]] : 0.f;
+}
+
+template <int K>
+__device__ __forceinline__ void diag_apply_multi(const float* __restrict__ Dinv, const float* y, int n, int jb,
+                                                 float (*yin)[kNb], float* part, float (*yd)[kNb]) {
+  for (int e = threadIdx.x; e < K * jb; e += blockDim.x) yin[e / jb][e % jb] = y[(size_t)(e / jb) * n + e % jb];
+  __syncthreads();
+  constexpr int kQ = kSolveThreads / kNb;
+  const int m = threadIdx.x % kNb, q = threadIdx.x / kNb;
+  float s[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) s[c] = 0.f;
+  if (m < jb) {
+    for (int k = q * (kNb / kQ); k < (q + 1) * (kNb / kQ); ++k)
+      if (k < jb) {
+        const float d = __ldg(Dinv + (size_t)k * kNb + m);
+#pragma unroll
+        for (int c = 0; c < K; ++c) s[c] = fmaf(d, yin[c][k], s[c]);
+      }
+  }
+#pragma unroll
+  for (int c = 0; c < K; ++c) part[(c * kQ + q) * kNb + m] = s[c];
+  __syncthreads();
+  for (int e = threadIdx.x; e < K * jb; e += blockDim.x) {
+    const int c = e / jb, tt = e % jb;
+    float v = 0.f;
+#pragma unroll
+    for (int qq = 0; qq < kQ; ++qq) v += part[(c * kQ + qq) * kNb + tt];
+    yd[c][tt] = v;
+  }
+  __syncthreads();
+}
+
+template <int K>
+__device__ __forceinline__ void update_rows_multi(const float* __restrict__ LU, long long ld, int n, int k0, int jb,
+                                                  int i0, int i1, float (*yd)[kNb], float* y, float* part) {
+  const int nr = i1 - i0;
+  if (nr <= 0) return;
+  if (jb != kNb) {
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      float s[K];
+#pragma unroll
+      for (int c = 0; c < K; ++c) s[c] = 0.f;
+      for (int m = 0; m < jb; ++m) {
+        const float a = LU[(size_t)(k0 + m) * ld + i];
+#pragma unroll
+        for (int c = 0; c < K; ++c) s[c] = fmaf(a, yd[c][m], s[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < K; ++c) y[(size_t)c * n + i] -= s[c];
+    }
+    return;
+  }
+  constexpr int kChunks = 4, kW = kNb / kChunks, kRows = kSolveThreads / kChunks;
+  for (int r0 = 0; r0 < nr; r0 += kRows) {
+    const int rows = min(kRows, nr - r0);
+    const int q = threadIdx.x / kRows, r = threadIdx.x % kRows;
+    if (r < rows) {
+      const float* col = LU + (size_t)(k0 + q * kW) * ld + i0 + r0 + r;
+      float s[K];
+#pragma unroll
+      for (int c = 0; c < K; ++c) s[c] = 0.f;
+#pragma unroll 8
+      for (int m = 0; m < kW; ++m) {
+        const float a = __ldg(col + (size_t)m * ld);
+#pragma unroll
+        for (int c = 0; c < K; ++c) s[c] = fmaf(a, yd[c][q * kW + m], s[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < K; ++c) part[(c * kChunks + q) * kRows + r] = s[c];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < K * rows; e += blockDim.x) {
+      const int c = e / rows, rr = e % rows;
+      float v = 0.f;
+#pragma unroll
+      for (int qq = 0; qq < kChunks; ++qq) v += part[(c * kChunks + qq) * kRows + rr];
+      y[(size_t)c * n + i0 + r0 + rr] -= v;
+    }
+    __syncthreads();
+  }
+}
+
+// L w = y and U x = w for K right-hand sides (y, out: K vectors of n, column c at c n)
+template <int K>
+__global__ void __launch_bounds__(kSolveThreads) k_trsv_lower_multi(TrsvArgs a) {
+  __shared__ float yd[K][kNb], yin[K][kNb];
+  __shared__ float part[K * kSolveThreads];
+  const int G = gridDim.x;
+  for (int k0 = 0; k0 < a.n; k0 += kNb) {
+    const int jb = min(kNb, a.n - k0);
+    diag_apply_multi<K>(a.dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb, a.y + k0, a.n, jb, yin, part, yd);
+    const int rest = a.n - k0 - jb;
+    const int chunk = (rest + G - 1) / G;
+    const int i0 = k0 + jb + blockIdx.x * chunk, i1 = min(a.n, i0 + chunk);
+    update_rows_multi<K>(a.LU, a.ld, a.n, k0, jb, i0, i1, yd, a.y, part);
+    if (blockIdx.x == 0)
+      for (int e = threadIdx.x; e < K * jb; e += blockDim.x) a.out[(size_t)(e / jb) * a.n + k0 + e % jb] = yd[e / jb][e % jb];
+    if (!grid_sync(a.bar)) return;
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kSolveThreads) k_trsv_upper_multi(TrsvArgs a) {
+  __shared__ float yd[K][kNb], yin[K][kNb];
+  __shared__ float part[K * kSolveThreads];
+  const int G = gridDim.x;
+  const int nblk = (a.n + kNb - 1) / kNb;
+  for (int kb = nblk - 1; kb >= 0; --kb) {
+    const int k0 = kb * kNb, jb = min(kNb, a.n - k0);
+    diag_apply_multi<K>(a.dinv + (size_t)kb * 2 * kNb * kNb + (size_t)kNb * kNb, a.y + k0, a.n, jb, yin, part, yd);
+    const int chunk = (k0 + G - 1) / G;
+    const int i0 = blockIdx.x * chunk, i1 = min(k0, i0 + chunk);
+    update_rows_multi<K>(a.LU, a.ld, a.n, k0, jb, i0, i1, yd, a.y, part);
+    if (blockIdx.x == 0)
+      for (int e = threadIdx.x; e < K * jb; e += blockDim.x) a.out[(size_t)(e / jb) * a.n + k0 + e % jb] = yd[e / jb][e % jb];
+    if (!grid_sync(a.bar)) return;
+  }
+}
+
+// the products b_c - A x_c (b given) or A x_c for K vectors in one pass over A, with the
+// squared norms of the results on the host (synchronises) when norm2 is given
+static int32_t matvec_multi(o3g_bem_t* h, int K, const DIn& x, const DIn& b, const DOut& y, float* xh, float* xl,
+                            double* part, double* nrm, std::vector<double>* norm2, cudaStream_t st) {
+  const int n = h->n;
+  const int nrb = (n + 255) / 256;
+  const int ncb = (n + kMvChunkM - 1) / kMvChunkM;
+  int nc = 0;
+  if (x.p[0]) {
+    k_split_f64_multi<<<dim3(nrb, K), 256, 0, st>>>(x, xh, xl, n);
+    const dim3 g(nrb, ncb);
+    switch (K) {
+      case 1: k_matvec_ds_multi<1><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      case 2: k_matvec_ds_multi<2><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      case 3: k_matvec_ds_multi<3><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      case 4: k_matvec_ds_multi<4><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      case 5: k_matvec_ds_multi<5><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      case 6: k_matvec_ds_multi<6><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      case 7: k_matvec_ds_multi<7><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+      default: k_matvec_ds_multi<8><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
+    }
+    note_launch(2);
+    nc = ncb;
+  }
+  k_matvec_finish_multi<<<dim3(nrb, K), 256, 0, st>>>(part, nc, K, n, b, y, nrm);
+  note_launch();
+  O3G_CUDA_TRY(cudaGetLastError());
+  if (norm2) {
+    std::vector<double> hn((size_t)K * nrb);
+    O3G_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, hn.size() * 8, cudaMemcpyDeviceToHost, st));
+    O3G_CUDA_TRY(cudaStreamSynchronize(st));
+    norm2->assign(K, 0.0);
+    for (int c = 0; c < K; ++c)
+      for (int k = 0; k < nrb; ++k) (*norm2)[c] += hn[(size_t)c * nrb + k];
+  }
+  return O3G_OK;
+}
+
+template <int K>
+static int32_t launch_trsv_multi(const TrsvArgs& lower, const TrsvArgs& upper, int G, cudaStream_t st) {
+  TrsvArgs a = lower, b = upper;
+  void* aa[] = {&a};
+  void* bb[] = {&b};
+  int* flags = reinterpret_cast<int*>(a.bar.err);
+  O3G_CUDA_TRY(zero_barrier(flags, st));
+  O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_lower_multi<K>, dim3(G), dim3(kSolveThreads), aa, 0,
+                                           st));
+  O3G_CUDA_TRY(zero_barrier(flags, st));
+  O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_trsv_upper_multi<K>, dim3(G), dim3(kSolveThreads), bb, 0,
+                                           st));
+  note_launch(2);
+  return O3G_OK;
+}
+
+static int32_t trsv_multi(int K, const TrsvArgs& lower, const TrsvArgs& upper, int G, cudaStream_t st) {
+  switch (K) {
+    case 1: return launch_trsv_multi<1>(lower, upper, G, st);
+    case 2: return launch_trsv_multi<2>(lower, upper, G, st);
+    case 3: return launch_trsv_multi<3>(lower, upper, G, st);
+    case 4: return launch_trsv_multi<4>(lower, upper, G, st);
+    case 5: return launch_trsv_multi<5>(lower, upper, G, st);
+    case 6: return launch_trsv_multi<6>(lower, upper, G, st);
+    case 7: return launch_trsv_multi<7>(lower, upper, G, st);
+    default: return launch_trsv_multi<8>(lower, upper, G, st);
+  }
+}
+
+// blocks per SM of the K-vector solve kernels (their shared memory grows with K)
+static int32_t trsv_multi_grid(int K, int num_sms, int* G) {
+  int per_sm = 0;
+  cudaError_t e;
+  switch (K) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<1>, kSolveThreads, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<2>, kSolveThreads, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<3>, kSolveThreads, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<4>, kSolveThreads, 0); break;
+    case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<5>, kSolveThreads, 0); break;
+    case 6: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<6>, kSolveThreads, 0); break;
+    case 7: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<7>, kSolveThreads, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_lower_multi<8>, kSolveThreads, 0); break;
+  }
+  O3G_CUDA_TRY(e);
+  if (per_sm < 1) {
+    set_error("o3g_bem_solve_many: the solve kernel does not fit on an SM");
+    return O3G_ERR_CUDA;
+  }
+  *G = num_sms;   // one block per SM, as the single-vector solve
+  return O3G_OK;
+}
+
+}  // namespace o3g
+
+static int32_t many_args(o3g_bem_t* h, int32_t nrhs, const float* B, int32_t mem, double tol, int32_t max_iter,
+                         const char* who) {
+  O3G_TRY(bem_check(h));
+  if (nrhs < 0 || (nrhs > 0 && !B) || (mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || max_iter < 1 ||
+      !(tol >= 0.0)) {
+    char msg[160];
+    std::snprintf(msg, sizeof(msg), "%s: bad arguments (nrhs >= 0, B given, mem HOST or DEVICE, max_iter >= 1, tol >= 0)",
+                  who);
+    set_error(msg);
+    return O3G_ERR_INVALID_ARG;
+  }
+  return O3G_OK;
+}
+
+extern "C" int32_t o3g_bem_solve_many(o3g_bem_t* h, int32_t nrhs, const float* B, float* X, double* X64, int32_t mem,
+                                      double tol, int32_t max_iter, int32_t* iters, double* relres, void* stream) {
+  O3G_TRY(many_args(h, nrhs, B, mem, tol, max_iter, "o3g_bem_solve_many"));
+  if (!h->factored) {
+    set_error("o3g_bem_solve_many: factor the matrix first (o3g_bem_factor)");
+    return O3G_ERR_STATE;
+  }
+  if (nrhs == 0) return O3G_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = h->n;
+  const long long ld = h->ld;
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+  const int KM = std::min(nrhs, kMaxRhs);
+  const int ncb = (n + kMvChunkM - 1) / kMvChunkM;
+  const int nrb = (n + 255) / 256;
+  const size_t kn = (size_t)KM * n;
+  const size_t need = 3 * align_up(kn * 8) + 5 * align_up(kn * 4) + align_up((size_t)ncb * kn * 8) +
+                      align_up((size_t)KM * nrb * 8);
+  O3G_TRY(bem_scratch(h, need));
+  Carve cv(h->scratch);
+  double* bd = cv.take<double>(kn);
+  double* xd = cv.take<double>(kn);
+  double* rd = cv.take<double>(kn);
+  float* bf = cv.take<float>(kn);
+  float* y = cv.take<float>(kn);
+  float* w = cv.take<float>(kn);
+  float* xh = cv.take<float>(kn);
+  float* xl = cv.take<float>(kn);
+  double* part = cv.take<double>((size_t)ncb * kn);
+  double* nrm = cv.take<double>((size_t)KM * nrb);
+  const cudaMemcpyKind h2d = mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const cudaMemcpyKind d2h = mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  bool timed_out = false, all_converged = true;
+  KernelTimer& tm = thread_timer();
+  tm.begin(st);
+  for (int g0 = 0; g0 < nrhs; g0 += kMaxRhs) {
+    const int K = std::min(kMaxRhs, nrhs - g0);
+    const size_t knn = (size_t)K * n;
+    O3G_CUDA_TRY(cudaMemcpyAsync(bf, B + (size_t)g0 * n, knn * 4, h2d, st));
+    k_f2d<<<(unsigned)((knn + 255) / 256), 256, 0, st>>>(bf, bd, (int)knn);
+    note_launch();
+    O3G_CUDA_TRY(cudaMemsetAsync(xd, 0, knn * 8, st));
+    O3G_CUDA_TRY(cudaMemsetAsync(h->flags, 0, 4 * sizeof(int), st));
+    DIn xin{}, bin{};
+    DOut rout{};
+    for (int c = 0; c < K; ++c) {
+      xin.p[c] = xd + (size_t)c * n;
+      bin.p[c] = bd + (size_t)c * n;
+      rout.p[c] = rd + (size_t)c * n;
+    }
+    DIn none{};
+    int G = 0;
+    O3G_TRY(trsv_multi_grid(K, df.num_sms, &G));
+    TrsvArgs lo, up;
+    lo.LU = h->LU; lo.dinv = h->dinv; lo.ld = ld; lo.n = n; lo.y = y; lo.out = w;
+    lo.bar = make_barrier(h->flags);
+    up = lo;
+    up.y = w; up.out = y;
+    std::vector<double> rr, bnorm(K, 0.0), rel(K, 1.0);
+    unsigned active = (1u << K) - 1u;
+    std::vector<int> it_of(K, max_iter);
+    for (int it = 0; it <= max_iter; ++it) {
+      O3G_TRY(matvec_multi(h, K, it > 0 ? xin : none, bin, rout, xh, xl, part, nrm, &rr, st));
+      for (int c = 0; c < K; ++c) {
+        if (it == 0) bnorm[c] = std::sqrt(rr[c]);
+        if (!((active >> c) & 1u)) continue;
+        rel[c] = bnorm[c] > 0.0 ? std::sqrt(rr[c]) / bnorm[c] : std::sqrt(rr[c]);
+        if (rel[c] <= tol || it == max_iter) {
+          active &= ~(1u << c);
+          it_of[c] = it;
+        }
+      }
+      if (!active) break;
+      k_permute_to_float_multi<<<dim3(nrb, K), 256, 0, st>>>(rd, h->perm, y, n, active);
+      note_launch();
+      O3G_TRY(trsv_multi(K, lo, up, G, st));
+      k_axpy_f2d<<<(unsigned)((knn + 255) / 256), 256, 0, st>>>(xd, y, (int)knn);
+      note_launch();
+    }
+    int fl = 0;
+    O3G_CUDA_TRY(cudaMemcpyAsync(&fl, h->flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    k_d2f<<<(unsigned)((knn + 255) / 256), 256, 0, st>>>(xd, bf, (int)knn);
+    note_launch();
+    if (X) O3G_CUDA_TRY(cudaMemcpyAsync(X + (size_t)g0 * n, bf, knn * 4, d2h, st));
+    if (X64) O3G_CUDA_TRY(cudaMemcpyAsync(X64 + (size_t)g0 * n, xd, knn * 8, d2h, st));
+    O3G_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int c = 0; c < K; ++c) {
+      if (iters) iters[g0 + c] = it_of[c];
+      if (relres) relres[g0 + c] = rel[c];
+      if (!(rel[c] <= tol)) all_converged = false;
+    }
+    if (fl) {
+      timed_out = true;
+      break;
+    }
+  }
+  tm.end(st);
+  if (timed_out) {
+    set_error("o3g_bem_solve_many: a grid barrier timed out");
+    return O3G_ERR_TIMEOUT;
+  }
+  if (!all_converged) {
+    set_error("o3g_bem_solve_many: some right-hand sides did not reach the tolerance (see relres)");
+    return O3G_ERR_NOT_CONVERGED;
+  }
+  return O3G_OK;
+}
+
+// GMRES(restart) for several right-hand sides in lockstep: each keeps its own Krylov basis,
+// Hessenberg matrix and restarts (the single-vector algorithm of o3g_bem_solve_gmres), and
+// every iteration applies A to all of their current vectors in one pass over the matrix.
+extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const float* B, float* X, double* X64,
+                                            int32_t mem, double tol, int32_t max_iter, int32_t restart,
+                                            int32_t* iters, double* relres, void* stream) {
+  O3G_TRY(many_args(h, nrhs, B, mem, tol, max_iter, "o3g_bem_solve_gmres_many"));
+  if (restart < 1 || restart > 500) {
+    set_error("o3g_bem_solve_gmres_many: restart must be 1..500");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (nrhs == 0) return O3G_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = h->n;
+  const int m = std::min(restart, max_iter);
+  const int KM = std::min(nrhs, kMaxRhs);
+  const int ncb = (n + kMvChunkM - 1) / kMvChunkM;
+  const int nrb = (n + 255) / 256;
+  const size_t kn = (size_t)KM * n;
+  const size_t need = align_up(kn * (m + 1) * 8) + 2 * align_up(kn * 8) + 3 * align_up(kn * 4) +
+                      align_up((size_t)ncb * kn * 8) + align_up((size_t)KM * nrb * 8) +
+                      align_up((size_t)KM * 2 * (m + 1) * 8);
+  O3G_TRY(bem_scratch(h, need));
+  Carve cv(h->scratch);
+  double* V = cv.take<double>(kn * (m + 1));     // basis of column c at V + c (m+1) n
+  double* bd = cv.take<double>(kn);
+  double* xd = cv.take<double>(kn);
+  float* bf = cv.take<float>(kn);
+  float* xh = cv.take<float>(kn);
+  float* xl = cv.take<float>(kn);
+  double* part = cv.take<double>((size_t)ncb * kn);
+  double* nrm = cv.take<double>((size_t)KM * nrb);
+  double* hd = cv.take<double>((size_t)KM * 2 * (m + 1));
+  if (cublasSetStream(h->cublas, st) != CUBLAS_STATUS_SUCCESS) {
+    set_error("o3g_bem_solve_gmres_many: cublasSetStream failed");
+    return O3G_ERR_CUDA;
+  }
+  cublasSetPointerMode(h->cublas, CUBLAS_POINTER_MODE_HOST);
+  auto cublas_ok = [&](cublasStatus_t cs, const char* what) -> int32_t {
+    if (cs == CUBLAS_STATUS_SUCCESS) return O3G_OK;
+    set_error(what);
+    return O3G_ERR_CUDA;
+  };
+  const cudaMemcpyKind h2d = mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const cudaMemcpyKind d2h = mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  const double one = 1.0, zero = 0.0, minus1 = -1.0;
+  bool all_converged = true;
+  KernelTimer& tm = thread_timer();
+  tm.begin(st);
+  struct Rhs {
+    std::vector<double> H, cs, sn, g, y;
+    double bnorm = 0.0, rel = 1.0;
+    int k = 0, total = 0;
+    bool done = false, fresh = true;   // fresh: a cycle starts (residual, basis reset) next
+  };
+  for (int g0 = 0; g0 < nrhs; g0 += kMaxRhs) {
+    const int K = std::min(kMaxRhs, nrhs - g0);
+    const size_t knn = (size_t)K * n;
+    O3G_CUDA_TRY(cudaMemcpyAsync(bf, B + (size_t)g0 * n, knn * 4, h2d, st));
+    k_f2d<<<(unsigned)((knn + 255) / 256), 256, 0, st>>>(bf, bd, (int)knn);
+    note_launch();
+    O3G_CUDA_TRY(cudaMemsetAsync(xd, 0, knn * 8, st));
+    std::vector<Rhs> R(K);
+    auto Vc = [&](int c, int k) { return V + ((size_t)c * (m + 1) + k) * n; };
+    for (int c = 0; c < K; ++c) {
+      R[c].H.assign((size_t)(m + 1) * m, 0.0);
+      R[c].cs.assign(m, 0.0);
+      R[c].sn.assign(m, 0.0);
+      R[c].g.assign(m + 1, 0.0);
+      R[c].y.assign(m, 0.0);
+    }
+    // ||b_c||
+    {
+      DIn none{}, bin{};
+      DOut vout{};
+      for (int c = 0; c < K; ++c) {
+        bin.p[c] = bd + (size_t)c * n;
+        vout.p[c] = Vc(c, 0);
+      }
+      std::vector<double> bb;
+      O3G_TRY(matvec_multi(h, K, none, bin, vout, xh, xl, part, nrm, &bb, st));
+      for (int c = 0; c < K; ++c) {
+        R[c].bnorm = std::sqrt(bb[c]);
+        if (R[c].bnorm == 0.0) { R[c].done = true; R[c].rel = 0.0; }
+      }
+    }
+    for (;;) {
+      // columns starting a cycle: r = b - A x into their V_0, in one pass (x = 0 on the
+      // first cycle: r = b, no product)
+      std::vector<int> fr;
+      for (int c = 0; c < K; ++c)
+        if (!R[c].done && R[c].fresh) fr.push_back(c);
+      if (!fr.empty()) {
+        DIn xin{}, bin{};
+        DOut vout{};
+        bool any_x = false;
+        for (int q = 0; q < (int)fr.size(); ++q) {
+          const int c = fr[q];
+          xin.p[q] = xd + (size_t)c * n;
+          bin.p[q] = bd + (size_t)c * n;
+          vout.p[q] = Vc(c, 0);
+          any_x = any_x || R[c].total > 0;
+        }
+        if (!any_x) xin = DIn{};
+        std::vector<double> rr;
+        O3G_TRY(matvec_multi(h, (int)fr.size(), xin, bin, vout, xh, xl, part, nrm, &rr, st));
+        for (int q = 0; q < (int)fr.size(); ++q) {
+          Rhs& s = R[fr[q]];
+          s.rel = std::sqrt(rr[q]) / s.bnorm;
+          if (s.rel <= tol || s.total >= max_iter) {
+            s.done = true;
+            continue;
+          }
+          const double beta = std::sqrt(rr[q]), ib = 1.0 / beta;
+          O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &ib, Vc(fr[q], 0), 1), "o3g_bem_solve_gmres_many: cublasDscal"));
+          std::fill(s.g.begin(), s.g.end(), 0.0);
+          s.g[0] = beta;
+          s.k = 0;
+          s.fresh = false;
+        }
+      }
+      std::vector<int> act;
+      for (int c = 0; c < K; ++c)
+        if (!R[c].done) act.push_back(c);
+      if (act.empty()) break;
+      // w_c = A v_{c,k} for every active column, one pass
+      {
+        DIn xin{}, none{};
+        DOut wout{};
+        for (int q = 0; q < (int)act.size(); ++q) {
+          xin.p[q] = Vc(act[q], R[act[q]].k);
+          wout.p[q] = Vc(act[q], R[act[q]].k + 1);
+        }
+        O3G_TRY(matvec_multi(h, (int)act.size(), xin, none, wout, xh, xl, part, nrm, nullptr, st));
+      }
+      for (int c : act) {
+        Rhs& s = R[c];
+        const int k = s.k;
+        double* Vb = Vc(c, 0);
+        double* w = Vc(c, k + 1);
+        double* hc_d = hd + (size_t)c * 2 * (m + 1);
+        for (int pass = 0; pass < 2; ++pass) {
+          double* hp = hc_d + (size_t)pass * (m + 1);
+          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_T, n, k + 1, &one, Vb, n, w, 1, &zero, hp, 1),
+                            "o3g_bem_solve_gmres_many: cublasDgemv"));
+          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, k + 1, &minus1, Vb, n, hp, 1, &one, w, 1),
+                            "o3g_bem_solve_gmres_many: cublasDgemv"));
+        }
+        double wn = 0.0;
+        O3G_TRY(cublas_ok(cublasDnrm2(h->cublas, n, w, 1, &wn), "o3g_bem_solve_gmres_many: cublasDnrm2"));
+        std::vector<double> hc(2 * (size_t)(m + 1));
+        O3G_CUDA_TRY(cudaMemcpyAsync(hc.data(), hc_d, hc.size() * 8, cudaMemcpyDeviceToHost, st));
+        O3G_CUDA_TRY(cudaStreamSynchronize(st));
+        auto Hat = [&](int i, int kk) -> double& { return s.H[(size_t)kk * (m + 1) + i]; };
+        for (int i = 0; i <= k; ++i) Hat(i, k) = hc[i] + hc[(size_t)(m + 1) + i];
+        Hat(k + 1, k) = wn;
+        if (wn > 0.0) {
+          const double iw = 1.0 / wn;
+          O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &iw, w, 1), "o3g_bem_solve_gmres_many: cublasDscal"));
+        }
+        for (int i = 0; i < k; ++i) {
+          const double a = Hat(i, k), cc = Hat(i + 1, k);
+          Hat(i, k) = s.cs[i] * a + s.sn[i] * cc;
+          Hat(i + 1, k) = -s.sn[i] * a + s.cs[i] * cc;
+        }
+        const double dd = std::hypot(Hat(k, k), Hat(k + 1, k));
+        s.cs[k] = dd > 0.0 ? Hat(k, k) / dd : 1.0;
+        s.sn[k] = dd > 0.0 ? Hat(k + 1, k) / dd : 0.0;
+        Hat(k, k) = dd;
+        Hat(k + 1, k) = 0.0;
+        s.g[k + 1] = -s.sn[k] * s.g[k];
+        s.g[k] = s.cs[k] * s.g[k];
+        s.k = k + 1;
+        ++s.total;
+        if (s.k == m || s.total >= max_iter || std::fabs(s.g[s.k]) <= 0.5 * tol * s.bnorm || wn == 0.0) {
+          // end of the cycle: x += V y with H(0:k, 0:k) y = g(0:k)
+          const int kk = s.k;
+          for (int i = kk - 1; i >= 0; --i) {
+            double sacc = s.g[i];
+            for (int j = i + 1; j < kk; ++j) sacc -= Hat(i, j) * s.y[j];
+            s.y[i] = Hat(i, i) != 0.0 ? sacc / Hat(i, i) : 0.0;
+          }
+          O3G_CUDA_TRY(cudaMemcpyAsync(hc_d, s.y.data(), (size_t)kk * 8, cudaMemcpyHostToDevice, st));
+          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, kk, &one, Vb, n, hc_d, 1, &one,
+                                        xd + (size_t)c * n, 1),
+                            "o3g_bem_solve_gmres_many: cublasDgemv"));
+          s.fresh = true;
+        }
+      }
+    }
+    k_d2f<<<(unsigned)((knn + 255) / 256), 256, 0, st>>>(xd, bf, (int)knn);
+    note_launch();
+    if (X) O3G_CUDA_TRY(cudaMemcpyAsync(X + (size_t)g0 * n, bf, knn * 4, d2h, st));
+    if (X64) O3G_CUDA_TRY(cudaMemcpyAsync(X64 + (size_t)g0 * n, xd, knn * 8, d2h, st));
+    O3G_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int c = 0; c < K; ++c) {
+      if (iters) iters[g0 + c] = R[c].total;
+      if (relres) relres[g0 + c] = R[c].rel;
+      if (!(R[c].rel <= tol)) all_converged = false;
+    }
+  }
+  tm.end(st);
+  if (!all_converged) {
+    set_error("o3g_bem_solve_gmres_many: some right-hand sides did not reach the tolerance (see relres)");
     return O3G_ERR_NOT_CONVERGED;
   }
   return O3G_OK;

@@ -86,6 +86,12 @@ void note_launch(int n = 1);
 cudaError_t dev_alloc(void** p, size_t bytes);
 cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t st);
 
+// tensor-core update C -= A B (o3g_tcgemm.cu): column-major FP32 operands, TF32 products,
+// FP32 sums; `at` holds tc_gemm_scratch_floats(m, k) floats, `err` is a device error word
+size_t tc_gemm_scratch_floats(int m, int k);
+int32_t tc_gemm_sub(int m, int n, int k, const float* A, long long lda, const float* B, long long ldb, float* C,
+                    long long ldc, float* at, int* err, cudaStream_t st);
+
 // wait test (o3g_debug_wait_test): when on, the bounded device-side waits of the BEM
 // factorisation and solves and of the particle split wait for a condition nothing fulfils,
 // with a short limit, so that they run out and the call returns O3G_ERR_TIMEOUT
@@ -205,9 +211,12 @@ __device__ __forceinline__ float exp_tang(float x) {
 }
 
 // dx dx + dy dy + dz dz with every product and sum rounded, left to right: the reference's
-// expression (Kernels.h:167-170) as an uncontracted float build evaluates it
+// expression (Kernels.h:167-170) as an uncontracted build evaluates it
 __device__ __forceinline__ float dist2_ref(float dx, float dy, float dz) {
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+__device__ __forceinline__ double dist2_ref(double dx, double dy, double dz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
 __device__ __forceinline__ float dev_erf(float x) { return erff(x); }
@@ -234,29 +243,37 @@ __device__ __forceinline__ int gauss_interval(float q) {
 
 // G(q) and D(q) by Horner's rule in t.  The table is coefficient-major (entry e of interval
 // j at e * kGaussPolyN + j), so the lanes of a warp, whatever their intervals, read each
-// entry from one cache line.  Scalar loads: vector loads of a row made the compiler keep
-// all of it live, which cost the pair kernel a fifth of its occupancy.
-__device__ __forceinline__ void gauss_poly(float q, float& G, float& D) {
+// entry from one cache line (or, from a shared-memory copy, from distinct banks).  Scalar
+// loads: vector loads of a row made the compiler keep all of it live, which cost the pair
+// kernel a fifth of its occupancy.  `tab`: a block's shared-memory copy of kGaussPoly
+// (stage_gauss_table), or nullptr for the global table through the read-only cache.
+__device__ __forceinline__ float gtab_ld(const float* tab, int i) { return tab ? tab[i] : __ldg(kGaussPoly + i); }
+__device__ __forceinline__ void gauss_poly(float q, float& G, float& D, const float* tab = nullptr) {
   constexpr int N = kGaussPolyN;
-  const float* c = kGaussPoly + gauss_interval(q);   // entry e of this interval: c[e * N]
-  const float t = fmaf(q, __ldg(c), __ldg(c + N));
-  float g = __ldg(c + 2 * N), d = __ldg(c + 3 * N);
+  const int j = gauss_interval(q);   // entry e of this interval: e * N + j
+  const float t = fmaf(q, gtab_ld(tab, j), gtab_ld(tab, N + j));
+  float g = gtab_ld(tab, 2 * N + j), d = gtab_ld(tab, 3 * N + j);
 #pragma unroll
   for (int k = 1; k <= kGaussPolyDeg; ++k) {
-    g = fmaf(g, t, __ldg(c + (2 + 2 * k) * N));
-    d = fmaf(d, t, __ldg(c + (3 + 2 * k) * N));
+    g = fmaf(g, t, gtab_ld(tab, (2 + 2 * k) * N + j));
+    d = fmaf(d, t, gtab_ld(tab, (3 + 2 * k) * N + j));
   }
   G = g;
   D = d;
 }
-__device__ __forceinline__ float gauss_poly_g(float q) {
+__device__ __forceinline__ float gauss_poly_g(float q, const float* tab = nullptr) {
   constexpr int N = kGaussPolyN;
-  const float* c = kGaussPoly + gauss_interval(q);
-  const float t = fmaf(q, __ldg(c), __ldg(c + N));
-  float g = __ldg(c + 2 * N);
+  const int j = gauss_interval(q);
+  const float t = fmaf(q, gtab_ld(tab, j), gtab_ld(tab, N + j));
+  float g = gtab_ld(tab, 2 * N + j);
 #pragma unroll
-  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, __ldg(c + (2 + 2 * k) * N));
+  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, gtab_ld(tab, (2 + 2 * k) * N + j));
   return g;
+}
+// copies the polynomial table into a block's shared array (all threads call; synchronise
+// before the first use)
+__device__ __forceinline__ void stage_gauss_table(float* s) {
+  for (int i = threadIdx.x; i < kGaussPolyStride * kGaussPolyN; i += blockDim.x) s[i] = kGaussPoly[i];
 }
 
 // Gaussian core with gradient factor (the project's own definition, see o3dgpu.h):
@@ -264,7 +281,7 @@ __device__ __forceinline__ float gauss_poly_g(float q) {
 // beyond q = qfar.  FP32 evaluates G from the polynomials above; FP64 (the comparator) from
 // the Taylor series for q < 1 and the closed form with erf/exp beyond.
 template <bool ACC, class T>
-__device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb) {
+__device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb, const float* tab = nullptr) {
   const T c = T(0.79788456080286535588);  // sqrt(2/pi)
   if (distsq > GaussP<T>::qfar * sig2) {   // q > qfar without the division
     const T rs = rsq<ACC>(distsq);
@@ -277,7 +294,7 @@ __device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb) {
     const float rsg = rsq<ACC>(sig2);
     const float rsg2 = rsg * rsg;
     float G, D;
-    gauss_poly(distsq * rsg2, G, D);
+    gauss_poly(distsq * rsg2, G, D, tab);
     const float isig3 = rsg2 * rsg;
     r3 = G * isig3;
     bbb = D * isig3 * rsg2;
@@ -306,7 +323,7 @@ __device__ __forceinline__ void gauss_g(T distsq, T sig2, T& r3, T& bbb) {
   }
 }
 template <bool ACC, class T>
-__device__ __forceinline__ T gauss_v(T distsq, T sig2) {
+__device__ __forceinline__ T gauss_v(T distsq, T sig2, const float* tab = nullptr) {
   const T c = T(0.79788456080286535588);
   if (distsq > GaussP<T>::qfar * sig2) {
     const T rs = rsq<ACC>(distsq);
@@ -315,7 +332,7 @@ __device__ __forceinline__ T gauss_v(T distsq, T sig2) {
   if constexpr (std::is_same<T, float>::value) {
     const float rsg = rsq<ACC>(sig2);
     const float rsg2 = rsg * rsg;
-    return gauss_poly_g(distsq * rsg2) * (rsg2 * rsg);
+    return gauss_poly_g(distsq * rsg2, tab) * (rsg2 * rsg);
   }
   const T q = distsq / sig2;
   if (q < T(1.0)) {
@@ -335,7 +352,7 @@ __device__ __forceinline__ T gauss_v(T distsq, T sig2) {
 
 // r3 and bbb of one pair; dx,dy,dz = target - source; cst as above.
 template <int C, bool ACC, class T>
-__device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
+__device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb, const float* gtab = nullptr) {
   if (C == CORE_RM) {
     // CoreFunc.h:66-71: r2 = d^2 + sr^2 + tr^2, r3 = r2^-1.5, bbb = -3 r3 / r2
     const T r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, cst)));
@@ -355,20 +372,23 @@ __device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
     bbb = fma(T(-5.0) * r3, rs2, T(2.0) * dn5);
   } else if (C == CORE_EXP) {
     // CoreFunc.h:226-236 with the branches of exp_cond / exp_bbb (:119-174).  The core
-    // jumps by reld3/2 (5e-4) where it switches form at reld3 = 0.001, so plain FP32 forms
-    // distsq and the bbb difference in the reference's operation order, each operation
-    // rounded (Kernels.h:167-170), and takes each branch exactly where the reference does.
+    // jumps by reld3/2 (5e-4) where it switches form at reld3 = 0.001, so distsq is formed
+    // in the reference's operation order, each operation rounded (Kernels.h:167-170), and
+    // each branch is taken where the reference's build of the same precision takes it.
+    // Plain FP32 also evaluates the middle branch as the reference does (REF).
     constexpr bool REF = !ACC && std::is_same<T, float>::value;
-    const T distsq = REF ? (T)dist2_ref((float)dx, (float)dy, (float)dz) : fma(dx, dx, fma(dy, dy, dz * dz));
+    const T distsq = dist2_ref(dx, dy, dz);
     const T dist = dev_sqrt(distsq);
     const T corefac = T(1.0) / cst;
     const T d3 = distsq * dist;
     const T reld3 = d3 * corefac;
     const T ood3 = T(1.0) / d3;
-    if (reld3 > T(16.0)) {
+    // the thresholds are the float literals 16.0f and 0.001f of the reference's exp_cond /
+    // exp_bbb (CoreFunc.h:121-132, :164-177), also in its double build
+    if (reld3 > T(16.0f)) {
       r3 = ood3;
       bbb = T(-3.0) * r3 / distsq;
-    } else if (reld3 < T(0.001)) {
+    } else if (reld3 < T(0.001f)) {
       r3 = corefac;
       bbb = T(-1.5) * dist * r3 * r3;
     } else if (REF) {
@@ -394,13 +414,13 @@ __device__ __forceinline__ void core_g(T dx, T dy, T dz, T cst, T& r3, T& bbb) {
     bbb = T(-3.0) * r3 * rs;
   } else {
     const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
-    gauss_g<ACC, T>(distsq, cst, r3, bbb);
+    gauss_g<ACC, T>(distsq, cst, r3, bbb, gtab);
   }
 }
 
 // r3 only (velocity-only kernels): CoreFunc.h:48-52, :246-252, :202-209, :297-304
 template <int C, bool ACC, class T>
-__device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst) {
+__device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst, const float* gtab = nullptr) {
   if (C == CORE_RM) {
     const T r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, cst)));
     const T rs = rsq<ACC>(r2);
@@ -413,13 +433,13 @@ __device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst) {
     return fma(T(2.5), cst, distsq) * (rs2 * rs2 * rs);
   } else if (C == CORE_EXP) {
     constexpr bool REF = !ACC && std::is_same<T, float>::value;   // as in core_g
-    const T distsq = REF ? (T)dist2_ref((float)dx, (float)dy, (float)dz) : fma(dx, dx, fma(dy, dy, dz * dz));
+    const T distsq = dist2_ref(dx, dy, dz);
     const T dist = dev_sqrt(distsq);
     const T ood3 = T(1.0) / (distsq * dist);
     const T corefac = T(1.0) / cst;
     const T reld3 = corefac / ood3;
-    if (reld3 > T(16.0)) return ood3;
-    if (reld3 < T(0.001)) return corefac;
+    if (reld3 > T(16.0f)) return ood3;
+    if (reld3 < T(0.001f)) return corefac;
     if (REF) return (T)__fmul_rn((float)ood3, __fsub_rn(1.0f, exp_tang((float)-reld3)));
     return ood3 * (-dev_expm1(-reld3));
   } else if (C == CORE_V2) {
@@ -428,7 +448,7 @@ __device__ __forceinline__ T core_v(T dx, T dy, T dz, T cst) {
     return rs * dev_sqrt(rs);
   } else {
     const T distsq = fma(dx, dx, fma(dy, dy, dz * dz));
-    return gauss_v<ACC, T>(distsq, cst);
+    return gauss_v<ACC, T>(distsq, cst, gtab);
   }
 }
 

@@ -55,7 +55,8 @@ template <class T, class O> struct PairArgs {
 // bbb * d (x) (s x d) in the reference order, a[12..14] = sum r3 * s (folded into the
 // antisymmetric gradient terms by fold_grads, Kernels.h:184-192).
 template <int C, bool ACC, bool HAVE_TR, class T>
-__device__ __forceinline__ void pair_g(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a) {
+__device__ __forceinline__ void pair_g(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a,
+                                       const float* gtab = nullptr) {
   const T dx = t.x - s.x;
   const T dy = t.y - s.y;
   const T dz = t.z - s.z;
@@ -68,7 +69,7 @@ __device__ __forceinline__ void pair_g(const V4<T>& t, const V4<T>& s, const V4<
     bbb = T(-3.0) * r3 * rs2;
   } else {
     const T cst = HAVE_TR ? (s.w + t.w) : s.w;
-    core_g<C, ACC, T>(dx, dy, dz, cst, r3, bbb);
+    core_g<C, ACC, T>(dx, dy, dz, cst, r3, bbb, gtab);
   }
   T cx = dz * w.y - dy * w.z;
   T cy = dx * w.z - dz * w.x;
@@ -95,7 +96,8 @@ __device__ __forceinline__ void pair_g(const V4<T>& t, const V4<T>& s, const V4<
 
 // velocity only
 template <int C, bool ACC, bool HAVE_TR, class T>
-__device__ __forceinline__ void pair_v(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a) {
+__device__ __forceinline__ void pair_v(const V4<T>& t, const V4<T>& s, const V4<T>& w, T* a,
+                                       const float* gtab = nullptr) {
   const T dx = t.x - s.x;
   const T dy = t.y - s.y;
   const T dz = t.z - s.z;
@@ -105,7 +107,7 @@ __device__ __forceinline__ void pair_v(const V4<T>& t, const V4<T>& s, const V4<
     r3 = rs * rs * rs;
   } else {
     const T cst = HAVE_TR ? (s.w + t.w) : s.w;
-    r3 = core_v<C, ACC, T>(dx, dy, dz, cst);
+    r3 = core_v<C, ACC, T>(dx, dy, dz, cst, gtab);
   }
   a[0] = fma(r3, dz * w.y - dy * w.z, a[0]);
   a[1] = fma(r3, dx * w.z - dz * w.x, a[1]);
@@ -129,7 +131,7 @@ __device__ __forceinline__ void fold_grads(T* a) {
 // Fast2Sum.
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, int NA, int NC, int NH, int NS = kBlock>
 __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, const V4<T>* tp, T (*acc)[NA],
-                                           float (*hi)[NH], float (*lo)[NH]) {
+                                           float (*hi)[NH], float (*lo)[NH], const float* gtab = nullptr) {
   constexpr bool ACC = (MODE == MODE_COMP);
   constexpr int FOLD = ACC ? 16 : NS;
 #pragma unroll 1
@@ -140,8 +142,8 @@ __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, con
       const V4<T> w = sw[j];
 #pragma unroll
       for (int k = 0; k < TPT; ++k) {
-        if (GRADS) pair_g<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k]);
-        else       pair_v<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k]);
+        if (GRADS) pair_g<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k], gtab);
+        else       pair_v<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k], gtab);
       }
     }
     if (ACC) {
@@ -160,6 +162,139 @@ __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, con
         }
 #pragma unroll
         for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
+      }
+    }
+  }
+}
+
+// ---- packed FP32: two sources per instruction (FFMA2 / FADD2 / FMUL2 on float2) -----------
+// The FP32 kernels are bound by instruction issue, not by the FMA pipe: a packed
+// instruction does two sources' operation in one issue slot.  Each lane of a packed
+// operation rounds exactly like the scalar instruction.  A staged tile is re-laid out in
+// shared memory as pairs of sources (2p, 2p+1), component-major so every load yields
+// float2 operands directly:
+//   Q[0][p] = (-x0, -x1, -y0, -y1)    Q[1][p] = (-z0, -z1, c0, c1)     (c: core parameter)
+//   Q[2][p] = (wx0, wx1, wy0, wy1)    Q[3][p] = (wz0, wz1, -wx0, -wx1)
+//   Q[4][p] = (-wy0, -wy1, -wz0, -wz1)
+// (negated copies turn the separations and the cross products' differences into adds
+// and fused multiply-adds).
+__device__ __forceinline__ void stage_pair(const V4<float>& s, const V4<float>& w, float4 (*Q)[kBlock / 2], int j) {
+  const int p = j >> 1, h = j & 1;
+  float* q0 = reinterpret_cast<float*>(&Q[0][p]);
+  float* q1 = reinterpret_cast<float*>(&Q[1][p]);
+  float* q2 = reinterpret_cast<float*>(&Q[2][p]);
+  float* q3 = reinterpret_cast<float*>(&Q[3][p]);
+  float* q4 = reinterpret_cast<float*>(&Q[4][p]);
+  q0[h] = -s.x; q0[2 + h] = -s.y;
+  q1[h] = -s.z; q1[2 + h] = s.w;
+  q2[h] = w.x;  q2[2 + h] = w.y;
+  q3[h] = w.z;  q3[2 + h] = -w.x;
+  q4[h] = -w.y; q4[2 + h] = -w.z;
+}
+
+__device__ __forceinline__ float2 f2lo(const float4& q) { return make_float2(q.x, q.y); }
+__device__ __forceinline__ float2 f2hi(const float4& q) { return make_float2(q.z, q.w); }
+
+// one target (tt = (x,x), (y,y), (z,z), (c,c)) against the source pair of q0..q4; a[] as in
+// pair_g / pair_v, one float2 lane per source.  RM and the singular far-field kernel are
+// packed throughout; the other cores evaluate r3 (and bbb) per lane with the scalar core.
+template <int C, bool ACC, bool HAVE_TR, bool GRADS>
+__device__ __forceinline__ void pair2(const float2* tt, const float4& q0, const float4& q1, const float4& q2,
+                                      const float4& q3, const float4& q4, float2* a, const float* gtab) {
+  const float2 dx = __fadd2_rn(tt[0], f2lo(q0));
+  const float2 dy = __fadd2_rn(tt[1], f2hi(q0));
+  const float2 dz = __fadd2_rn(tt[2], f2lo(q1));
+  float2 r3, bbb = make_float2(0.f, 0.f);
+  if constexpr (C == CORE_SING || C == CORE_RM) {
+    float2 r2;
+    if constexpr (C == CORE_RM) {
+      const float2 cst = HAVE_TR ? __fadd2_rn(f2hi(q1), tt[3]) : f2hi(q1);
+      r2 = __ffma2_rn(dz, dz, cst);
+    } else {
+      r2 = __fmul2_rn(dz, dz);
+    }
+    r2 = __ffma2_rn(dy, dy, r2);
+    r2 = __ffma2_rn(dx, dx, r2);
+    float2 rs = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+    if (ACC) {
+      // y' = y + y/2 (1 - x y^2), as rsq<true>: fma(-y/2, x y^2 - 1, y)
+      const float2 h = __fmul2_rn(r2, rs);
+      const float2 e = __ffma2_rn(h, rs, make_float2(-1.f, -1.f));
+      rs = __ffma2_rn(__fmul2_rn(rs, make_float2(-0.5f, -0.5f)), e, rs);
+    }
+    const float2 rs2 = __fmul2_rn(rs, rs);
+    r3 = __fmul2_rn(rs2, rs);
+    if (GRADS) bbb = __fmul2_rn(__fmul2_rn(r3, make_float2(-3.f, -3.f)), rs2);
+  } else {
+    const float2 cst = HAVE_TR ? __fadd2_rn(f2hi(q1), tt[3]) : f2hi(q1);
+    if (GRADS) {
+      core_g<C, ACC, float>(dx.x, dy.x, dz.x, cst.x, r3.x, bbb.x, gtab);
+      core_g<C, ACC, float>(dx.y, dy.y, dz.y, cst.y, r3.y, bbb.y, gtab);
+    } else {
+      r3.x = core_v<C, ACC, float>(dx.x, dy.x, dz.x, cst.x, gtab);
+      r3.y = core_v<C, ACC, float>(dx.y, dy.y, dz.y, cst.y, gtab);
+    }
+  }
+  const float2 wx = f2lo(q2), wy = f2hi(q2), wz = f2lo(q3);
+  const float2 nwx = f2hi(q3), nwy = f2lo(q4), nwz = f2hi(q4);
+  float2 cx = __ffma2_rn(dz, wy, __fmul2_rn(dy, nwz));   // dz wy - dy wz
+  float2 cy = __ffma2_rn(dx, wz, __fmul2_rn(dz, nwx));   // dx wz - dz wx
+  float2 cz = __ffma2_rn(dy, wx, __fmul2_rn(dx, nwy));   // dy wx - dx wy
+  a[0] = __ffma2_rn(r3, cx, a[0]);
+  a[1] = __ffma2_rn(r3, cy, a[1]);
+  a[2] = __ffma2_rn(r3, cz, a[2]);
+  if (GRADS) {
+    cx = __fmul2_rn(cx, bbb);
+    cy = __fmul2_rn(cy, bbb);
+    cz = __fmul2_rn(cz, bbb);
+    a[3] = __ffma2_rn(dx, cx, a[3]);
+    a[4] = __ffma2_rn(dx, cy, a[4]);
+    a[5] = __ffma2_rn(dx, cz, a[5]);
+    a[6] = __ffma2_rn(dy, cx, a[6]);
+    a[7] = __ffma2_rn(dy, cy, a[7]);
+    a[8] = __ffma2_rn(dy, cz, a[8]);
+    a[9] = __ffma2_rn(dz, cx, a[9]);
+    a[10] = __ffma2_rn(dz, cy, a[10]);
+    a[11] = __ffma2_rn(dz, cz, a[11]);
+    a[12] = __ffma2_rn(r3, wx, a[12]);
+    a[13] = __ffma2_rn(r3, wy, a[13]);
+    a[14] = __ffma2_rn(r3, wz, a[14]);
+  }
+}
+
+// Sweep NP staged source pairs from pair p0 for TPT targets; in the compensated mode the
+// two lanes' partials of every 8 pairs (16 sources) are added and folded into (hi, lo)
+// with Fast2Sum, as sweep_tile does.
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, int NA, int NC, int NH, int NP>
+__device__ __forceinline__ void sweep_pairs(const float4 (*Q)[kBlock / 2], int p0, const float2 (*tt)[4],
+                                            float2 (*acc)[NA], float (*hi)[NH], float (*lo)[NH], const float* gtab) {
+  constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr int FOLD = ACC ? 8 : NP;
+#pragma unroll 1
+  for (int j0 = 0; j0 < NP; j0 += FOLD) {
+#pragma unroll 2
+    for (int j = j0; j < j0 + FOLD; ++j) {
+      const int p = p0 + j;
+      const float4 q0 = Q[0][p], q1 = Q[1][p], q2 = Q[2][p], q3 = Q[3][p], q4 = Q[4][p];
+#pragma unroll
+      for (int k = 0; k < TPT; ++k) pair2<C, ACC, HAVE_TR, GRADS>(tt[k], q0, q1, q2, q3, q4, acc[k], gtab);
+    }
+    if (ACC) {
+#pragma unroll
+      for (int k = 0; k < TPT; ++k) {
+        float a1[NA];
+#pragma unroll
+        for (int c = 0; c < NA; ++c) a1[c] = acc[k][c].x + acc[k][c].y;
+        if (GRADS) fold_grads(a1);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const float s = hi[k][c] + a1[c];
+          const float e = a1[c] - (s - hi[k][c]);
+          hi[k][c] = s;
+          lo[k][c] += e;
+        }
+#pragma unroll
+        for (int c = 0; c < NA; ++c) acc[k][c] = make_float2(0.f, 0.f);
       }
     }
   }
@@ -315,6 +450,112 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
   }
 }
 
+// k_pair for FP32 (PLAIN and COMPENSATED): the same blocks, tiles, far-field classification,
+// splits and epilogue, with the sweep in packed FP32 over pairs of sources.
+template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT>
+__global__ void __launch_bounds__(kBlock) k_pair_f(const PairArgs<float, float> a) {
+  constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr bool CLASSIFY = (C == CORE_GAUSS || C == CORE_EXP);
+  constexpr int NA = GRADS ? 15 : 3;
+  constexpr int NC = GRADS ? 12 : 3;
+  constexpr int NH = ACC ? NC : 1;
+  __shared__ float4 Q[5][kBlock / 2];
+  // the Gaussian core's polynomial table, read from shared memory by the near-field pairs
+  __shared__ float gsh[C == CORE_GAUSS ? kGaussPolyStride * kGaussPolyN : 1];
+  const float* gtab = nullptr;
+  if constexpr (C == CORE_GAUSS) {
+    stage_gauss_table(gsh);   // visible after the first tile's __syncthreads
+    gtab = gsh;
+  }
+
+  const int tid = threadIdx.x;
+  const int split = blockIdx.y;
+  const int tbase = blockIdx.x * (kBlock * TPT) + (tid >> 5) * (32 * TPT) + (tid & 31);
+
+  V4<float> tp[TPT];
+  bool real[TPT];
+  float2 tt[TPT][4];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    tp[k] = a.tpos[tbase + 32 * k];
+    real[k] = tbase + 32 * k < a.nt;
+    tt[k][0] = make_float2(tp[k].x, tp[k].x);
+    tt[k][1] = make_float2(tp[k].y, tp[k].y);
+    tt[k][2] = make_float2(tp[k].z, tp[k].z);
+    tt[k][3] = make_float2(tp[k].w, tp[k].w);
+  }
+
+  float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
+  bool live = true;
+  if (CLASSIFY) live = warp_box<TPT, float>(tp, real, blo, bhi, bw);
+
+  float2 acc[TPT][NA];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k)
+#pragma unroll
+    for (int c = 0; c < NA; ++c) acc[k][c] = make_float2(0.f, 0.f);
+  float hi[TPT][NH], lo[TPT][NH];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k)
+#pragma unroll
+    for (int c = 0; c < NH; ++c) { hi[k][c] = 0.f; lo[k][c] = 0.f; }
+
+  const int t_begin = split * a.tiles_per_split;
+  const int t_end = min(a.ntiles, t_begin + a.tiles_per_split);
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    __syncthreads();
+    stage_pair(a.spos[(size_t)tile * kBlock + tid], a.sstr[(size_t)tile * kBlock + tid], Q, tid);
+    __syncthreads();
+    if constexpr (CLASSIFY) {
+      if (!live) continue;
+#pragma unroll 1
+      for (int hf = 0; hf < kBlock / kHalf; ++hf) {
+        const int u = tile * (kBlock / kHalf) + hf;
+        if (half_is_far<C, HAVE_TR>(a.tile_lo[u], a.tile_hi[u], blo, bhi, bw))
+          sweep_pairs<CORE_SING, MODE, GRADS, HAVE_TR, TPT, NA, NC, NH, kHalf / 2>(Q, hf * (kHalf / 2), tt, acc,
+                                                                                  hi, lo, gtab);
+        else
+          sweep_pairs<C, MODE, GRADS, HAVE_TR, TPT, NA, NC, NH, kHalf / 2>(Q, hf * (kHalf / 2), tt, acc, hi, lo,
+                                                                          gtab);
+      }
+    } else {
+      sweep_pairs<C, MODE, GRADS, HAVE_TR, TPT, NA, NC, NH, kBlock / 2>(Q, 0, tt, acc, hi, lo, gtab);
+    }
+  }
+
+  // epilogue: the two lanes of the plain sums are added here, as the last step of the sums
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    const int idx = tbase + 32 * k;
+    float a1[NA];
+#pragma unroll
+    for (int c = 0; c < NA; ++c) a1[c] = acc[k][c].x + acc[k][c].y;
+    if (!ACC && GRADS) fold_grads(a1);
+    if (a.partial) {
+      if (ACC) {
+        float* base = a.partial + (size_t)split * (2 * NC) * a.nt_pad;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          base[(size_t)c * a.nt_pad + idx] = hi[k][c];
+          base[(size_t)(NC + c) * a.nt_pad + idx] = lo[k][c];
+        }
+      } else {
+        float* base = a.partial + (size_t)split * NC * a.nt_pad;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) base[(size_t)c * a.nt_pad + idx] = a1[c];
+      }
+    } else if (idx < a.nt) {
+      const int o = a.tperm ? (int)a.tperm[idx] : idx;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        float* p = a.out.p[c] + o;
+        if (ACC) *p = (float)((double)*p + ((double)hi[k][c] + (double)lo[k][c]));
+        else     *p = *p + a1[c];
+      }
+    }
+  }
+}
+
 // Sum the per-split partials in split order and add into the outputs.
 template <int NC, bool ACC, class T, class O>
 __global__ void k_reduce(const T* __restrict__ partial, int nsplit, int nt, int nt_pad, OutPtrs<O> out,
@@ -432,7 +673,12 @@ struct PairPlan {
 
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
 struct PairKernel {
-  static const void* ptr() { return (const void*)&k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O>; }
+  static const void* ptr() {
+    if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value)
+      return (const void*)&k_pair_f<C, MODE, GRADS, HAVE_TR, TPT>;
+    else
+      return (const void*)&k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O>;
+  }
 };
 
 // Chooses the source split so that the grid covers >= ~6 waves of resident blocks.
@@ -518,7 +764,10 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   dim3 grid(pl.tblocks, pl.nsplit);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
-  k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O><<<grid, kBlock, 0, st>>>(a);
+  if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value)
+    k_pair_f<C, MODE, GRADS, HAVE_TR, TPT><<<grid, kBlock, 0, st>>>(a);
+  else
+    k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O><<<grid, kBlock, 0, st>>>(a);
   note_launch();
   tm.end(st);
   if (pl.nsplit > 1) {

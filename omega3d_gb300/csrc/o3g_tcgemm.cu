@@ -1,0 +1,349 @@
+// o3g_tcgemm.cu -- C -= A B on GB300's 5th-generation tensor cores (tcgen05, TF32 inputs,
+// FP32 accumulation in tensor memory): the trailing updates of the BEM's blocked LU.
+//
+// All matrices are column-major FP32 (the BEM's layout).  A (m x k) has rows contiguous,
+// so it is first copied to a K-major (row-major) scratch with k padded to whole 32-column
+// slabs (zeros); B (k x n) is already K-major.  Then:
+//   * one CTA per 128 x 128 tile of C, 6 warps: warp 0 issues TMA loads, warp 1 owns the
+//     tensor-memory allocation and issues the MMAs, warps 2-5 run the epilogue;
+//   * k is swept in slabs of 32 (128 bytes of every row, the 128-byte swizzle width) through
+//     a ring of kStages shared-memory stages: full/empty mbarrier pairs, TMA with
+//     complete_tx on the full barrier, tcgen05.commit on the empty one;
+//   * each slab is 4 MMAs of 128 x 128 x 8 (kind::tf32) into 128 TMEM columns;
+//   * the epilogue reads the accumulator row by row (TMEM lane = row of the tile) and
+//     subtracts it from C with coalesced loads and stores.
+// Every mbarrier wait is bounded: after kWaitLimit polls it sets the error word, every
+// other wait then gives up at once, the CTA still frees its tensor memory, and the host
+// returns O3G_ERR_TIMEOUT.
+#include "o3g_common.cuh"
+
+#include <cuda.h>
+
+#include <mutex>
+
+namespace o3g {
+namespace {
+
+constexpr int kTM = 128, kTN = 128, kTK = 32, kStages = 4;
+constexpr int kTileBytes = kTM * kTK * 4;                  // 16 KB per operand and stage
+constexpr int kGemmThreads = 192;
+constexpr uint32_t kTmemCols = 128;
+constexpr unsigned long long kWaitLimit = 1ull << 26;
+constexpr size_t kGemmSmem = 1024 + (size_t)kStages * 2 * kTileBytes + 256;
+
+// instruction descriptor of tcgen05.mma kind::tf32: D format F32 (bits 4-5 = 1), A and B
+// TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22,
+// M >> 4 at bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTN >> 3) << 17) |
+                            ((uint32_t)(kTM >> 4) << 24);
+
+struct GemmArgs {
+  float* C;
+  long long ldc;
+  int m, n, nkb;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// false, with the error word set, after kWaitLimit polls; false at once (within 256 polls)
+// when another wait already gave up
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+  for (unsigned long long it = 0; it < kWaitLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255ull) == 255ull && *(volatile int*)err) return false;
+    if (it > 64) __nanosleep(32);
+  }
+  atomicCAS(err, 0, O3G_ERR_TIMEOUT);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128 bytes, 8-row
+// groups 1024 bytes apart (SBO), start address >> 4 at bits 0-13, LBO (unused for this
+// layout) 1, descriptor version 1 at bits 46-47, layout SWIZZLE_128B (2) at bits 61-63
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive TMEM columns of this warp's 32 lanes: thread t gets lane (base lane + t)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_tc_gemm_sub(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+  extern __shared__ unsigned char smem_raw[];
+  // the 128-byte swizzle repeats every 1024 bytes: stage buffers start on 1024-byte boundaries
+  const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023;
+  unsigned char* sA = reinterpret_cast<unsigned char*>(base);
+  unsigned char* sB = sA + (size_t)kStages * kTileBytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)kStages * kTileBytes);   // full, empty, accum
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * kTN;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages), accum = smem_u32(bars + 2 * kStages);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer
+      int issued = 0;
+      for (int kb = 0; kb < g.nkb; ++kb) {
+        const int s = kb % kStages;
+        if (kb >= kStages && !mbar_wait(empty0 + 8 * s, (uint32_t)((kb / kStages) - 1) & 1u, g.err)) break;
+        mbar_expect_tx(full0 + 8 * s, 2 * kTileBytes);
+        tma_load_2d(smem_u32(sA + (size_t)s * kTileBytes), &tmA, kb * kTK, m0, full0 + 8 * s);
+        tma_load_2d(smem_u32(sB + (size_t)s * kTileBytes), &tmB, kb * kTK, n0, full0 + 8 * s);
+        ++issued;
+      }
+      // every issued load has landed before the CTA may leave (a consumer that gave up does
+      // not wait for them): the last phase issued on each stage, bounded (at once normally)
+      for (int kb = issued - 1; kb >= 0 && kb >= issued - kStages; --kb)
+        (void)mbar_wait(full0 + 8 * (kb % kStages), (uint32_t)(kb / kStages) & 1u, g.err);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      int kb = 0;
+      for (; kb < g.nkb; ++kb) {
+        const int s = kb % kStages;
+        if (!mbar_wait(full0 + 8 * s, (uint32_t)(kb / kStages) & 1u, g.err)) break;
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(sA + (size_t)s * kTileBytes), b0 = smem_u32(sB + (size_t)s * kTileBytes);
+#pragma unroll
+        for (int kk = 0; kk < kTK / 8; ++kk)
+          mma_tf32(tmem, sw128_desc(a0 + 32u * kk), sw128_desc(b0 + 32u * kk), (kb | kk) != 0 ? 1u : 0u);
+        mma_commit(empty0 + 8 * s);
+      }
+      // also after a failure: the epilogue's wait then ends once every issued MMA is done
+      mma_commit(accum);
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile
+    const int q = warp & 3;
+    const int row = m0 + 32 * q + lane;
+    int ok = 0;
+    if (lane == 0) ok = mbar_wait(accum, 0u, g.err) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (ok) {
+      tc_fence_after();
+      const bool write = (*(volatile int*)g.err == 0) && row < g.m;
+#pragma unroll 1
+      for (int c0 = 0; c0 < kTN; c0 += 16) {
+        uint32_t v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+        if (write) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = n0 + c0 + j;
+            if (col < g.n) {
+              float* p = g.C + (size_t)col * g.ldc + row;
+              *p = *p - __uint_as_float(v[j]);
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+// At[i kp + kk] = A[kk lda + i] for kk < k, 0 for k <= kk < kp (rows i < m)
+__global__ void k_transpose_pad(const float* __restrict__ A, long long lda, int m, int k, int kp,
+                                float* __restrict__ At) {
+  __shared__ float tile[32][33];
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int kk = k0 + r, i = i0 + threadIdx.x;
+    tile[r][threadIdx.x] = (kk < k && i < m) ? A[(size_t)kk * lda + i] : 0.f;
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int i = i0 + r, kk = k0 + threadIdx.x;
+    if (i < m && kk < kp) At[(size_t)i * kp + kk] = tile[threadIdx.x][r];
+  }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int32_t encode_fn(EncodeTiled* out) {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiled)f;
+    (void)cudaGetLastError();
+  });
+  if (!fn) {
+    set_error("tensor-core GEMM: cuTensorMapEncodeTiled is not available");
+    return O3G_ERR_CUDA;
+  }
+  *out = fn;
+  return O3G_OK;
+}
+
+// a 2-D FP32 tensor map: `inner` contiguous elements per line, `outer` lines `stride`
+// elements apart, boxes of 32 x 128 with the 128-byte swizzle; reads outside are zeros
+int32_t make_map(CUtensorMap* map, const float* base, long long inner, long long outer, long long stride) {
+  EncodeTiled enc;
+  O3G_TRY(encode_fn(&enc));
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) || ((stride * 4) & 15) || inner <= 0 || outer <= 0) {
+    set_error("tensor-core GEMM: operand not 16-byte aligned");
+    return O3G_ERR_INVALID_ARG;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+  const cuuint64_t strides[1] = {(cuuint64_t)(stride * 4)};
+  const cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    char msg[96];
+    std::snprintf(msg, sizeof(msg), "tensor-core GEMM: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    set_error(msg);
+    return O3G_ERR_CUDA;
+  }
+  return O3G_OK;
+}
+
+}  // namespace
+
+size_t tc_gemm_scratch_floats(int m, int k) {
+  const size_t kp = (size_t)(k + kTK - 1) / kTK * kTK;
+  return (size_t)((m + kTM - 1) / kTM * kTM) * kp;
+}
+
+int32_t tc_gemm_sub(int m, int n, int k, const float* A, long long lda, const float* B, long long ldb, float* C,
+                    long long ldc, float* at, int* err, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || k <= 0) return O3G_OK;
+  const int kp = (k + kTK - 1) / kTK * kTK;
+  k_transpose_pad<<<dim3((m + 31) / 32, kp / 32), dim3(32, 8), 0, st>>>(A, lda, m, k, kp, at);
+  note_launch();
+  CUtensorMap ta, tb;
+  O3G_TRY(make_map(&ta, at, kp, m, kp));
+  O3G_TRY(make_map(&tb, B, k, n, ldb));
+  static std::once_flag attr;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr, [] {
+    attr_err = cudaFuncSetAttribute(k_tc_gemm_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
+  });
+  O3G_CUDA_TRY(attr_err);
+  GemmArgs g{C, ldc, m, n, kp / kTK, err};
+  k_tc_gemm_sub<<<dim3((m + kTM - 1) / kTM, (n + kTN - 1) / kTN), kGemmThreads, kGemmSmem, st>>>(ta, tb, g);
+  note_launch();
+  O3G_CUDA_TRY(cudaGetLastError());
+  return O3G_OK;
+}
+
+}  // namespace o3g
+
+extern "C" int32_t o3g_gemm_tf32_sub(int32_t m, int32_t n, int32_t k, const float* A, int64_t lda, const float* B,
+                                     int64_t ldb, float* C, int64_t ldc, void* stream) {
+  using namespace o3g;
+  if (m < 0 || n < 0 || k < 0 || (m > 0 && k > 0 && (!A || lda < m)) || (n > 0 && k > 0 && (!B || ldb < k)) ||
+      (m > 0 && n > 0 && (!C || ldc < m))) {
+    set_error("o3g_gemm_tf32_sub: bad sizes or pointers");
+    return O3G_ERR_INVALID_ARG;
+  }
+  if (m == 0 || n == 0 || k == 0) return O3G_OK;
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+  cudaStream_t st = (cudaStream_t)stream;
+  Workspace* ws = nullptr;
+  const size_t at_bytes = align_up(tc_gemm_scratch_floats(m, k) * sizeof(float));
+  O3G_TRY(workspace_get(st, at_bytes + 256, &ws));
+  float* at = reinterpret_cast<float*>(ws->base);
+  int* err = reinterpret_cast<int*>(ws->base + at_bytes);
+  O3G_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  O3G_TRY(tc_gemm_sub(m, n, k, A, lda, B, ldb, C, ldc, at, err, st));
+  int herr = 0;
+  O3G_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  O3G_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) {
+    set_error("o3g_gemm_tf32_sub: a pipeline wait timed out");
+    return O3G_ERR_TIMEOUT;
+  }
+  return O3G_OK;
+}

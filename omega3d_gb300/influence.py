@@ -539,6 +539,42 @@ class BEM:
             self.strengths = x
         return (x, xd) if x64 else x
 
+    def solve_many(self, B, tol=1e-10, max_iter=30, stream=None, x64=False, method="lu", restart=60):
+        """Several right-hand sides at once: B is (nrhs, n), one right-hand side per row
+        (numpy or torch CUDA float32).  Each refinement sweep / GMRES iteration streams the
+        matrix once for up to 8 of them.  Returns X (nrhs, n) float32 (and the FP64 X64 if
+        asked); per-column refinement or iteration counts and residuals in self.iters_many,
+        self.relres_many."""
+        if method not in ("lu", "gmres"):
+            raise ValueError("method must be 'lu' or 'gmres'")
+        if method == "lu" and not self.factored:
+            self.factor(stream)
+        on = _is_dev(B)
+        k = int(B.shape[0])
+        if B.shape != (k, self.n):
+            raise ValueError("B must have shape (nrhs, %d)" % self.n)
+        if on:
+            B = B.contiguous().float()
+            X = torch.empty((k, self.n), dtype=torch.float32, device=B.device)
+            Xd = torch.empty((k, self.n), dtype=torch.float64, device=B.device) if x64 else None
+        else:
+            B = np.ascontiguousarray(B, np.float32)
+            X = np.empty((k, self.n), np.float32)
+            Xd = np.empty((k, self.n), np.float64) if x64 else None
+        its = np.zeros(max(k, 1), np.int32)
+        rrs = np.zeros(max(k, 1), np.float64)
+        mem, sh = L.MEM_DEVICE if on else L.MEM_HOST, ExecEnv(stream=stream).stream_handle(on)
+        xdp = None if Xd is None else _base(Xd)
+        if method == "lu":
+            st = L.lib().o3g_bem_solve_many(self.h, k, _base(B), _base(X), xdp, mem, tol, max_iter,
+                                            its.ctypes.data, rrs.ctypes.data, sh)
+        else:
+            st = L.lib().o3g_bem_solve_gmres_many(self.h, k, _base(B), _base(X), xdp, mem, tol, max_iter, restart,
+                                                  its.ctypes.data, rrs.ctypes.data, sh)
+        self.iters_many, self.relres_many = its[:k].copy(), rrs[:k].copy()
+        L.check(st, "o3g_bem_solve_many" if method == "lu" else "o3g_bem_solve_gmres_many")
+        return (X, Xd) if x64 else X
+
     def get_str(self, cstart, ncols):
         return self.strengths[cstart:cstart + ncols]
 

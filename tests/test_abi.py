@@ -73,6 +73,13 @@ def _prototypes():
     return out
 
 
+def test_every_entry_point_has_declared_argument_types(built_lib):
+    """A ctypes call without argtypes passes Python ints as 32-bit C ints, which truncates
+    device pointers: every entry point of the header must have its argument types declared."""
+    missing = [n for n in L.header_symbols() if getattr(built_lib, n).argtypes is None]
+    assert not missing, missing
+
+
 def test_bindings_match_header_prototypes(built_lib):
     """Every entry point the Python binding declares argtypes for takes as many arguments
     as its C prototype (a miscounted argtypes list would shift every later pointer)."""

@@ -195,3 +195,47 @@ def test_sphere_gmres_agrees_with_lu_and_fp64(cuda, nunk):
     for v in (xg64, xl64):
         assert np.abs(v.cpu().numpy() - xref).max() <= 1e-9 * np.abs(xref).max()
     assert it_g <= 60       # a well-conditioned second-kind system
+
+
+@pytest.mark.parametrize("method", ["lu", "gmres"])
+@pytest.mark.parametrize("nrhs", [1, 2, 3, 8, 11])
+def test_many_right_hand_sides_match_fp64_lu(cuda, method, nrhs):
+    """o3g_bem_solve_many / o3g_bem_solve_gmres_many: every column against an FP64 LU of the
+    same FP32 matrix (1e-9 relative) and to ||b - A x|| / ||b|| <= 1e-10; the columns come out
+    as the single-vector solves give them (1e-9 relative); 11 columns run in two groups;
+    host and device memory give the same bits."""
+    import torch
+    n = 1500
+    rng = np.random.default_rng(70 + nrhs)
+    A = rng.normal(size=(n, n)) / np.sqrt(n) + 2.0 * np.eye(n)
+    B = rng.normal(size=(nrhs, n)).astype(np.float32)
+    B[0] *= 1e-3                                   # uneven scales converge at different sweeps
+    bem = G.BEM(n)
+    bem.set_block(0, 0, np.ascontiguousarray(A.T.astype(np.float32)))
+    X, X64 = bem.solve_many(B, tol=1e-10, max_iter=300 if method == "gmres" else 30, method=method, x64=True)
+    assert (bem.relres_many <= 1e-10).all() and bem.iters_many.shape == (nrhs,)
+    A32 = A.astype(np.float32).astype(np.float64)
+    Xref = np.linalg.solve(A32, B.astype(np.float64).T).T
+    for c in range(nrhs):
+        assert np.linalg.norm(B[c] - A32 @ X64[c]) / np.linalg.norm(B[c]) <= 1e-10
+        assert np.abs(X64[c] - Xref[c]).max() <= 1e-9 * np.abs(Xref[c]).max()
+        x1, x164 = bem.solve(B[c], tol=1e-10, max_iter=300 if method == "gmres" else 30, method=method, x64=True)
+        assert np.abs(X64[c] - x164).max() <= 1e-9 * np.abs(x164).max()
+    Xg, Xg64 = bem.solve_many(torch.from_numpy(B).cuda(), tol=1e-10, max_iter=300 if method == "gmres" else 30,
+                              method=method, x64=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(Xg64.cpu().numpy(), X64)
+
+
+def test_many_right_hand_sides_empty_and_zero_columns(cuda):
+    n = 300
+    rng = np.random.default_rng(80)
+    A = rng.normal(size=(n, n)) / np.sqrt(n) + 2.0 * np.eye(n)
+    bem = G.BEM(n)
+    bem.set_block(0, 0, np.ascontiguousarray(A.T.astype(np.float32)))
+    for method in ("lu", "gmres"):
+        X = bem.solve_many(np.zeros((0, n), np.float32), method=method)
+        assert X.shape == (0, n)
+        B = np.stack([np.zeros(n, np.float32), rng.normal(size=n).astype(np.float32)])
+        X = bem.solve_many(B, tol=1e-10, max_iter=300, method=method)
+        assert not X[0].any() and bem.relres_many[1] <= 1e-10

@@ -523,3 +523,16 @@ def test_oracle_gmres_restarted_solves_bem_system():
     # a restart shorter than the iteration count still converges
     x2_, it2, rel2 = O.gmres_restarted(A, b, restart=4)
     assert rel2 < 1e-5 and it2 >= it
+
+
+@pytest.mark.parametrize("core", ["rm", "gauss", "exp"])
+def test_o3_timing_build_agrees_with_the_checker_build(core):
+    """The -O3 build the CPU baseline is timed with (the reference's Release optimisation,
+    contraction allowed) computes the same sums as the bit-exact -O2 checker build, up to
+    rounding: 1e-6 per target (prec 1: float pairs, double sums)."""
+    from omega3d_gb300.metrics import rel_err
+    x, s, r = W.gaussian_cloud(3000, seed=61, pos_std=0.3)
+    tx, tr = x[:, :500].copy(), r[:500].copy()
+    a = O.points_affect_points(x, r, s, tx, tr, True, core, 1)
+    b = O.points_affect_points(x, r, s, tx, tr, True, core, 1, fast=True)
+    assert rel_err(b[0], a[0])[0] <= 1e-6 and rel_err(b[1], a[1])[0] <= 1e-6

@@ -207,7 +207,10 @@ def test_branch_edges_vs_reference_build(cuda, core):
         form 1 - exp(-x) makes of the exp results: CUDA's expf and the host's libm may
         differ by up to ~3 ulp, which 1 - e amplifies by e/(1 - e), so 4 ulp(1) e/(1 - e)
         more (2.4e-4 at x = 0.001, 5e-7 at x = 1).
-      * COMPENSATED vs the reference's FP64 build: 2e-6.
+      * COMPENSATED vs the reference's FP64 build: 2e-6.  At the exponential core's exact
+        switch points (d^3/sigma^3 = 0.001 and 16 to the rounding of the inputs) a float and
+        a double evaluation of the same pair may land on either side, as the reference's own
+        float and double builds do, so there the bound is the jump, 6e-4.
       * FP64 (double entry point) vs FP64 build: 1e-11.
     """
     d = np.load(os.path.join(GOLD, "branch_edges.npz"))
@@ -215,8 +218,10 @@ def test_branch_edges_vs_reference_build(cuda, core):
     e = np.exp(-rel)
     mid = (rel >= 1e-3 * 0.999) & (rel <= 16.0 * 1.001)
     tol_p = np.full(rel.size, 5e-6)
+    tol_c = np.full(rel.size, 2e-6)
     if core == "exp":
         tol_p = tol_p + np.where(mid, 4 * 2.0 ** -24 * e / np.maximum(-np.expm1(-rel), 1e-30), 0.0)
+        tol_c[np.isclose(rel, 1e-3, rtol=1e-9) | np.isclose(rel, 16.0, rtol=1e-9)] = 6e-4
     for tag, tx, tr in (("pg", d["tx_p"], d["tr"]), ("fg", d["tx_f"], None)):
         u, g = gpu_eval(d["sx"], d["ss"], d["sr"], tx, tr, True, core, "plain")
         eu = _per_pair_err(u, d["%s_%s_u_p0" % (core, tag)])
@@ -225,14 +230,14 @@ def test_branch_edges_vs_reference_build(cuda, core):
         u, g = gpu_eval(d["sx"], d["ss"], d["sr"], tx, tr, True, core, "compensated")
         eu = _per_pair_err(u, d["%s_%s_u_p2" % (core, tag)])
         eg = _per_pair_err(g, d["%s_%s_g_p2" % (core, tag)])
-        assert eu.max() <= 2e-6 and eg.max() <= 2e-6, (tag, eu.max(), eg.max())
+        assert (eu <= tol_c).all() and (eg <= tol_c).all(), (tag, eu.max(), eg.max())
         u, g = gpu_eval(d["sx"], d["ss"], d["sr"], tx, tr, True, core, "fp64", dtype=np.float64)
         assert _per_pair_err(u, d["%s_%s_u_p2" % (core, tag)]).max() <= 1e-11
         assert _per_pair_err(g, d["%s_%s_g_p2" % (core, tag)]).max() <= 1e-11
     u, _ = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx_p"], d["tr"], False, core, "plain")
     assert (_per_pair_err(u, d["%s_pv_u_p0" % core]) <= tol_p).all()
     u, _ = gpu_eval(d["sx"], d["ss"], d["sr"], d["tx_p"], d["tr"], False, core, "compensated")
-    assert _per_pair_err(u, d["%s_pv_u_p2" % core]).max() <= 2e-6
+    assert (_per_pair_err(u, d["%s_pv_u_p2" % core]) <= tol_c).all()
 
 
 @pytest.mark.parametrize("method", [(1, 0), (0, 0), (3, 1)])
