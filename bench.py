@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-bem", action="store_true")
     ap.add_argument("--skip-bem-fp64", action="store_true", help="skip the FP64 LU comparator (~50 s)")
+    ap.add_argument("--bem-level", type=int, default=5,
+                    help="sphere refinement levels of the BEM section (5: 20,480 panels; smaller for profiling)")
     ap.add_argument("--skip-ring", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-splitmerge", action="store_true")
@@ -198,7 +200,7 @@ def bench_bem(args, G, torch, W, fp64=True):
     residual refinement to 1e-10.  Reported for 2 unknowns per panel (n = 40,960) and the
     reference's default 3 (n = 61,440), after one untimed warm-up pass at each size."""
     out = {}
-    x, i = G.generate_ovoid(5, 2.0, 2.0, 2.0)
+    x, i = G.generate_ovoid(args.bem_level, 2.0, 2.0, 2.0)
     px, ps, pr = W.shell_particles(100000, seed=3)
     src = G.Points(*(torch.from_numpy(a).cuda() for a in (px, ps, pr)))
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
@@ -297,6 +299,53 @@ def bench_many_rhs(bem, rhs, torch, ev):
                            "max_relres": float(bem.relres_many.max()), "iterations": bem.iters_many.tolist()}
         out["k%d" % k] = row
     out["single_ms"] = single
+    return out
+
+
+def measured_peaks():
+    """MEASURED_PEAKS.json (written beside this file by the measuring harness), or {}."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def bench_tc_gemm(G, torch, m=8192, n=8192, k=512, reps=5):
+    """The LU's trailing update on its own: C -= A B (o3g_gemm_tf32_sub, tcgen05 kind::tf32)
+    at the size of a mid-factorisation update, k = 512 (the outer panel).  Achieved TFLOP/s
+    (2 m n k per call) against the TF32 tensor roof, taken as half the measured dense bf16
+    rate (MEASURED_PEAKS.json bf16_tflops; TF32 runs at half the bf16 rate), and the HBM
+    traffic the update cannot avoid (C read and written once, A and B read) against the
+    measured copy bandwidth."""
+    g = torch.Generator(device="cuda").manual_seed(11)
+    A = torch.randn((k, m), device="cuda", generator=g)       # column-major m x k
+    B = torch.randn((n, k), device="cuda", generator=g)       # column-major k x n
+    C = torch.randn((n, m), device="cuda", generator=g)
+    lib = G.lib()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    times = []
+    for _ in range(reps + 1):
+        e0, e1 = ev(), ev()
+        e0.record()
+        st = lib.o3g_gemm_tf32_sub(m, n, k, A.data_ptr(), m, B.data_ptr(), k, C.data_ptr(), m, None)
+        e1.record()
+        torch.cuda.synchronize()
+        if st != 0:
+            raise RuntimeError(lib.o3g_last_error().decode())
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times[1:])
+    tflops = 2.0 * m * n * k / (ms * 1e-3) / 1e12
+    gb = (2.0 * m * n + m * k + k * n) * 4 / 1e9
+    pk = measured_peaks()
+    out = {"m": m, "n": n, "k": k, "ms": ms, "tflops": tflops, "hbm_gb": gb, "gbs": gb / (ms * 1e-3),
+           "note": "includes the K-major copy of A and the stream synchronisation of the entry point"}
+    if pk.get("bf16_tflops"):
+        out["tf32_roof_tflops"] = pk["bf16_tflops"] / 2.0
+        out["frac_of_tf32_roof"] = tflops / out["tf32_roof_tflops"]
+    if pk.get("hbm_gbs"):
+        out["frac_of_hbm"] = out["gbs"] / pk["hbm_gbs"]
     return out
 
 
@@ -735,6 +784,7 @@ def guarded(fn):
 
 def bem_section(args, G, torch, W, rank):
     bem = bench_bem(args, G, torch, W, fp64=not args.skip_bem_fp64)
+    bem["tc_gemm_update"] = guarded(lambda: bench_tc_gemm(G, torch))
     if rank == 0:
         bem["cpu_baseline_nunk2"] = cpu = bench_bem_cpu(W)
         g = bem["nunk2"]["gmres"]["total_ms_with_rhs_and_assembly"] * 1e-3

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # bases, areas) rounds exactly like the reference on both x86-64 and aarch64
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE]
-LINK_LIBS = ["-lcublas", "-lcudart"]
+LINK_LIBS = ["-lcudart"]
 
 
 def nvcc():

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
   constexpr int NP = ACC ? 2 * NC : NC;
   constexpr int TB = kBlock * TPT;
   static_assert(std::is_same<T, float>::value, "the batched sums are FP32 (packed pair arithmetic)");
-  __shared__ float4 Q[5][kBlock / 2];   // the staged tile as source pairs (stage_pair)
+  __shared__ float4 QB[2][5][kBlock / 2];   // staged tiles as source pairs, double-buffered
   __shared__ int s_item, s_last;
   // the Gaussian core's polynomial table, read from shared memory by the near-field pairs
   __shared__ float gsh[C == CORE_GAUSS && std::is_same<T, float>::value ? kGaussPolyStride * kGaussPolyN : 1];
@@ -113,10 +113,16 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
 #pragma unroll
       for (int c = 0; c < NH; ++c) { hi[k][c] = 0.f; lo[k][c] = 0.f; }
 
+    // double-buffered tiles, as in k_pair_f: one barrier per tile
+    if (item.y < item.z)
+      stage_pair(a.spos[(size_t)item.y * kBlock + tid], a.sstr[(size_t)item.y * kBlock + tid], QB[0], tid);
     for (int tile = item.y; tile < item.z; ++tile) {
       __syncthreads();
-      stage_pair(a.spos[(size_t)tile * kBlock + tid], a.sstr[(size_t)tile * kBlock + tid], Q, tid);
-      __syncthreads();
+      const int buf = (tile - item.y) & 1;
+      if (tile + 1 < item.z)
+        stage_pair(a.spos[(size_t)(tile + 1) * kBlock + tid], a.sstr[(size_t)(tile + 1) * kBlock + tid],
+                   QB[buf ^ 1], tid);
+      const float4 (*Q)[kBlock / 2] = QB[buf];
       if constexpr (CLASSIFY) {
         if (!live) continue;
 #pragma unroll 1

@@ -12,7 +12,8 @@
 //         pivot and both rows to swap, so a column costs one barrier;
 //       - k_laswp: the panel's row interchanges applied to the other columns;
 //       - k_trsm_unit_lower: U12 = L11^-1 A12, one warp per column, L11 in shared memory;
-//       - trailing update A22 -= L21 U12 as a TF32 tensor-core GEMM (cuBLAS, a plain GEMM);
+//       - trailing update A22 -= L21 U12 on the tensor cores (o3g_tcgemm.cu: tcgen05, TF32
+//         products, FP32 sums), two-level blocking so the big updates have k = 512;
 //   * iterative refinement: residuals r = b - A x formed FP64-accurately (double-single
 //     FP32 arithmetic, k_matvec_ds) from the unfactored FP32 matrix and the FP64 iterate,
 //     corrections from the FP32 factors (forward/back substitution in one cooperative kernel
@@ -24,7 +25,6 @@
 // blocks check, so a fault in the barrier logic ends the kernel instead of hanging.
 #include "o3g_common.cuh"
 
-#include <cublas_v2.h>
 
 #include <algorithm>
 #include <cmath>
@@ -671,7 +671,6 @@ struct o3g_bem {
   int* flags = nullptr;   // [0] barrier error, [1] singular column + 1, [2] barrier arrivals,
                           // [4] tensor-core update error
   float* tcw = nullptr;   // K-major copies of the update's left operand (n x 512)
-  cublasHandle_t cublas = nullptr;
   bool factored = false;
   int panel_blocks = 0, solve_blocks = 0;
 };
@@ -725,12 +724,6 @@ extern "C" int32_t o3g_bem_create(int64_t n, o3g_bem_t** out) {
     return O3G_ERR_ALLOC;
   }
   cudaMemset(h->A, 0, mat);
-  if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS) {
-    set_error("o3g_bem_create: cublasCreate failed");
-    cudaFree(h->A); cudaFree(h->LU); cudaFree(h->piv); cudaFree(h->perm); cudaFree(h->flags);
-    delete h;
-    return O3G_ERR_CUDA;
-  }
   *out = h;
   return O3G_OK;
 }
@@ -741,7 +734,6 @@ extern "C" int32_t o3g_bem_destroy(o3g_bem_t* h) {
   cudaFree(h->A); cudaFree(h->LU); cudaFree(h->piv); cudaFree(h->perm); cudaFree(h->flags); cudaFree(h->scratch);
   cudaFree(h->dinv);
   cudaFree(h->tcw);
-  if (h->cublas) cublasDestroy(h->cublas);
   h->A = nullptr;
   delete h;
   return O3G_OK;
@@ -1076,9 +1068,83 @@ extern "C" int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double*
   return O3G_OK;
 }
 
+// ---- the Krylov bases' FP64 operations (Gram-Schmidt, norms, updates), sums in a fixed order
+namespace o3g {
+constexpr int kKrylovRows = 4096;   // rows per block of the reductions
+
+// part[b kc + j] = sum over the rows [b R, b R + R) of V[j n + i] w[i], j < kc
+__global__ void __launch_bounds__(256) k_kry_dots(const double* __restrict__ V, int n, int kc,
+                                                  const double* __restrict__ w, double* __restrict__ part) {
+  __shared__ double red[8];
+  const int r0 = blockIdx.x * kKrylovRows, r1 = min(n, r0 + kKrylovRows);
+  for (int j = 0; j < kc; ++j) {
+    double s = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) s = fma(V[(size_t)j * n + i], w[i], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) a += red[q];
+      part[(size_t)blockIdx.x * kc + j] = a;
+    }
+    __syncthreads();
+  }
+}
+
+// h[j] = sum over the nb blocks, in block order, of part[b kc + j]
+__global__ void k_kry_sum(const double* __restrict__ part, int nb, int kc, double* __restrict__ h) {
+  for (int j = threadIdx.x; j < kc; j += blockDim.x) {
+    double a = 0.0;
+    for (int b = 0; b < nb; ++b) a += part[(size_t)b * kc + j];
+    h[j] = a;
+  }
+}
+
+// y[i] += alpha sum_j V[j n + i] h[j], kc <= 512
+__global__ void __launch_bounds__(256) k_kry_update(const double* __restrict__ V, int n, int kc,
+                                                    const double* __restrict__ h, double alpha, double* y) {
+  __shared__ double hs[512];
+  for (int j = threadIdx.x; j < kc; j += blockDim.x) hs[j] = h[j];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int j = 0; j < kc; ++j) s = fma(V[(size_t)j * n + i], hs[j], s);
+  y[i] = fma(alpha, s, y[i]);
+}
+
+__global__ void k_kry_scale(double* w, int n, double s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) w[i] *= s;
+}
+
+namespace {
+// one classical Gram-Schmidt pass: hp = V^T w (kc columns), w -= V hp
+void gs_pass(const double* V, int n, int kc, double* w, double* hp, double* part, cudaStream_t st) {
+  const int nb = (n + kKrylovRows - 1) / kKrylovRows;
+  k_kry_dots<<<nb, 256, 0, st>>>(V, n, kc, w, part);
+  k_kry_sum<<<1, 256, 0, st>>>(part, nb, kc, hp);
+  k_kry_update<<<(n + 255) / 256, 256, 0, st>>>(V, n, kc, hp, -1.0, w);
+  note_launch(3);
+}
+// per-block partial sums of w^2 into part (nb of them), summed on the host in order
+void norm_partials(const double* w, int n, double* part, cudaStream_t st) {
+  k_kry_dots<<<(n + kKrylovRows - 1) / kKrylovRows, 256, 0, st>>>(w, n, 1, w, part);
+  note_launch();
+}
+double host_sum(const std::vector<double>& v) {
+  double a = 0.0;
+  for (double x : v) a += x;
+  return a;
+}
+}  // namespace
+}  // namespace o3g
+
 // ---- GMRES: the reference's solver (Eigen GMRES, BEM.h:182-202) ----------------------------
 // Restarted GMRES(m) on the unfactored FP32 matrix: FP64 Krylov vectors, classical
-// Gram-Schmidt with one reorthogonalisation (cuBLAS DGEMV on the n x (k+1) basis), Givens
+// Gram-Schmidt with one reorthogonalisation (k_kry_dots / k_kry_update on the n x (k+1)
+// basis, sums in a fixed order), Givens
 // rotations of the small Hessenberg matrix on the host, FP64-accurate matrix products
 // (k_matvec_ds).  The true residual ||b - A x|| / ||b|| (BEM.h:227-230) is recomputed at
 // every restart and decides convergence.  No preconditioner: the vortex-sheet rows of the
@@ -1099,8 +1165,10 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
   const int m = std::min(restart, max_iter);
   const int ncb = (n + kMvChunk - 1) / kMvChunk;
   const int nrb = (n + 255) / 256;
+  const int nkb = (n + kKrylovRows - 1) / kKrylovRows;
   const size_t need = align_up((size_t)(m + 1) * n * 8) + 2 * align_up((size_t)n * 8) + 4 * align_up((size_t)n * 4) +
-                      align_up((size_t)ncb * n * 8) + align_up((size_t)nrb * 8) + align_up((size_t)2 * (m + 1) * 8);
+                      align_up((size_t)ncb * n * 8) + align_up((size_t)nrb * 8) + align_up((size_t)2 * (m + 1) * 8) +
+                      2 * align_up((size_t)nkb * (m + 1) * 8);
   O3G_TRY(bem_scratch(h, need));
   Carve cv(h->scratch);
   double* V = cv.take<double>((size_t)(m + 1) * n);
@@ -1113,11 +1181,9 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
   double* part = cv.take<double>((size_t)ncb * n);
   double* nrm = cv.take<double>(nrb);
   double* hd = cv.take<double>(2 * (size_t)(m + 1));
-  if (cublasSetStream(h->cublas, st) != CUBLAS_STATUS_SUCCESS) {
-    set_error("o3g_bem_solve_gmres: cublasSetStream failed");
-    return O3G_ERR_CUDA;
-  }
-  cublasSetPointerMode(h->cublas, CUBLAS_POINTER_MODE_HOST);
+  double* kpart = cv.take<double>((size_t)nkb * (m + 1));
+  double* npart = cv.take<double>((size_t)nkb * (m + 1));
+  std::vector<double> hnp((size_t)nkb);
   O3G_CUDA_TRY(cudaMemcpyAsync(bf, b, (size_t)n * 4, mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice
                                                                            : cudaMemcpyDeviceToDevice, st));
   k_f2d<<<nrb, 256, 0, st>>>(bf, bd, n);
@@ -1145,11 +1211,6 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
     }
     return O3G_OK;
   };
-  auto cublas_ok = [&](cublasStatus_t cs, const char* what) -> int32_t {
-    if (cs == CUBLAS_STATUS_SUCCESS) return O3G_OK;
-    set_error(what);
-    return O3G_ERR_CUDA;
-  };
   double bb = 0.0;
   O3G_TRY(matvec(nullptr, bd, V, &bb));           // V0 = b, ||b||^2
   const double bnorm = std::sqrt(bb);
@@ -1160,15 +1221,14 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
   if (bnorm > 0.0) {
     std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), hc(2 * (size_t)(m + 1));
     auto Hat = [&](int i, int k) -> double& { return H[(size_t)k * (m + 1) + i]; };
-    const double one = 1.0, zero = 0.0, minus1 = -1.0;
     for (;;) {
       double rr = 0.0;
       O3G_TRY(matvec(total > 0 ? xd : nullptr, bd, V, &rr));   // V0 = r = b - A x
       rel = std::sqrt(rr) / bnorm;
       if (rel <= tol || total >= max_iter) break;
       const double beta = std::sqrt(rr);
-      const double ib = 1.0 / beta;
-      O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &ib, V, 1), "o3g_bem_solve_gmres: cublasDscal"));
+      k_kry_scale<<<nrb, 256, 0, st>>>(V, n, 1.0 / beta);
+      note_launch();
       std::fill(g.begin(), g.end(), 0.0);
       g[0] = beta;
       int k = 0;
@@ -1177,22 +1237,17 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
         double* w = V + (size_t)(k + 1) * n;
         O3G_TRY(matvec(vk, nullptr, w, nullptr));
         // classical Gram-Schmidt, twice
-        for (int pass = 0; pass < 2; ++pass) {
-          double* hp = hd + (size_t)pass * (m + 1);
-          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_T, n, k + 1, &one, V, n, w, 1, &zero, hp, 1),
-                            "o3g_bem_solve_gmres: cublasDgemv"));
-          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, k + 1, &minus1, V, n, hp, 1, &one, w, 1),
-                            "o3g_bem_solve_gmres: cublasDgemv"));
-        }
-        double wn = 0.0;
-        O3G_TRY(cublas_ok(cublasDnrm2(h->cublas, n, w, 1, &wn), "o3g_bem_solve_gmres: cublasDnrm2"));
+        for (int pass = 0; pass < 2; ++pass) gs_pass(V, n, k + 1, w, hd + (size_t)pass * (m + 1), kpart, st);
+        norm_partials(w, n, npart, st);
         O3G_CUDA_TRY(cudaMemcpyAsync(hc.data(), hd, 2 * (size_t)(m + 1) * 8, cudaMemcpyDeviceToHost, st));
+        O3G_CUDA_TRY(cudaMemcpyAsync(hnp.data(), npart, (size_t)nkb * 8, cudaMemcpyDeviceToHost, st));
         O3G_CUDA_TRY(cudaStreamSynchronize(st));
+        const double wn = std::sqrt(host_sum(hnp));
         for (int i = 0; i <= k; ++i) Hat(i, k) = hc[i] + hc[(size_t)(m + 1) + i];
         Hat(k + 1, k) = wn;
         if (wn > 0.0) {
-          const double iw = 1.0 / wn;
-          O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &iw, w, 1), "o3g_bem_solve_gmres: cublasDscal"));
+          k_kry_scale<<<nrb, 256, 0, st>>>(w, n, 1.0 / wn);
+          note_launch();
         }
         // previous rotations, then a new one that zeroes H(k+1, k)
         for (int i = 0; i < k; ++i) {
@@ -1218,8 +1273,8 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
         y[i] = Hat(i, i) != 0.0 ? sacc / Hat(i, i) : 0.0;
       }
       O3G_CUDA_TRY(cudaMemcpyAsync(hd, y.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
-      O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, k, &one, V, n, hd, 1, &one, xd, 1),
-                        "o3g_bem_solve_gmres: cublasDgemv"));
+      k_kry_update<<<nrb, 256, 0, st>>>(V, n, k, hd, 1.0, xd);
+      note_launch();
     }
   }
   tm.end(st);
@@ -1698,9 +1753,10 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
   const int ncb = (n + kMvChunkM - 1) / kMvChunkM;
   const int nrb = (n + 255) / 256;
   const size_t kn = (size_t)KM * n;
+  const int nkb = (n + kKrylovRows - 1) / kKrylovRows;
   const size_t need = align_up(kn * (m + 1) * 8) + 2 * align_up(kn * 8) + 3 * align_up(kn * 4) +
                       align_up((size_t)ncb * kn * 8) + align_up((size_t)KM * nrb * 8) +
-                      align_up((size_t)KM * 2 * (m + 1) * 8);
+                      align_up((size_t)KM * 2 * (m + 1) * 8) + 2 * align_up((size_t)nkb * (m + 1) * 8);
   O3G_TRY(bem_scratch(h, need));
   Carve cv(h->scratch);
   double* V = cv.take<double>(kn * (m + 1));     // basis of column c at V + c (m+1) n
@@ -1712,19 +1768,11 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
   double* part = cv.take<double>((size_t)ncb * kn);
   double* nrm = cv.take<double>((size_t)KM * nrb);
   double* hd = cv.take<double>((size_t)KM * 2 * (m + 1));
-  if (cublasSetStream(h->cublas, st) != CUBLAS_STATUS_SUCCESS) {
-    set_error("o3g_bem_solve_gmres_many: cublasSetStream failed");
-    return O3G_ERR_CUDA;
-  }
-  cublasSetPointerMode(h->cublas, CUBLAS_POINTER_MODE_HOST);
-  auto cublas_ok = [&](cublasStatus_t cs, const char* what) -> int32_t {
-    if (cs == CUBLAS_STATUS_SUCCESS) return O3G_OK;
-    set_error(what);
-    return O3G_ERR_CUDA;
-  };
+  double* kpart = cv.take<double>((size_t)nkb * (m + 1));
+  double* npart = cv.take<double>((size_t)nkb * (m + 1));
+  std::vector<double> hnp((size_t)nkb);
   const cudaMemcpyKind h2d = mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const cudaMemcpyKind d2h = mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  const double one = 1.0, zero = 0.0, minus1 = -1.0;
   bool all_converged = true;
   KernelTimer& tm = thread_timer();
   tm.begin(st);
@@ -1792,8 +1840,9 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
             s.done = true;
             continue;
           }
-          const double beta = std::sqrt(rr[q]), ib = 1.0 / beta;
-          O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &ib, Vc(fr[q], 0), 1), "o3g_bem_solve_gmres_many: cublasDscal"));
+          const double beta = std::sqrt(rr[q]);
+          k_kry_scale<<<nrb, 256, 0, st>>>(Vc(fr[q], 0), n, 1.0 / beta);
+          note_launch();
           std::fill(s.g.begin(), s.g.end(), 0.0);
           s.g[0] = beta;
           s.k = 0;
@@ -1820,24 +1869,19 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
         double* Vb = Vc(c, 0);
         double* w = Vc(c, k + 1);
         double* hc_d = hd + (size_t)c * 2 * (m + 1);
-        for (int pass = 0; pass < 2; ++pass) {
-          double* hp = hc_d + (size_t)pass * (m + 1);
-          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_T, n, k + 1, &one, Vb, n, w, 1, &zero, hp, 1),
-                            "o3g_bem_solve_gmres_many: cublasDgemv"));
-          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, k + 1, &minus1, Vb, n, hp, 1, &one, w, 1),
-                            "o3g_bem_solve_gmres_many: cublasDgemv"));
-        }
-        double wn = 0.0;
-        O3G_TRY(cublas_ok(cublasDnrm2(h->cublas, n, w, 1, &wn), "o3g_bem_solve_gmres_many: cublasDnrm2"));
+        for (int pass = 0; pass < 2; ++pass) gs_pass(Vb, n, k + 1, w, hc_d + (size_t)pass * (m + 1), kpart, st);
+        norm_partials(w, n, npart, st);
         std::vector<double> hc(2 * (size_t)(m + 1));
         O3G_CUDA_TRY(cudaMemcpyAsync(hc.data(), hc_d, hc.size() * 8, cudaMemcpyDeviceToHost, st));
+        O3G_CUDA_TRY(cudaMemcpyAsync(hnp.data(), npart, (size_t)nkb * 8, cudaMemcpyDeviceToHost, st));
         O3G_CUDA_TRY(cudaStreamSynchronize(st));
+        const double wn = std::sqrt(host_sum(hnp));
         auto Hat = [&](int i, int kk) -> double& { return s.H[(size_t)kk * (m + 1) + i]; };
         for (int i = 0; i <= k; ++i) Hat(i, k) = hc[i] + hc[(size_t)(m + 1) + i];
         Hat(k + 1, k) = wn;
         if (wn > 0.0) {
-          const double iw = 1.0 / wn;
-          O3G_TRY(cublas_ok(cublasDscal(h->cublas, n, &iw, w, 1), "o3g_bem_solve_gmres_many: cublasDscal"));
+          k_kry_scale<<<nrb, 256, 0, st>>>(w, n, 1.0 / wn);
+          note_launch();
         }
         for (int i = 0; i < k; ++i) {
           const double a = Hat(i, k), cc = Hat(i + 1, k);
@@ -1862,9 +1906,8 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
             s.y[i] = Hat(i, i) != 0.0 ? sacc / Hat(i, i) : 0.0;
           }
           O3G_CUDA_TRY(cudaMemcpyAsync(hc_d, s.y.data(), (size_t)kk * 8, cudaMemcpyHostToDevice, st));
-          O3G_TRY(cublas_ok(cublasDgemv(h->cublas, CUBLAS_OP_N, n, kk, &one, Vb, n, hc_d, 1, &one,
-                                        xd + (size_t)c * n, 1),
-                            "o3g_bem_solve_gmres_many: cublasDgemv"));
+          k_kry_update<<<nrb, 256, 0, st>>>(Vb, n, kk, hc_d, 1.0, xd + (size_t)c * n);
+          note_launch();
           s.fresh = true;
         }
       }

@@ -451,7 +451,10 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
 }
 
 // k_pair for FP32 (PLAIN and COMPENSATED): the same blocks, tiles, far-field classification,
-// splits and epilogue, with the sweep in packed FP32 over pairs of sources.
+// splits and epilogue, with the sweep in packed FP32 over pairs of sources.  The staged
+// tiles are double-buffered: the next tile is loaded into the other buffer before the
+// current one is swept, so one barrier per tile orders both (two, without the second
+// buffer, and the loads' latency in the open).
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT>
 __global__ void __launch_bounds__(kBlock) k_pair_f(const PairArgs<float, float> a) {
   constexpr bool ACC = (MODE == MODE_COMP);
@@ -459,7 +462,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_f(const PairArgs<float, float> 
   constexpr int NA = GRADS ? 15 : 3;
   constexpr int NC = GRADS ? 12 : 3;
   constexpr int NH = ACC ? NC : 1;
-  __shared__ float4 Q[5][kBlock / 2];
+  __shared__ float4 QB[2][5][kBlock / 2];
   // the Gaussian core's polynomial table, read from shared memory by the near-field pairs
   __shared__ float gsh[C == CORE_GAUSS ? kGaussPolyStride * kGaussPolyN : 1];
   const float* gtab = nullptr;
@@ -502,10 +505,17 @@ __global__ void __launch_bounds__(kBlock) k_pair_f(const PairArgs<float, float> 
 
   const int t_begin = split * a.tiles_per_split;
   const int t_end = min(a.ntiles, t_begin + a.tiles_per_split);
+  if (t_begin < t_end)
+    stage_pair(a.spos[(size_t)t_begin * kBlock + tid], a.sstr[(size_t)t_begin * kBlock + tid], QB[0], tid);
   for (int tile = t_begin; tile < t_end; ++tile) {
+    // this tile's buffer is visible after the barrier, which also ends every sweep of the
+    // other buffer (the previous tile), so the next tile may be written there
     __syncthreads();
-    stage_pair(a.spos[(size_t)tile * kBlock + tid], a.sstr[(size_t)tile * kBlock + tid], Q, tid);
-    __syncthreads();
+    const int buf = (tile - t_begin) & 1;
+    if (tile + 1 < t_end)
+      stage_pair(a.spos[(size_t)(tile + 1) * kBlock + tid], a.sstr[(size_t)(tile + 1) * kBlock + tid], QB[buf ^ 1],
+                 tid);
+    const float4 (*Q)[kBlock / 2] = QB[buf];
     if constexpr (CLASSIFY) {
       if (!live) continue;
 #pragma unroll 1

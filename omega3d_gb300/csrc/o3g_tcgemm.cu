@@ -11,7 +11,10 @@
 //     complete_tx on the full barrier, tcgen05.commit on the empty one;
 //   * each slab is 4 MMAs of 128 x 128 x 8 (kind::tf32) into 128 TMEM columns;
 //   * the epilogue reads the accumulator row by row (TMEM lane = row of the tile) and
-//     subtracts it from C with coalesced loads and stores.
+//     subtracts it from C with coalesced loads and stores, 32 columns at a time: all of
+//     a chunk's loads are issued before any store (a load after a store to another column
+//     would otherwise wait for it, the compiler cannot tell they do not overlap);
+//   * two CTAs per SM, so one CTA's epilogue overlaps the other's main loop.
 // Every mbarrier wait is bounded: after kWaitLimit polls it sets the error word, every
 // other wait then gives up at once, the CTA still frees its tensor memory, and the host
 // returns O3G_ERR_TIMEOUT.
@@ -24,7 +27,7 @@
 namespace o3g {
 namespace {
 
-constexpr int kTM = 128, kTN = 128, kTK = 32, kStages = 4;
+constexpr int kTM = 128, kTN = 128, kTK = 32, kStages = 3;   // 3 stages: two CTAs per SM
 constexpr int kTileBytes = kTM * kTK * 4;                  // 16 KB per operand and stage
 constexpr int kGemmThreads = 192;
 constexpr uint32_t kTmemCols = 128;
@@ -121,7 +124,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kGemmThreads, 1)
+__global__ void __launch_bounds__(kGemmThreads, 2)
     k_tc_gemm_sub(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
   extern __shared__ unsigned char smem_raw[];
   // the 128-byte swizzle repeats every 1024 bytes: stage buffers start on 1024-byte boundaries
@@ -198,18 +201,23 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     if (ok) {
       tc_fence_after();
       const bool write = (*(volatile int*)g.err == 0) && row < g.m;
+      const float* __restrict__ cin = g.C + row;
 #pragma unroll 1
-      for (int c0 = 0; c0 < kTN; c0 += 16) {
-        uint32_t v[16];
+      for (int c0 = 0; c0 < kTN; c0 += 32) {
+        float cv[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + c0 + j;
+          cv[j] = (write && col < g.n) ? __ldcs(cin + (size_t)col * g.ldc) : 0.f;
+        }
+        uint32_t v[32];
         tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c0 + 16), v + 16);
         if (write) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < 32; ++j) {
             const int col = n0 + c0 + j;
-            if (col < g.n) {
-              float* p = g.C + (size_t)col * g.ldc + row;
-              *p = *p - __uint_as_float(v[j]);
-            }
+            if (col < g.n) __stcs(g.C + (size_t)col * g.ldc + row, cv[j] - __uint_as_float(v[j]));
           }
         }
       }
