@@ -9,7 +9,9 @@
 //         block keeps its slab of rows in shared memory; per column every block publishes
 //         its local pivot candidate (value, row, the whole row) and, for the block holding
 //         the diagonal row, that row; one bounded grid barrier later every block knows the
-//         pivot and both rows to swap, so a column costs one barrier;
+//         pivot and both rows to swap, so a column costs one barrier.  Each block updates
+//         the next column first, publishes its next candidate, arrives at the barrier, and
+//         runs the rest of the rank-1 update while the other blocks arrive;
 //       - k_laswp: the panel's row interchanges applied to the other columns;
 //       - k_trsm_unit_lower: U12 = L11^-1 A12, one warp per column, L11 in shared memory;
 //       - trailing update A22 -= L21 U12 on the tensor cores (o3g_tcgemm.cu: tcgen05, TF32
@@ -34,7 +36,7 @@
 namespace o3g {
 
 constexpr int kNb = 128;              // panel width
-constexpr int kPanelThreads = 256;
+constexpr int kPanelThreads = 512;
 constexpr int kSolveThreads = 1024;
 constexpr unsigned long long kSpinLimit = 1ull << 25;
 
@@ -57,15 +59,22 @@ inline Barrier make_barrier(int* flags) {
 // Grid-wide barrier on one arrival counter that only grows.  The host zeroes the counter
 // before each cooperative launch (zero_barrier); the k-th barrier of the launch is passed
 // when the counter reaches k * gridDim.x.  One atomic per block and acquire loads of one
-// word: no reset or generation step on the critical path.  Bounded: returns false (in every
-// thread) once the error flag is set, by a timeout here or anywhere else.
-__device__ bool grid_sync(const Barrier& b) {
+// word: no reset or generation step on the critical path.  Bounded: the wait returns false
+// (in every thread) once the error flag is set, by a timeout here or anywhere else.
+//
+// grid_arrive (thread 0, after a __syncthreads that orders the block's writes before it)
+// returns the count that passes this barrier; grid_wait (every thread) waits for it.  Work
+// between the two overlaps the other blocks' arrivals.  Consecutive waits must be separated
+// by a __syncthreads (the result word is shared).
+__device__ __forceinline__ unsigned grid_arrive(const Barrier& b) {
+  __threadfence();
+  const unsigned arrived = atomicAdd(b.count, 1u) + 1u;
+  return (arrived + gridDim.x - 1u) / gridDim.x * gridDim.x + b.extra;
+}
+
+__device__ bool grid_wait(const Barrier& b, unsigned target) {
   __shared__ int ok;
-  __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned arrived = atomicAdd(b.count, 1u) + 1u;
-    const unsigned target = (arrived + gridDim.x - 1u) / gridDim.x * gridDim.x + b.extra;
     unsigned long long it = 0;
     for (;;) {
       unsigned c;
@@ -82,6 +91,13 @@ __device__ bool grid_sync(const Barrier& b) {
   }
   __syncthreads();
   return ok != 0;
+}
+
+__device__ bool grid_sync(const Barrier& b) {
+  __syncthreads();
+  unsigned target = 0;
+  if (threadIdx.x == 0) target = grid_arrive(b);
+  return grid_wait(b, target);
 }
 
 // zeroes the arrival counter of make_barrier(flags) before a cooperative launch
@@ -129,6 +145,51 @@ __device__ __forceinline__ void argmax_merge(float& v, int& i, float ov, int oi)
   if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
 }
 
+// The block's pivot candidate for panel column jc: the block argmax of (best, bi), then
+// warp 0 publishes (|value|, row, the whole row) and warp 1 the diagonal row k0 + jc if this
+// block holds it.  Rows go out in their state after column jc - 1's elimination: in the slab
+// that update is still pending for the columns beyond jc (it runs while the grid barrier
+// fills), so those entries are updated on the fly here, with the same fmaf as the slab's.
+__device__ __forceinline__ void panel_publish(const PanelArgs& a, const float* slab, const float* prow, int jc,
+                                              bool pending, float best, int bi, float* rv, int* ri, int r0, int nr) {
+  const int G = gridDim.x, b = blockIdx.x, jb = a.jb, R = a.R, par = jc & 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
+  if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
+  __syncthreads();
+  const int c = a.k0 + jc;
+  auto put_row = [&](float* dst, int rr) {
+    const float l = pending ? slab[(size_t)(jc - 1) * R + rr] : 0.f;
+    for (int jj = lane; jj < jb; jj += 32) {
+      float v = slab[(size_t)jj * R + rr];
+      if (pending && jj > jc) v = fmaf(-l, prow[jj], v);
+      dst[jj] = v;
+    }
+  };
+  if (warp == 0) {
+    float v = lane < kPanelThreads / 32 ? rv[lane] : -1.f;
+    int i = lane < kPanelThreads / 32 ? ri[lane] : 0x7fffffff;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
+    if (lane == 0) {
+      a.cval[par * G + b] = v;
+      a.crow[par * G + b] = i;
+    }
+    if (v >= 0.f) put_row(a.crows + ((size_t)par * G + b) * jb, i - r0);
+  } else if (warp == 1 && c >= r0 && c < r0 + nr) {
+    put_row(a.drow + par * jb, c - r0);
+  }
+}
+
+// Partial-pivoting LU of the panel's jb columns, rows k0..n-1 spread over the blocks (R rows
+// each, kept in shared memory).  Per column: every block's candidate goes out, one grid
+// barrier, then every block finds the same pivot (largest |value|, first row on ties),
+// swaps, forms its multipliers and updates the next column first -- enough for the next
+// candidate, which is published and the barrier arrived at -- and only then updates the
+// rest of its rows, while the other blocks arrive.
 __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
   extern __shared__ float smem[];
   const int G = gridDim.x, b = blockIdx.x, jb = a.jb, R = a.R;
@@ -142,34 +203,15 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
   const int nr = max(0, min(a.n, r0 + R) - r0);
   if (nr > 0) stage_in(slab, R, a.A + (size_t)a.k0 * a.ld + r0, a.ld, nr, jb);
   __syncthreads();
-  // this thread's best |a(i, c)| over its rows i >= c for the current column
-  float best = -1.f;
-  int bi = 0x7fffffff;
-  for (int r = threadIdx.x; r < nr; r += blockDim.x) argmax_merge(best, bi, fabsf(slab[r]), r0 + r);
+  {
+    float best = -1.f;
+    int bi = 0x7fffffff;
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) argmax_merge(best, bi, fabsf(slab[r]), r0 + r);
+    panel_publish(a, slab, prow, 0, false, best, bi, rv, ri, r0, nr);
+  }
+  if (!grid_sync(a.bar)) return;
   for (int j = 0; j < jb; ++j) {
     const int c = a.k0 + j, par = j & 1;
-    // block argmax (first index on ties) -> candidate (value, row, whole row) published
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-      argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
-    if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
-    __syncthreads();
-    if (warp == 0) {
-      float v = lane < kPanelThreads / 32 ? rv[lane] : -1.f;
-      int i = lane < kPanelThreads / 32 ? ri[lane] : 0x7fffffff;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-        argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
-      if (lane == 0) {
-        a.cval[par * G + b] = v;
-        a.crow[par * G + b] = i;
-      }
-      if (v >= 0.f)
-        for (int jj = lane; jj < jb; jj += 32) a.crows[((size_t)par * G + b) * jb + jj] = slab[(size_t)jj * R + (i - r0)];
-    } else if (warp == 1 && c >= r0 && c < r0 + nr) {
-      for (int jj = lane; jj < jb; jj += 32) a.drow[par * jb + jj] = slab[(size_t)jj * R + (c - r0)];
-    }
-    if (!grid_sync(a.bar)) return;
     // warp 0: global pivot (same answer in every block) and the pivot row
     if (warp == 0) {
       float v = -1.f;
@@ -211,23 +253,49 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
           slab[(size_t)jj * R + (prow_i - r0)] = a.drow[par * jb + jj];
       __syncthreads();
     }
-    // multipliers, rank-1 update, and the next column's local argmax on the fly
+    // multipliers and the next column, with the next column's local argmax on the fly
     const float p = prow[j];
-    best = -1.f;
-    bi = 0x7fffffff;
     const bool nxt = (j + 1 < jb);
+    float best = -1.f;
+    int bi = 0x7fffffff;
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
       if (r0 + r <= c) continue;
       float* row = slab + r;
       if (p != 0.f) {
         const float l = row[(size_t)j * R] / p;
         row[(size_t)j * R] = l;
-        for (int jj = j + 1; jj < jb; ++jj) row[(size_t)jj * R] = fmaf(-l, prow[jj], row[(size_t)jj * R]);
+        if (nxt) row[(size_t)(j + 1) * R] = fmaf(-l, prow[j + 1], row[(size_t)(j + 1) * R]);
       }
       if (nxt) argmax_merge(best, bi, fabsf(row[(size_t)(j + 1) * R]), r0 + r);
     }
+    if (!nxt) break;
+    panel_publish(a, slab, prow, j + 1, p != 0.f, best, bi, rv, ri, r0, nr);
     __syncthreads();
+    unsigned target = 0;
+    if (threadIdx.x == 0) target = grid_arrive(a.bar);
+    // the rest of the rank-1 update, eight loads in flight per thread
+    if (p != 0.f) {
+      for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+        if (r0 + r <= c) continue;
+        float* row = slab + r;
+        const float l = row[(size_t)j * R];
+        int jj = j + 2;
+        for (; jj + 8 <= jb; jj += 8) {
+          float v[8], q[8];
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            v[t] = row[(size_t)(jj + t) * R];
+            q[t] = prow[jj + t];
+          }
+#pragma unroll
+          for (int t = 0; t < 8; ++t) row[(size_t)(jj + t) * R] = fmaf(-l, q[t], v[t]);
+        }
+        for (; jj < jb; ++jj) row[(size_t)jj * R] = fmaf(-l, prow[jj], row[(size_t)jj * R]);
+      }
+    }
+    if (!grid_wait(a.bar, target)) return;
   }
+  __syncthreads();
   if (nr > 0) stage_out(a.A + (size_t)a.k0 * a.ld + r0, a.ld, slab, R, nr, jb);
 }
 

@@ -3,36 +3,54 @@
 //
 // All matrices are column-major FP32 (the BEM's layout).  A (m x k) has rows contiguous,
 // so it is first copied to a K-major (row-major) scratch with k padded to whole 32-column
-// slabs (zeros); B (k x n) is already K-major.  Then:
-//   * one CTA per 128 x 128 tile of C, 6 warps: warp 0 issues TMA loads, warp 1 owns the
-//     tensor-memory allocation and issues the MMAs, warps 2-5 run the epilogue;
+// slabs (zeros); B (k x n) is already K-major.  Then one persistent kernel:
+//   * CTAs come in clusters of two; a cluster walks pairs of 128 x 256 tiles of C that
+//     share their 256 columns (the two CTAs take the two 128-row halves), so every slab of
+//     B is fetched once for both: each CTA loads 128 of its 256 rows with a TMA multicast
+//     into both CTAs' shared memory.  Per 32-deep slab a CTA thus reads 16 KB of A and
+//     16 KB of B from L2 for 128 x 256 outputs (a lone 128 x 128 tile reads 32 KB for half
+//     as many), which keeps the TF32 operand feed below what L2 delivers;
+//   * 10 warps: warp 0 issues the TMA loads, warp 1 owns the tensor memory and issues the
+//     MMAs, warps 2-9 run the epilogue (two warps per 32-lane quarter of tensor memory,
+//     one per 128-column half of the tile);
 //   * k is swept in slabs of 32 (128 bytes of every row, the 128-byte swizzle width) through
 //     a ring of kStages shared-memory stages: full/empty mbarrier pairs, TMA with
-//     complete_tx on the full barrier, tcgen05.commit on the empty one;
-//   * each slab is 4 MMAs of 128 x 128 x 8 (kind::tf32) into 128 TMEM columns;
+//     complete_tx on the full barrier; an empty barrier takes one tcgen05.commit from each
+//     CTA of the pair (the stage is refilled by both);
+//   * each slab is 4 MMAs of 128 x 256 x 8 (kind::tf32) into 256 TMEM columns; the 512
+//     columns hold two accumulators, so the epilogue of one tile overlaps the MMAs of the
+//     next;
 //   * the epilogue reads the accumulator row by row (TMEM lane = row of the tile) and
-//     subtracts it from C with coalesced loads and stores, 32 columns at a time: all of
-//     a chunk's loads are issued before any store (a load after a store to another column
-//     would otherwise wait for it, the compiler cannot tell they do not overlap);
-//   * two CTAs per SM, so one CTA's epilogue overlaps the other's main loop.
+//     subtracts it from C with coalesced streaming loads and stores, 32 columns at a time,
+//     the next chunk's loads in flight while the current one is stored; the first chunk
+//     is loaded before the accumulator is waited for.
 // Every mbarrier wait is bounded: after kWaitLimit polls it sets the error word, every
-// other wait then gives up at once, the CTA still frees its tensor memory, and the host
-// returns O3G_ERR_TIMEOUT.
+// other wait then gives up at once, the CTA still drains its copies, leaves the cluster
+// together with its peer and frees its tensor memory, and the host returns
+// O3G_ERR_TIMEOUT.
 #include "o3g_common.cuh"
 
 #include <cuda.h>
 
+#include <algorithm>
 #include <mutex>
 
 namespace o3g {
 namespace {
 
-constexpr int kTM = 128, kTN = 128, kTK = 32, kStages = 3;   // 3 stages: two CTAs per SM
-constexpr int kTileBytes = kTM * kTK * 4;                  // 16 KB per operand and stage
-constexpr int kGemmThreads = 192;
-constexpr uint32_t kTmemCols = 128;
+constexpr int kTM = 128, kTN = 256, kTK = 32, kStages = 4;
+constexpr int kHalfN = kTN / 2;                            // B rows each CTA of a pair loads
+static_assert(kHalfN == kTM, "A and B boxes share one tensor-map shape");
+constexpr int kABytes = kTM * kTK * 4;                     // 16 KB
+constexpr int kBBytes = kTN * kTK * 4;                     // 32 KB
+constexpr int kStageBytes = kABytes + kBBytes;
+constexpr int kEpiWarps = 8;
+constexpr int kGemmThreads = 64 + 32 * kEpiWarps;
+constexpr uint32_t kTmemCols = 2 * kTN;                    // two accumulators
 constexpr unsigned long long kWaitLimit = 1ull << 26;
-constexpr size_t kGemmSmem = 1024 + (size_t)kStages * 2 * kTileBytes + 256;
+constexpr unsigned long long kDrainLimit = 1ull << 22;
+constexpr int kNumBars = 2 * kStages + 5;                  // full, empty, tmem full[2], tmem empty[2], done
+constexpr size_t kGemmSmem = 1024 + (size_t)kStages * kStageBytes + 8 * kNumBars + 16;
 
 // instruction descriptor of tcgen05.mma kind::tf32: D format F32 (bits 4-5 = 1), A and B
 // TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22,
@@ -44,6 +62,7 @@ struct GemmArgs {
   float* C;
   long long ldc;
   int m, n, nkb;
+  int mpairs, ntiles;      // 128-row tile pairs, 256-column tiles
   int* err;
 };
 
@@ -80,12 +99,44 @@ __device__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
   return false;
 }
 
+// a wait on the CTA's own copies and commits, which always complete: it does not give up
+// when another wait has, only after kDrainLimit polls (then it sets the error word)
+__device__ bool mbar_wait_drain(uint32_t bar, uint32_t parity, int* err) {
+  for (unsigned long long it = 0; it < kDrainLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  atomicCAS(err, 0, O3G_ERR_TIMEOUT);
+  return false;
+}
+
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
           dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
       : "memory");
+}
+
+// the same box into this CTA and its cluster peer (ctaMask 0b11): data and complete_tx land
+// at the same shared-memory offsets in both
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+  const uint16_t mask = 3;
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar), "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128 bytes, 8-row
@@ -109,40 +160,59 @@ __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
+// one arrival on the barrier at this offset in both CTAs of the pair, once the MMAs issued
+// so far have completed
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+  const uint16_t mask = 3;
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+      "h"(mask)
+      : "memory");
+}
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 16 consecutive TMEM columns of this warp's 32 lanes: thread t gets lane (base lane + t)
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
+// 32 consecutive TMEM columns of this warp's 32 lanes: thread t gets lane (base lane + t)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
-      "[%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
-        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+        "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
       : "r"(taddr)
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kGemmThreads, 2)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
     k_tc_gemm_sub(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
   extern __shared__ unsigned char smem_raw[];
-  // the 128-byte swizzle repeats every 1024 bytes: stage buffers start on 1024-byte boundaries
+  // the 128-byte swizzle repeats every 1024 bytes: stage buffers start on 1024-byte
+  // boundaries; both CTAs of a pair have the same layout (multicast writes by offset)
   const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023;
-  unsigned char* sA = reinterpret_cast<unsigned char*>(base);
-  unsigned char* sB = sA + (size_t)kStages * kTileBytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + (size_t)kStages * kTileBytes);   // full, empty, accum
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
+  unsigned char* stages = reinterpret_cast<unsigned char*>(base);             // [kStages][A 16 KB | B 32 KB]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stages + (size_t)kStages * kStageBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kNumBars);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * kTN;
-  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages), accum = smem_u32(bars + 2 * kStages);
+  const uint32_t rank = cluster_rank();
+  const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+  const int ntp = g.mpairs * g.ntiles;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages);
+  const uint32_t tfull0 = smem_u32(bars + 2 * kStages), tempty0 = smem_u32(bars + 2 * kStages + 2);
+  const uint32_t done = smem_u32(bars + 2 * kStages + 4);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 2);          // one commit from each CTA of the pair
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tempty0 + 8 * b, kEpiWarps);
+    }
+    mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -154,70 +224,120 @@ __global__ void __launch_bounds__(kGemmThreads, 2)
   }
   tc_fence_before();
   __syncthreads();
+  // the peer's barriers are initialised before anything is multicast into them
+  cluster_sync_all();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
     if (lane == 0) {
-      // TMA producer
-      int issued = 0;
-      for (int kb = 0; kb < g.nkb; ++kb) {
-        const int s = kb % kStages;
-        if (kb >= kStages && !mbar_wait(empty0 + 8 * s, (uint32_t)((kb / kStages) - 1) & 1u, g.err)) break;
-        mbar_expect_tx(full0 + 8 * s, 2 * kTileBytes);
-        tma_load_2d(smem_u32(sA + (size_t)s * kTileBytes), &tmA, kb * kTK, m0, full0 + 8 * s);
-        tma_load_2d(smem_u32(sB + (size_t)s * kTileBytes), &tmB, kb * kTK, n0, full0 + 8 * s);
-        ++issued;
+      // TMA producer: this CTA's A tile, and its half of the pair's B tile into both CTAs
+      // a box wholly outside the matrix (the odd last row tile, a half tile beyond n) is
+      // replaced by the last one inside: those rows and columns of C are never written
+      const int mlast = (g.m - 1) / kTM * kTM, nlast = (g.n - 1) / kHalfN * kHalfN;
+      long long it = 0;
+      bool ok = true;
+      for (int tp = cid; tp < ntp && ok; tp += ncl) {
+        const int m0 = min((2 * (tp % g.mpairs) + (int)rank) * kTM, mlast);
+        const int nb = min((tp / g.mpairs) * kTN + (int)rank * kHalfN, nlast);
+        for (int kb = 0; kb < g.nkb; ++kb, ++it) {
+          const int s = (int)(it % kStages);
+          const long long use = it / kStages;
+          if (use > 0 && !mbar_wait(empty0 + 8 * s, (uint32_t)((use - 1) & 1), g.err)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = stages + (size_t)s * kStageBytes;
+          mbar_expect_tx(full0 + 8 * s, kStageBytes);
+          tma_load_2d(smem_u32(st), &tmA, kb * kTK, m0, full0 + 8 * s);
+          tma_load_2d_pair(smem_u32(st + kABytes + (size_t)rank * (kBBytes / 2)), &tmB, kb * kTK, nb,
+                           full0 + 8 * s);
+        }
       }
-      // every issued load has landed before the CTA may leave (a consumer that gave up does
-      // not wait for them): the last phase issued on each stage, bounded (at once normally)
-      for (int kb = issued - 1; kb >= 0 && kb >= issued - kStages; --kb)
-        (void)mbar_wait(full0 + 8 * (kb % kStages), (uint32_t)(kb / kStages) & 1u, g.err);
+      // before the CTA may leave: every stage's last fill has landed and both CTAs' MMAs
+      // have released it (their commits arrive on this CTA's barriers); bounded
+      for (long long u = it - 1; u >= 0 && u >= it - kStages; --u) {
+        const int s = (int)(u % kStages);
+        (void)mbar_wait_drain(full0 + 8 * s, (uint32_t)((u / kStages) & 1), g.err);
+        (void)mbar_wait_drain(empty0 + 8 * s, (uint32_t)((u / kStages) & 1), g.err);
+      }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       // MMA issuer
-      int kb = 0;
-      for (; kb < g.nkb; ++kb) {
-        const int s = kb % kStages;
-        if (!mbar_wait(full0 + 8 * s, (uint32_t)(kb / kStages) & 1u, g.err)) break;
+      long long it = 0;
+      int t = 0;
+      bool ok = true;
+      for (int tp = cid; tp < ntp && ok; tp += ncl, ++t) {
+        const int buf = t & 1;
+        if (t >= 2 && !mbar_wait(tempty0 + 8 * buf, (uint32_t)(((t >> 1) - 1) & 1), g.err)) break;
         tc_fence_after();
-        const uint32_t a0 = smem_u32(sA + (size_t)s * kTileBytes), b0 = smem_u32(sB + (size_t)s * kTileBytes);
+        const uint32_t acc = tmem + (uint32_t)(buf * kTN);
+        for (int kb = 0; kb < g.nkb; ++kb, ++it) {
+          const int s = (int)(it % kStages);
+          if (!mbar_wait(full0 + 8 * s, (uint32_t)((it / kStages) & 1), g.err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(stages + (size_t)s * kStageBytes), b0 = a0 + kABytes;
 #pragma unroll
-        for (int kk = 0; kk < kTK / 8; ++kk)
-          mma_tf32(tmem, sw128_desc(a0 + 32u * kk), sw128_desc(b0 + 32u * kk), (kb | kk) != 0 ? 1u : 0u);
-        mma_commit(empty0 + 8 * s);
+          for (int kk = 0; kk < kTK / 8; ++kk)
+            mma_tf32(acc, sw128_desc(a0 + 32u * kk), sw128_desc(b0 + 32u * kk), (kb | kk) != 0 ? 1u : 0u);
+          mma_commit_pair(empty0 + 8 * s);
+        }
+        if (ok) mma_commit(tfull0 + 8 * buf);
       }
-      // also after a failure: the epilogue's wait then ends once every issued MMA is done
-      mma_commit(accum);
+      // every MMA issued has completed before tensor memory is freed
+      mma_commit(done);
+      (void)mbar_wait_drain(done, 0u, g.err);
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile
-    const int q = warp & 3;
-    const int row = m0 + 32 * q + lane;
-    int ok = 0;
-    if (lane == 0) ok = mbar_wait(accum, 0u, g.err) ? 1 : 0;
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (ok) {
-      tc_fence_after();
-      const bool write = (*(volatile int*)g.err == 0) && row < g.m;
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile, columns
+    // 128 h .. + 127 of the accumulator
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    int t = 0;
+    for (int tp = cid; tp < ntp; tp += ncl, ++t) {
+      const int buf = t & 1;
+      const int m0 = (2 * (tp % g.mpairs) + (int)rank) * kTM, n0 = (tp / g.mpairs) * kTN + kHalfN * h;
+      const int row = m0 + 32 * q + lane;
+      const bool rowok = row < g.m;
       const float* __restrict__ cin = g.C + row;
-#pragma unroll 1
-      for (int c0 = 0; c0 < kTN; c0 += 32) {
-        float cv[32];
+      float cv[2][32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int col = n0 + c0 + j;
-          cv[j] = (write && col < g.n) ? __ldcs(cin + (size_t)col * g.ldc) : 0.f;
+      for (int j = 0; j < 32; ++j) {
+        const int col = n0 + j;
+        cv[0][j] = (rowok && col < g.n) ? __ldcs(cin + (size_t)col * g.ldc) : 0.f;
+      }
+      int ok = 0;
+      if (lane == 0) ok = mbar_wait(tfull0 + 8 * buf, (uint32_t)((t >> 1) & 1), g.err) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      tc_fence_after();
+      const bool write = rowok && (*(volatile int*)g.err == 0);
+      const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * kTN + kHalfN * h);
+#pragma unroll
+      for (int ch = 0; ch < kHalfN / 32; ++ch) {
+        if (ch + 1 < kHalfN / 32) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = n0 + 32 * (ch + 1) + j;
+            cv[(ch + 1) & 1][j] = (rowok && col < g.n) ? __ldcs(cin + (size_t)col * g.ldc) : 0.f;
+          }
         }
         uint32_t v[32];
-        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
-        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c0 + 16), v + 16);
+        tmem_ld32(tbase + (uint32_t)(32 * ch), v);
+        if (ch + 1 == kHalfN / 32) {
+          // the accumulator is read: the MMAs of the tile after next may overwrite it
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * buf) : "memory");
+        }
         if (write) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const int col = n0 + c0 + j;
-            if (col < g.n) __stcs(g.C + (size_t)col * g.ldc + row, cv[j] - __uint_as_float(v[j]));
+            const int col = n0 + 32 * ch + j;
+            if (col < g.n) __stcs(g.C + (size_t)col * g.ldc + row, cv[ch & 1][j] - __uint_as_float(v[j]));
           }
         }
       }
@@ -225,6 +345,8 @@ __global__ void __launch_bounds__(kGemmThreads, 2)
   }
   tc_fence_before();
   __syncthreads();
+  // neither CTA leaves while its peer may still write into its shared memory
+  cluster_sync_all();
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
@@ -318,8 +440,26 @@ int32_t tc_gemm_sub(int m, int n, int k, const float* A, long long lda, const fl
     attr_err = cudaFuncSetAttribute(k_tc_gemm_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
   });
   O3G_CUDA_TRY(attr_err);
-  GemmArgs g{C, ldc, m, n, kp / kTK, err};
-  k_tc_gemm_sub<<<dim3((m + kTM - 1) / kTM, (n + kTN - 1) / kTN), kGemmThreads, kGemmSmem, st>>>(ta, tb, g);
+  const int mtiles = (m + kTM - 1) / kTM;
+  GemmArgs g{C, ldc, m, n, kp / kTK, (mtiles + 1) / 2, (n + kTN - 1) / kTN, err};
+  // persistent: as many pairs as can be resident at once (a GPC may leave an SM unpaired)
+  static std::once_flag occ;
+  static int max_pairs = 0;
+  static cudaError_t occ_err = cudaSuccess;
+  std::call_once(occ, [] {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2, 1, 1);
+    cfg.blockDim = dim3(kGemmThreads, 1, 1);
+    cfg.dynamicSmemBytes = kGemmSmem;
+    occ_err = cudaOccupancyMaxActiveClusters(&max_pairs, (const void*)k_tc_gemm_sub, &cfg);
+  });
+  O3G_CUDA_TRY(occ_err);
+  if (max_pairs < 1) {
+    set_error("tensor-core GEMM: no CTA pair can be resident");
+    return O3G_ERR_CUDA;
+  }
+  const int pairs = std::max(1, std::min(g.mpairs * g.ntiles, max_pairs));
+  k_tc_gemm_sub<<<2 * pairs, kGemmThreads, kGemmSmem, st>>>(ta, tb, g);
   note_launch();
   O3G_CUDA_TRY(cudaGetLastError());
   return O3G_OK;

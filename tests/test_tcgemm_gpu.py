@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("m,n,k,pad", [(128, 128, 32, 0), (200, 300, 128, 5), (1000, 513, 512, 3),
-                                       (129, 257, 104, 0), (3000, 2000, 512, 32), (64, 1000, 8, 1)])
+                                       (129, 257, 104, 0), (3000, 2000, 512, 32), (64, 1000, 8, 1),
+                                       (5000, 3000, 256, 2)])
 def test_tf32_update_matches_fp64(cuda, m, n, k, pad):
     import torch
     rng = np.random.default_rng(m + n + k)
