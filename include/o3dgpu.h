@@ -52,8 +52,12 @@ enum { O3G_CORE_RM = 0, O3G_CORE_WL = 1, O3G_CORE_EXP = 2, O3G_CORE_GAUSS = 3, O
  *  PLAIN       FP32 pair arithmetic and FP32 accumulation (the reference's Vc path);
  *  COMPENSATED FP32 pair arithmetic with a Newton-refined rsqrt and per-tile partial
  *              sums folded into compensated (hi, lo) accumulators;
- *  FP64        everything in double (comparator / oracle on the device). */
-enum { O3G_PREC_PLAIN = 0, O3G_PREC_COMPENSATED = 1, O3G_PREC_FP64 = 2 };
+ *  FP64        everything in double (comparator / oracle on the device);
+ *  ACCURATE    COMPENSATED sums of terms formed in double-single FP32 arithmetic: exact
+ *              separations, d^2, core factor and cross product carried as float pairs,
+ *              each velocity term rounded once (o3g_points_affect_points only, RM and
+ *              Gaussian cores; gradients as in COMPENSATED). */
+enum { O3G_PREC_PLAIN = 0, O3G_PREC_COMPENSATED = 1, O3G_PREC_FP64 = 2, O3G_PREC_ACCURATE = 3 };
 
 enum { O3G_MEM_HOST = 0, O3G_MEM_DEVICE = 1 };
 

@@ -18,7 +18,7 @@ STATUS = {
     10: "output arrays too small",
 }
 CORES = {"rm": 0, "wl": 1, "exp": 2, "gauss": 3, "v2": 4}
-PRECS = {"plain": 0, "compensated": 1, "fp64": 2}
+PRECS = {"plain": 0, "compensated": 1, "fp64": 2, "accurate": 3}
 MEM_HOST, MEM_DEVICE = 0, 1
 
 _lib = None

@@ -1,6 +1,8 @@
 // o3g_api_pair.cu -- extern "C" points_affect_points entry points (float and double).
 #include "o3g_pair_impl.cuh"
 
+#include <type_traits>
+
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -45,8 +47,9 @@ template <class I>
 static int32_t ptpt_entry(int core, int mode, int mem, int ns, const I* sx, const I* sy, const I* sz, const I* sr,
                           const I* ssx, const I* ssy, const I* ssz, int nt, const I* tx, const I* ty, const I* tz,
                           const I* tr, I* tu, I* tv, I* tw, I* const* tug, void* stream) {
-  if (core < 0 || core > 4 || mode < 0 || mode > 2 || (mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) || ns < 0 ||
-      nt < 0) {
+  const int max_mode = std::is_same<I, float>::value ? O3G_PREC_ACCURATE : O3G_PREC_FP64;
+  if (core < 0 || core > 4 || mode < 0 || mode > max_mode || (mem != O3G_MEM_HOST && mem != O3G_MEM_DEVICE) ||
+      ns < 0 || nt < 0) {
     set_error("points_affect_points: bad core/prec/mem or negative count");
     return O3G_ERR_INVALID_ARG;
   }

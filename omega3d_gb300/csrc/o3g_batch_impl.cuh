@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchArgs<T> a) {
   __shared__ float4 QB[2][5][kBlock / 2];   // staged tiles as source pairs, double-buffered
   __shared__ int s_item, s_last;
   // the Gaussian core's polynomial table, read from shared memory by the near-field pairs
-  __shared__ float gsh[C == CORE_GAUSS && std::is_same<T, float>::value ? kGaussPolyStride * kGaussPolyN : 1];
+  __shared__ __align__(16) float gsh[C == CORE_GAUSS && std::is_same<T, float>::value ? kGaussPolyStride * kGaussPolyN : 1];
   const float* gtab = nullptr;
   if constexpr (C == CORE_GAUSS && std::is_same<T, float>::value) {
     stage_gauss_table(gsh);   // visible after the first __syncthreads of the item loop

@@ -7,11 +7,12 @@
 //     as LAPACK's getrf: largest magnitude, first index on ties), panels of kNb columns:
 //       - k_panel_lu: one cooperative kernel factors the whole kNb-column panel; each
 //         block keeps its slab of rows in shared memory; per column every block publishes
-//         its local pivot candidate (value, row, the whole row) and, for the block holding
-//         the diagonal row, that row; one bounded grid barrier later every block knows the
-//         pivot and both rows to swap, so a column costs one barrier.  Each block updates
-//         the next column first, publishes its next candidate, arrives at the barrier, and
-//         runs the rest of the rank-1 update while the other blocks arrive;
+//         its pivot candidate (the whole row, and the diagonal row if it holds it) and then
+//         a tagged 64-bit key with release semantics; every block polls all keys (relaxed
+//         loads issued together, then a fence), so one round of stores and polls is the
+//         column's grid barrier and its exchange.
+//         Each block updates the next column first, publishes its next candidate, and runs
+//         the rest of the rank-1 update while the other blocks publish;
 //       - k_laswp: the panel's row interchanges applied to the other columns;
 //       - k_trsm_unit_lower: U12 = L11^-1 A12, one warp per column, L11 in shared memory;
 //       - trailing update A22 -= L21 U12 on the tensor cores (o3g_tcgemm.cu: tcgen05, TF32
@@ -23,8 +24,9 @@
 //   * or, without any factorisation, restarted GMRES -- the reference's own solver
 //     (BEM.h:182-202) -- with FP64 Krylov vectors, classical Gram-Schmidt with one
 //     reorthogonalisation, and the same FP64-accurate products (o3g_bem_solve_gmres).
-// Every grid barrier here spins at most kSpinLimit rounds, then sets an error flag that all
-// blocks check, so a fault in the barrier logic ends the kernel instead of hanging.
+// Every grid barrier and key poll here spins at most kSpinLimit rounds, then sets an error
+// flag that all blocks check, so a fault in the barrier logic ends the kernel instead of
+// hanging.
 #include "o3g_common.cuh"
 
 
@@ -133,27 +135,52 @@ struct PanelArgs {
   long long ld;
   int n, k0, jb, R;        // matrix order, first panel column, panel width, rows per block
   int* piv;                // absolute pivot row of each column
-  float* cval;             // [2][G] candidate |value|
-  int* crow;               // [2][G] candidate row
+  unsigned long long* keys;  // [2][G] tagged pivot candidates (panel_key)
   float* crows;            // [2][G][jb] candidate rows
   float* drow;             // [2][jb] diagonal rows
   int* singular;           // first singular column + 1, or 0
-  Barrier bar;
+  unsigned tag0;           // tag of column 0 of this panel (nonzero; see panel_key)
+  Barrier bar;             // error word, poll limit and the wait test's offset
 };
+
+// A block's pivot candidate for one panel column as one 64-bit word, written with release
+// semantics after the candidate row (and the diagonal row) it describes:
+//   bits 42-63  tag = (tag0 + column) mod 2^22: which launch and column the word is for;
+//   bits 10-41  |value| bits + 1 (0: no finite candidate);
+//   bits 0-9    the candidate's row offset inside the block's slab (R <= 1023).
+// The host zeroes the words before each factorisation and numbers the panels from 1, so a
+// word is never mistaken for a later column's.  Readers poll the words themselves: one
+// round of release stores and polls (relaxed loads, then one fence) serves as the grid
+// barrier and the exchange.
+__device__ __forceinline__ unsigned long long panel_key(unsigned tag, float v, int rowoff) {
+  const unsigned long long vk = v >= 0.f ? (unsigned long long)__float_as_uint(v) + 1ull : 0ull;
+  return ((unsigned long long)(tag & 0x3FFFFFu) << 42) | (vk << 10) | (unsigned long long)rowoff;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+constexpr int kMaxKeysPerLane = 8;   // up to 256 panel blocks
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 
 __device__ __forceinline__ void argmax_merge(float& v, int& i, float ov, int oi) {
   if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
 }
 
-// The block's pivot candidate for panel column jc: the block argmax of (best, bi), then
-// warp 0 publishes (|value|, row, the whole row) and warp 1 the diagonal row k0 + jc if this
-// block holds it.  Rows go out in their state after column jc - 1's elimination: in the slab
-// that update is still pending for the columns beyond jc (it runs while the grid barrier
-// fills), so those entries are updated on the fly here, with the same fmaf as the slab's.
+// The block's candidate for panel column jc: the block argmax of (best, bi), then warp 0
+// writes the whole candidate row and warp 1 the diagonal row k0 + jc if this block holds
+// it; after a block barrier thread 0 releases the key.  Rows go out in their state after
+// column jc - 1's elimination: in the slab that update is still pending for the columns
+// beyond jc (it runs while the other blocks publish), so those entries are updated on the
+// fly here, with the same fmaf as the slab's.
 __device__ __forceinline__ void panel_publish(const PanelArgs& a, const float* slab, const float* prow, int jc,
                                               bool pending, float best, int bi, float* rv, int* ri, int r0, int nr) {
   const int G = gridDim.x, b = blockIdx.x, jb = a.jb, R = a.R, par = jc & 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ unsigned long long key;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
@@ -174,32 +201,104 @@ __device__ __forceinline__ void panel_publish(const PanelArgs& a, const float* s
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
       argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
-    if (lane == 0) {
-      a.cval[par * G + b] = v;
-      a.crow[par * G + b] = i;
-    }
     if (v >= 0.f) put_row(a.crows + ((size_t)par * G + b) * jb, i - r0);
+    if (lane == 0) key = panel_key(a.tag0 + (unsigned)jc, v, v >= 0.f ? i - r0 : 0);
   } else if (warp == 1 && c >= r0 && c < r0 + nr) {
     put_row(a.drow + par * jb, c - r0);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) st_release_u64(a.keys + (size_t)par * G + b, key);
+}
+
+// Warp 0: waits (bounded) until every block's key for column j is out, then the pivot
+// (largest |value|, first row on ties; the same answer in every block), the pivot row into
+// prow and, when this block holds the pivot row, the diagonal row into dsw.  Returns the
+// pivot row (absolute), or -1 after a timeout or another block's error.
+__device__ int panel_collect(const PanelArgs& a, int j, float* prow, float* dsw, int r0, int nr) {
+  const int G = gridDim.x, jb = a.jb, par = j & 1, lane = threadIdx.x & 31;
+  const int c = a.k0 + j;
+  const unsigned tag = (a.tag0 + (unsigned)j + a.bar.extra) & 0x3FFFFFu;
+  float v = -1.f;
+  int i = 0x7fffffff, ow = -1;
+  // this lane's keys (G <= 32 kMaxKeysPerLane blocks), polled together with relaxed loads;
+  // the fence after the last poll orders the row reads below after the keys' releases
+  unsigned long long k[kMaxKeysPerLane];
+  unsigned pending = 0;
+#pragma unroll
+  for (int q = 0; q < kMaxKeysPerLane; ++q)
+    if (lane + 32 * q < G) pending |= 1u << q;
+  bool ok = true;
+  for (unsigned long long it = 0; pending; ++it) {
+#pragma unroll
+    for (int q = 0; q < kMaxKeysPerLane; ++q)
+      if (pending & (1u << q)) k[q] = ld_relaxed_u64(a.keys + (size_t)par * G + lane + 32 * q);
+#pragma unroll
+    for (int q = 0; q < kMaxKeysPerLane; ++q)
+      if ((pending & (1u << q)) && (unsigned)(k[q] >> 42) == tag) pending &= ~(1u << q);
+    if (!pending) break;
+    if ((it & 63ull) == 63ull && *(volatile int*)a.bar.err) { ok = false; break; }
+    if (it > a.bar.limit) {
+      atomicExch(a.bar.err, 1);
+      ok = false;
+      break;
+    }
+  }
+  if (__any_sync(0xffffffffu, !ok)) return -1;
+#pragma unroll
+  for (int q = 0; q < kMaxKeysPerLane; ++q) {
+    const int g = lane + 32 * q;
+    if (g >= G) break;
+    const unsigned vk = (unsigned)(k[q] >> 10);
+    if (vk != 0u) {
+      const float gv = __uint_as_float(vk - 1u);
+      const int gi = a.k0 + g * a.R + (int)(k[q] & 1023ull);
+      if (gv > v || (gv == v && gi < i)) { v = gv; i = gi; ow = g; }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+    const int oo = __shfl_xor_sync(0xffffffffu, ow, o);
+    if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; ow = oo; }
+  }
+  if (!(v >= 0.f) || i < c || i >= a.n || ow < 0) {   // no finite candidate (a NaN column): keep the row
+    i = c;
+    ow = -1;
+    v = 0.f;
+  }
+  // the rows were written before the keys were released, and every key has been seen by
+  // some lane of this warp: the fence orders this warp's reads after those observations
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  const bool mine = i >= r0 && i < r0 + nr && i != c;
+  for (int jj = lane; jj < jb; jj += 32) {
+    prow[jj] = ow >= 0 ? __ldcg(a.crows + ((size_t)par * G + ow) * jb + jj) : __ldcg(a.drow + par * jb + jj);
+    if (mine) dsw[jj] = __ldcg(a.drow + par * jb + jj);
+  }
+  if (lane == 0 && blockIdx.x == 0) {
+    a.piv[c] = i;
+    if (!(v > 0.f) && *a.singular == 0) *a.singular = c + 1;
+  }
+  return i;
 }
 
 // Partial-pivoting LU of the panel's jb columns, rows k0..n-1 spread over the blocks (R rows
-// each, kept in shared memory).  Per column: every block's candidate goes out, one grid
-// barrier, then every block finds the same pivot (largest |value|, first row on ties),
-// swaps, forms its multipliers and updates the next column first -- enough for the next
-// candidate, which is published and the barrier arrived at -- and only then updates the
-// rest of its rows, while the other blocks arrive.
+// each, kept in shared memory).  Per column: every block publishes its candidate (its key
+// last, with release semantics), then polls all blocks' keys; every block finds the same
+// pivot, swaps, forms its multipliers and updates the next column first -- enough for the
+// next candidate, which is published at once -- and only then updates the rest of its
+// rows, while the other blocks publish.
 __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
   extern __shared__ float smem[];
-  const int G = gridDim.x, b = blockIdx.x, jb = a.jb, R = a.R;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int jb = a.jb, R = a.R;
+  const int warp = threadIdx.x >> 5;
   float* slab = smem;                       // [jb][R]
   float* prow = smem + (size_t)jb * R;      // [jb] pivot row
+  float* dsw = prow + jb;                   // [jb] diagonal row, for the swap
   __shared__ float rv[kPanelThreads / 32];
   __shared__ int ri[kPanelThreads / 32];
   __shared__ int sg_row;
-  const int r0 = a.k0 + b * R;
+  const int r0 = a.k0 + blockIdx.x * R;
   const int nr = max(0, min(a.n, r0 + R) - r0);
   if (nr > 0) stage_in(slab, R, a.A + (size_t)a.k0 * a.ld + r0, a.ld, nr, jb);
   __syncthreads();
@@ -209,48 +308,20 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
     for (int r = threadIdx.x; r < nr; r += blockDim.x) argmax_merge(best, bi, fabsf(slab[r]), r0 + r);
     panel_publish(a, slab, prow, 0, false, best, bi, rv, ri, r0, nr);
   }
-  if (!grid_sync(a.bar)) return;
   for (int j = 0; j < jb; ++j) {
-    const int c = a.k0 + j, par = j & 1;
-    // warp 0: global pivot (same answer in every block) and the pivot row
+    const int c = a.k0 + j;
     if (warp == 0) {
-      float v = -1.f;
-      int i = 0x7fffffff, ow = -1;
-      for (int g = lane; g < G; g += 32) {
-        const float gv = a.cval[par * G + g];
-        const int gi = a.crow[par * G + g];
-        if (gv > v || (gv == v && gi < i)) { v = gv; i = gi; ow = g; }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, i, o);
-        const int oo = __shfl_xor_sync(0xffffffffu, ow, o);
-        if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; ow = oo; }
-      }
-      if (!(v >= 0.f) || i < c || i >= a.n || ow < 0) {   // no finite candidate (a NaN column): keep the row
-        i = c;
-        ow = -1;
-        v = 0.f;
-      }
-      for (int jj = lane; jj < jb; jj += 32)
-        prow[jj] = ow >= 0 ? a.crows[((size_t)par * G + ow) * jb + jj] : a.drow[par * jb + jj];
-      if (lane == 0) {
-        sg_row = i;
-        if (b == 0) {
-          a.piv[c] = i;
-          if (!(v > 0.f) && *a.singular == 0) *a.singular = c + 1;
-        }
-      }
+      const int pi = panel_collect(a, j, prow, dsw, r0, nr);
+      if ((threadIdx.x & 31) == 0) sg_row = pi;
     }
     __syncthreads();
     const int prow_i = sg_row;
+    if (prow_i < 0) return;
     if (prow_i != c) {
       if (c >= r0 && c < r0 + nr)
         for (int jj = threadIdx.x; jj < jb; jj += blockDim.x) slab[(size_t)jj * R + (c - r0)] = prow[jj];
       if (prow_i >= r0 && prow_i < r0 + nr)
-        for (int jj = threadIdx.x; jj < jb; jj += blockDim.x)
-          slab[(size_t)jj * R + (prow_i - r0)] = a.drow[par * jb + jj];
+        for (int jj = threadIdx.x; jj < jb; jj += blockDim.x) slab[(size_t)jj * R + (prow_i - r0)] = dsw[jj];
       __syncthreads();
     }
     // multipliers and the next column, with the next column's local argmax on the fly
@@ -270,9 +341,6 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
     }
     if (!nxt) break;
     panel_publish(a, slab, prow, j + 1, p != 0.f, best, bi, rv, ri, r0, nr);
-    __syncthreads();
-    unsigned target = 0;
-    if (threadIdx.x == 0) target = grid_arrive(a.bar);
     // the rest of the rank-1 update, eight loads in flight per thread
     if (p != 0.f) {
       for (int r = threadIdx.x; r < nr; r += blockDim.x) {
@@ -293,24 +361,67 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
         for (; jj < jb; ++jj) row[(size_t)jj * R] = fmaf(-l, prow[jj], row[(size_t)jj * R]);
       }
     }
-    if (!grid_wait(a.bar, target)) return;
+    __syncthreads();
   }
   __syncthreads();
   if (nr > 0) stage_out(a.A + (size_t)a.k0 * a.ld + r0, a.ld, slab, R, nr, jb);
 }
 
-// row interchanges p0..p1-1 (piv) applied to the columns [c0, c1) outside [s0, s1): one warp
-// per column stages the column's rows [p0, p1) in shared memory (coalesced), lane 0 applies
-// the interchanges in order there (rows below p1 are swapped in global memory), and the
-// segment is written back
+// row interchanges p0..p1-1 (piv) applied to the columns [c0, c1) outside [s0, s1).  Each
+// block first composes the interchanges into one permutation of the rows they touch (the
+// np rows [p0, p1) and the distinct pivot rows below p1): slot s holds row rowof[s], and
+// after all interchanges the value of slot perm[s] ends up in slot s.  Then one warp per
+// column gathers the touched values and scatters them permuted: two parallel passes per
+// column instead of a chain of dependent loads.
 constexpr int kSwapMax = 512;
 __global__ void __launch_bounds__(256) k_laswp(float* A, long long ld, int n, int p0, int p1, const int* piv, int c0,
                                                int c1, int s0, int s1) {
-  __shared__ float seg[8][kSwapMax];
+  __shared__ float seg[8][2 * kSwapMax];
   __shared__ int pv[kSwapMax];
+  __shared__ int slot_of[kSwapMax];     // slot of pivot row pv[e]
+  __shared__ int rowof[2 * kSwapMax];
+  __shared__ int perm[2 * kSwapMax];
+  __shared__ int nslots;
   const int np_ = p1 - p0;
   for (int e = threadIdx.x; e < np_; e += blockDim.x) pv[e] = piv[p0 + e];
   __syncthreads();
+  // the first interchange naming each pivot row below p1 (the same row can be named twice)
+  for (int e = threadIdx.x; e < np_; e += blockDim.x) {
+    const int p = pv[e];
+    int first = e;
+    if (p >= p1 && p < n)
+      for (int f = 0; f < e; ++f)
+        if (pv[f] == p) { first = f; break; }
+    slot_of[e] = first;   // provisional: the first occurrence's index
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ns = np_;
+    for (int e = 0; e < np_; ++e) rowof[e] = p0 + e;
+    for (int e = 0; e < np_; ++e) {
+      const int p = pv[e];
+      if (p < p1 || p >= n) {
+        slot_of[e] = (p >= p0 && p < p1) ? p - p0 : -1;
+      } else if (slot_of[e] == e) {
+        rowof[ns] = p;
+        slot_of[e] = ns++;
+      } else {
+        slot_of[e] = slot_of[slot_of[e]];   // the earlier occurrence's slot (already final)
+      }
+    }
+    for (int q = 0; q < ns; ++q) perm[q] = q;
+    for (int e = 0; e < np_; ++e) {
+      const int p = pv[e];
+      if (p == p0 + e || p < p0 + e || p >= n) continue;
+      const int s2 = slot_of[e];
+      const int t = perm[e];
+      perm[e] = perm[s2];
+      perm[s2] = t;
+    }
+    nslots = ns;
+  }
+  __syncthreads();
+  const int ns = nslots;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int skip = (s1 > s0) ? (s1 - s0) : 0;
   const int ncol = c1 - c0 - skip;
@@ -318,24 +429,9 @@ __global__ void __launch_bounds__(256) k_laswp(float* A, long long ld, int n, in
     int col = c0 + t;
     if (skip && col >= s0) col += skip;
     float* a = A + (size_t)col * ld;
-    for (int e = lane; e < np_; e += 32) seg[warp][e] = a[p0 + e];
+    for (int q = lane; q < ns; q += 32) seg[warp][q] = a[rowof[perm[q]]];
     __syncwarp();
-    if (lane == 0) {
-      for (int e = 0; e < np_; ++e) {
-        const int p = pv[e];
-        if (p == p0 + e || p < p0 + e || p >= n) continue;
-        const float t0 = seg[warp][e];
-        if (p < p1) {
-          seg[warp][e] = seg[warp][p - p0];
-          seg[warp][p - p0] = t0;
-        } else {
-          seg[warp][e] = a[p];
-          a[p] = t0;
-        }
-      }
-    }
-    __syncwarp();
-    for (int e = lane; e < np_; e += 32) a[p0 + e] = seg[warp][e];
+    for (int q = lane; q < ns; q += 32) a[rowof[q]] = seg[warp][q];
     __syncwarp();
   }
 }
@@ -376,33 +472,54 @@ __global__ void k_eye(float* E, int jb) {
 
 // C[:, j] = L T[:, j] for j < ncols in FP32: L jb x jb (leading dimension jb, jb <= kNb), T
 // jb x ncols (leading dimension jb), C with leading dimension ldc.  L stays in shared memory;
-// 32 columns of T at a time, thread (r, g) sums row r of 16 of them, k in order.
-constexpr int kLeftCols = 32;
+// T goes through it 64 columns at a time, transposed (k-major, rows padded to 68 floats so
+// the transposing stores spread over the banks).  Thread (tr, tc) of 16 x 16 owns rows
+// 8 tr .. 8 tr + 7 and columns 4 tc .. 4 tc + 3 of the 128 x 64 block: per k two 16-byte
+// loads of L and one of T feed 32 FMAs, summed in k order.
+constexpr int kLeftCols = 64;
+constexpr int kLeftLd = kLeftCols + 4;
 __global__ void __launch_bounds__(256) k_left_gemm(const float* __restrict__ L, int jb, const float* __restrict__ T,
                                                    int ncols, float* __restrict__ C, long long ldc) {
-  extern __shared__ float lsm[];
-  float* Ls = lsm;                   // [jb][jb]
-  float* Ts = lsm + (size_t)jb * jb; // [kLeftCols][jb]
-  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) Ls[e] = L[e];
-  const int r = threadIdx.x & (kNb - 1), g = threadIdx.x / kNb;
+  extern __shared__ float4 lsm4[];
+  float* Ls = reinterpret_cast<float*>(lsm4);   // [k][kNb], zero beyond jb
+  float* Ts = Ls + (size_t)kNb * kNb;            // [k][kLeftLd]
+  for (int e = threadIdx.x; e < kNb * kNb; e += blockDim.x) {
+    const int kk = e / kNb, r = e % kNb;
+    Ls[e] = (kk < jb && r < jb) ? L[(size_t)kk * jb + r] : 0.f;
+  }
+  const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
   for (int c0 = blockIdx.x * kLeftCols; c0 < ncols; c0 += gridDim.x * kLeftCols) {
     const int nc = min(kLeftCols, ncols - c0);
     __syncthreads();
-    for (int e = threadIdx.x; e < kLeftCols * jb; e += blockDim.x)
-      Ts[e] = (e / jb) < nc ? T[(size_t)(c0 + e / jb) * jb + e % jb] : 0.f;
+    for (int e = threadIdx.x; e < kLeftCols * jb; e += blockDim.x) {
+      const int c = e / jb, kk = e % jb;
+      Ts[(size_t)kk * kLeftLd + c] = c < nc ? T[(size_t)(c0 + c) * jb + kk] : 0.f;
+    }
     __syncthreads();
-    if (r < jb) {
-      float acc[16];
+    float acc[8][4];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] = 0.f;
-      for (int kk = 0; kk < jb; ++kk) {
-        const float l = Ls[(size_t)kk * jb + r];
+    for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] = fmaf(l, Ts[(size_t)(g * 16 + c) * jb + kk], acc[c]);
-      }
+      for (int c = 0; c < 4; ++c) acc[i][c] = 0.f;
+#pragma unroll 4
+    for (int kk = 0; kk < jb; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(Ls + (size_t)kk * kNb + 8 * tr);
+      const float4 a1 = *reinterpret_cast<const float4*>(Ls + (size_t)kk * kNb + 8 * tr + 4);
+      const float4 b = *reinterpret_cast<const float4*>(Ts + (size_t)kk * kLeftLd + 4 * tc);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
-        if (g * 16 + c < nc) C[(size_t)(c0 + g * 16 + c) * ldc + r] = acc[c];
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[i][c] = fmaf(av[i], bv[c], acc[i][c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int col = 4 * tc + c;
+      if (col < nc)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          if (8 * tr + i < jb) C[(size_t)(c0 + col) * ldc + 8 * tr + i] = acc[i][c];
     }
   }
 }
@@ -864,9 +981,9 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   O3G_CUDA_TRY(cudaFuncGetAttributes(&fa, k_panel_lu));
   const size_t max_smem = (size_t)optin - fa.sharedSizeBytes;
   O3G_CUDA_TRY(cudaFuncSetAttribute(k_panel_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
-  int G = df.num_sms;
+  int G = std::min(df.num_sms, 32 * kMaxKeysPerLane);
   int R = (n + G - 1) / G;
-  size_t smem = ((size_t)kNb * R + kNb + 32) * sizeof(float);
+  size_t smem = ((size_t)kNb * R + 2 * kNb + 32) * sizeof(float);
   if (smem > max_smem) {
     set_error("o3g_bem_factor: matrix too large for the panel kernel's shared memory");
     return O3G_ERR_INVALID_ARG;
@@ -876,15 +993,15 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
     set_error("o3g_bem_factor: panel kernel cannot be resident");
     return O3G_ERR_INVALID_ARG;
   }
-  const size_t cand = align_up(2 * (size_t)G * sizeof(float)) + align_up(2 * (size_t)G * sizeof(int)) +
+  const size_t cand = align_up(2 * (size_t)G * sizeof(unsigned long long)) +
                       align_up(2 * (size_t)G * kNb * sizeof(float)) + align_up(2 * (size_t)kNb * sizeof(float));
   O3G_TRY(bem_scratch(h, cand + align_up((size_t)kNb * kNb * 4) + align_up((size_t)kNb * n * 4) + (1 << 20)));
   Carve cv(h->scratch);
-  float* cval = cv.take<float>(2 * (size_t)G);
-  int* crow = cv.take<int>(2 * (size_t)G);
+  unsigned long long* keys = cv.take<unsigned long long>(2 * (size_t)G);
   float* crows = cv.take<float>(2 * (size_t)G * kNb);
   float* drow = cv.take<float>(2 * (size_t)kNb);
   O3G_CUDA_TRY(cudaMemsetAsync(h->flags, 0, 64 * sizeof(int), st));
+  O3G_CUDA_TRY(cudaMemsetAsync(keys, 0, 2 * (size_t)G * sizeof(unsigned long long), st));
   O3G_CUDA_TRY(cudaMemcpy2DAsync(h->LU, ld * sizeof(float), h->A, ld * sizeof(float), n * sizeof(float), n,
                                  cudaMemcpyDeviceToDevice, st));
   KernelTimer& tm = thread_timer();
@@ -916,7 +1033,7 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   // the same solve for a wide right-hand side: Linv = L11^-1 once (TRSM on the identity),
   // then B <- Linv B as an FP32 product (k_left_gemm) through a scratch copy
   float* linv = cv.take<float>((size_t)kNb * kNb);
-  const size_t lsm_bytes = ((size_t)kNb * kNb + (size_t)kLeftCols * kNb) * sizeof(float);
+  const size_t lsm_bytes = ((size_t)kNb * kNb + (size_t)kNb * kLeftLd) * sizeof(float);
   O3G_CUDA_TRY(cudaFuncSetAttribute(k_left_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm_bytes));
   float* tmp = cv.take<float>((size_t)kNb * n);
   auto trsm_wide = [&](int k0, int jb, int c0, int ncols) -> int32_t {
@@ -957,12 +1074,12 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
       }
       PanelArgs pa;
       pa.A = h->LU; pa.ld = ld; pa.n = n; pa.k0 = k0; pa.jb = jb; pa.R = r;
-      pa.piv = h->piv; pa.cval = cval; pa.crow = crow; pa.crows = crows; pa.drow = drow;
+      pa.piv = h->piv; pa.keys = keys; pa.crows = crows; pa.drow = drow;
       pa.singular = h->flags + 1;
+      pa.tag0 = (unsigned)(k0 / kNb + 1) << 7;   // panels numbered from 1: zeroed keys never match
       pa.bar = make_barrier(h->flags);
       void* args[] = {&pa};
-      const size_t sm = ((size_t)jb * r + jb + 32) * sizeof(float);
-      O3G_CUDA_TRY(zero_barrier(h->flags, st));
+      const size_t sm = ((size_t)jb * r + 2 * jb + 32) * sizeof(float);
       O3G_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_panel_lu, dim3(g), dim3(kPanelThreads), args, sm, st));
       note_launch();
       // interchanges inside the outer panel; the other columns get them once per outer panel

@@ -241,33 +241,37 @@ __device__ __forceinline__ int gauss_interval(float q) {
   return min((int)(2.0f * qq * rsqrtf(qq)), kGaussPolyLast);
 }
 
-// G(q) and D(q) by Horner's rule in t.  The table is coefficient-major (entry e of interval
-// j at e * kGaussPolyN + j), so the lanes of a warp, whatever their intervals, read each
-// entry from one cache line (or, from a shared-memory copy, from distinct banks).  Scalar
-// loads: vector loads of a row made the compiler keep all of it live, which cost the pair
-// kernel a fifth of its occupancy.  `tab`: a block's shared-memory copy of kGaussPoly
-// (stage_gauss_table), or nullptr for the global table through the read-only cache.
+// G(q) and D(q) by Horner's rule in t.  The table holds float pairs (s, o), (G_k, D_k),
+// coefficient-major (pair e2 of interval j at e2 * N + j), so the lanes of a warp, whatever
+// their intervals, read each pair from one 112-byte span (or, from a shared-memory copy,
+// from distinct banks), and the two chains advance together in packed FMAs (FFMA2: each
+// lane rounds like FFMA, so G and D are bit-identical to two scalar chains).  `tab`: a
+// block's shared-memory copy of kGaussPoly (stage_gauss_table, 8-byte aligned), or nullptr
+// for the global table through the read-only cache.
+__device__ __forceinline__ float2 gtab_ld2(const float* tab, int i2) {
+  return tab ? reinterpret_cast<const float2*>(tab)[i2] : __ldg(reinterpret_cast<const float2*>(kGaussPoly) + i2);
+}
 __device__ __forceinline__ float gtab_ld(const float* tab, int i) { return tab ? tab[i] : __ldg(kGaussPoly + i); }
 __device__ __forceinline__ void gauss_poly(float q, float& G, float& D, const float* tab = nullptr) {
   constexpr int N = kGaussPolyN;
-  const int j = gauss_interval(q);   // entry e of this interval: e * N + j
-  const float t = fmaf(q, gtab_ld(tab, j), gtab_ld(tab, N + j));
-  float g = gtab_ld(tab, 2 * N + j), d = gtab_ld(tab, 3 * N + j);
+  const int j = gauss_interval(q);   // pair e2 of this interval: e2 * N + j
+  const float2 so = gtab_ld2(tab, j);
+  const float t = fmaf(q, so.x, so.y);
+  const float2 tt = make_float2(t, t);
+  float2 gd = gtab_ld2(tab, N + j);
 #pragma unroll
-  for (int k = 1; k <= kGaussPolyDeg; ++k) {
-    g = fmaf(g, t, gtab_ld(tab, (2 + 2 * k) * N + j));
-    d = fmaf(d, t, gtab_ld(tab, (3 + 2 * k) * N + j));
-  }
-  G = g;
-  D = d;
+  for (int k = 1; k <= kGaussPolyDeg; ++k) gd = __ffma2_rn(gd, tt, gtab_ld2(tab, (1 + k) * N + j));
+  G = gd.x;
+  D = gd.y;
 }
 __device__ __forceinline__ float gauss_poly_g(float q, const float* tab = nullptr) {
   constexpr int N = kGaussPolyN;
   const int j = gauss_interval(q);
-  const float t = fmaf(q, gtab_ld(tab, j), gtab_ld(tab, N + j));
-  float g = gtab_ld(tab, 2 * N + j);
+  const float2 so = gtab_ld2(tab, j);
+  const float t = fmaf(q, so.x, so.y);
+  float g = gtab_ld(tab, 2 * (N + j));
 #pragma unroll
-  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, gtab_ld(tab, (2 + 2 * k) * N + j));
+  for (int k = 1; k <= kGaussPolyDeg; ++k) g = fmaf(g, t, gtab_ld(tab, 2 * ((1 + k) * N + j)));
   return g;
 }
 // copies the polynomial table into a block's shared array (all threads call; synchronise

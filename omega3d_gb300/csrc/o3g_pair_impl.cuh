@@ -33,8 +33,15 @@ namespace o3g {
 constexpr int kBlock = 128;  // threads per block == sources per shared tile
 constexpr int kHalf = 64;    // sources per far-field classification unit (two per tile)
 
-enum { MODE_PLAIN = 0, MODE_COMP = 1, MODE_FP64 = 2 };
+enum { MODE_PLAIN = 0, MODE_COMP = 1, MODE_FP64 = 2, MODE_DS = 3 };
 enum { CORE_SING = 5 };      // internal: singular far-field kernel (cst ignored)
+
+}  // namespace o3g
+#include "o3g_ds.cuh"
+namespace o3g {
+
+// compensated (Fast2Sum-folded) sums: the COMPENSATED and the accurate mode
+template <int MODE> struct SumComp { static constexpr bool value = (MODE == MODE_COMP || MODE == MODE_DS); };
 
 template <class T, class O> struct PairArgs {
   const V4<T>* spos;
@@ -114,6 +121,57 @@ __device__ __forceinline__ void pair_v(const V4<T>& t, const V4<T>& s, const V4<
   a[2] = fma(r3, dy * w.x - dx * w.y, a[2]);
 }
 
+// The accurate mode's pair (o3g_ds.cuh): separation, d^2, core and cross product in
+// double-single; the velocity terms go unrounded into double-single running sums (a[0..2]
+// and their low parts a[15..17]); the gradient terms from the core rounded to float.  The
+// radii come raw: s.w of the strength record and t.w of the target record.
+template <int C, bool HAVE_TR>
+__device__ __forceinline__ void pair_g_ds(const V4<float>& t, const V4<float>& s, const V4<float>& w, float* a) {
+  const dsf dx = ds_two_sum(t.x, -s.x);
+  const dsf dy = ds_two_sum(t.y, -s.y);
+  const dsf dz = ds_two_sum(t.z, -s.z);
+  const dsf d2 = ds_add(ds_add(ds_sq(dx), ds_sq(dy)), ds_sq(dz));
+  dsf r3;
+  float bbb;
+  core_ds<C, true>(d2, w.w, HAVE_TR ? t.w : 0.f, r3, bbb);
+  const dsf cx = ds_cross(dz, w.y, dy, w.z);
+  const dsf cy = ds_cross(dx, w.z, dz, w.x);
+  const dsf cz = ds_cross(dy, w.x, dx, w.y);
+  ds_accum(a[0], a[15], r3, cx);
+  ds_accum(a[1], a[16], r3, cy);
+  ds_accum(a[2], a[17], r3, cz);
+  const float bx = __fmul_rn(__fadd_rn(cx.h, cx.l), bbb);
+  const float by = __fmul_rn(__fadd_rn(cy.h, cy.l), bbb);
+  const float bz = __fmul_rn(__fadd_rn(cz.h, cz.l), bbb);
+  const float ex = dx.h, ey = dy.h, ez = dz.h;
+  a[3] = fmaf(ex, bx, a[3]);
+  a[4] = fmaf(ex, by, a[4]);
+  a[5] = fmaf(ex, bz, a[5]);
+  a[6] = fmaf(ey, bx, a[6]);
+  a[7] = fmaf(ey, by, a[7]);
+  a[8] = fmaf(ey, bz, a[8]);
+  a[9] = fmaf(ez, bx, a[9]);
+  a[10] = fmaf(ez, by, a[10]);
+  a[11] = fmaf(ez, bz, a[11]);
+  const float r3f = ds_round(r3);
+  a[12] = fmaf(r3f, w.x, a[12]);
+  a[13] = fmaf(r3f, w.y, a[13]);
+  a[14] = fmaf(r3f, w.z, a[14]);
+}
+template <int C, bool HAVE_TR>
+__device__ __forceinline__ void pair_v_ds(const V4<float>& t, const V4<float>& s, const V4<float>& w, float* a) {
+  const dsf dx = ds_two_sum(t.x, -s.x);
+  const dsf dy = ds_two_sum(t.y, -s.y);
+  const dsf dz = ds_two_sum(t.z, -s.z);
+  const dsf d2 = ds_add(ds_add(ds_sq(dx), ds_sq(dy)), ds_sq(dz));
+  dsf r3;
+  float bbb;
+  core_ds<C, false>(d2, w.w, HAVE_TR ? t.w : 0.f, r3, bbb);
+  ds_accum(a[0], a[3], r3, ds_cross(dz, w.y, dy, w.z));
+  ds_accum(a[1], a[4], r3, ds_cross(dx, w.z, dz, w.x));
+  ds_accum(a[2], a[5], r3, ds_cross(dy, w.x, dx, w.y));
+}
+
 // a[12..14] -> antisymmetric gradient terms: tvx += sz r3, twx -= sy r3, tuy -= sz r3,
 // twy += sx r3, tuz += sy r3, tvz -= sx r3 (Kernels.h:185-191)
 template <class T>
@@ -133,7 +191,8 @@ template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, int NA, i
 __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, const V4<T>* tp, T (*acc)[NA],
                                            float (*hi)[NH], float (*lo)[NH], const float* gtab = nullptr) {
   constexpr bool ACC = (MODE == MODE_COMP);
-  constexpr int FOLD = ACC ? 16 : NS;
+  constexpr bool SUMC = SumComp<MODE>::value;
+  constexpr int FOLD = SUMC ? 16 : NS;
 #pragma unroll 1
   for (int j0 = 0; j0 < NS; j0 += FOLD) {
 #pragma unroll 4
@@ -142,23 +201,41 @@ __device__ __forceinline__ void sweep_tile(const V4<T>* sp, const V4<T>* sw, con
       const V4<T> w = sw[j];
 #pragma unroll
       for (int k = 0; k < TPT; ++k) {
-        if (GRADS) pair_g<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k], gtab);
-        else       pair_v<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k], gtab);
+        if constexpr (MODE == MODE_DS) {
+          if (GRADS) pair_g_ds<C, HAVE_TR>(tp[k], s, w, acc[k]);
+          else       pair_v_ds<C, HAVE_TR>(tp[k], s, w, acc[k]);
+        } else {
+          if (GRADS) pair_g<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k], gtab);
+          else       pair_v<C, ACC, HAVE_TR, T>(tp[k], s, w, acc[k], gtab);
+        }
       }
     }
-    if (ACC) {
+    if (SUMC) {
 #pragma unroll
       for (int k = 0; k < TPT; ++k) {
         if (GRADS) fold_grads(acc[k]);
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           float s, e;
-          // Fast2Sum: exact error term when |hi| >= |partial|, the usual case once a few
-          // folds have accumulated; otherwise that fold loses at most its own rounding
-          s = hi[k][c] + (float)acc[k][c];
-          e = (float)acc[k][c] - (s - hi[k][c]);
+          if constexpr (MODE == MODE_DS) {
+            // two-sum: exact in any order (a running sum that passes near zero while the
+            // partials are large would otherwise lose the partial's rounding)
+            const dsf t2 = ds_two_sum(hi[k][c], (float)acc[k][c]);
+            s = t2.h;
+            e = t2.l;
+          } else {
+            // Fast2Sum: exact error term when |hi| >= |partial|, the usual case once a few
+            // folds have accumulated; otherwise that fold loses at most its own rounding
+            s = hi[k][c] + (float)acc[k][c];
+            e = (float)acc[k][c] - (s - hi[k][c]);
+          }
           hi[k][c] = s;
           lo[k][c] += e;
+        }
+        if constexpr (MODE == MODE_DS) {
+          // the velocity sums' low parts (the last three accumulators)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) lo[k][c] += (float)acc[k][NA - 3 + c];
         }
 #pragma unroll
         for (int c = 0; c < NA; ++c) acc[k][c] = T(0);
@@ -317,7 +394,7 @@ template <> struct FarRule<CORE_EXP> {
 // bounding box and largest core parameter of the real targets of one warp (all lanes get
 // the result), widened by a relative 1e-6 so float rounding never makes it too small;
 // returns false when the warp holds no real target
-template <int TPT, class T>
+template <int TPT, class T, bool RAW_R = false>
 __device__ __forceinline__ bool warp_box(const V4<T>* tp, const bool* real, float* blo, float* bhi, float& bw) {
   float lo3[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi3[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mw = 0.f;
   bool any = false;
@@ -327,7 +404,8 @@ __device__ __forceinline__ bool warp_box(const V4<T>* tp, const bool* real, floa
       const float v[3] = {(float)tp[k].x, (float)tp[k].y, (float)tp[k].z};
 #pragma unroll
       for (int d = 0; d < 3; ++d) { lo3[d] = fminf(lo3[d], v[d]); hi3[d] = fmaxf(hi3[d], v[d]); }
-      mw = fmaxf(mw, (float)tp[k].w);
+      // the core parameter r^2; the accurate mode's targets carry r itself
+      mw = fmaxf(mw, RAW_R ? (float)tp[k].w * (float)tp[k].w : (float)tp[k].w);
       any = true;
     }
   }
@@ -360,9 +438,10 @@ __device__ __forceinline__ bool half_is_far(const float4& slo, const float4& shi
 
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
 __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
-  constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr bool ACC = SumComp<MODE>::value;
   constexpr bool CLASSIFY = (C == CORE_GAUSS || C == CORE_EXP);
-  constexpr int NA = GRADS ? 15 : 3;   // accumulators during the sweep
+  // accumulators during the sweep (the accurate mode adds the velocity sums' low parts)
+  constexpr int NA = (GRADS ? 15 : 3) + (MODE == MODE_DS ? 3 : 0);
   constexpr int NC = GRADS ? 12 : 3;   // output components
   constexpr int NH = ACC ? NC : 1;
   __shared__ V4<T> sp[kBlock];
@@ -383,7 +462,7 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PairArgs<T, O> a) {
 
   float blo[3] = {0.f, 0.f, 0.f}, bhi[3] = {0.f, 0.f, 0.f}, bw = 0.f;
   bool live = true;
-  if (CLASSIFY) live = warp_box<TPT, T>(tp, real, blo, bhi, bw);
+  if (CLASSIFY) live = warp_box<TPT, T, MODE == MODE_DS>(tp, real, blo, bhi, bw);
 
   T acc[TPT][NA];
 #pragma unroll
@@ -464,7 +543,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_f(const PairArgs<float, float> 
   constexpr int NH = ACC ? NC : 1;
   __shared__ float4 QB[2][5][kBlock / 2];
   // the Gaussian core's polynomial table, read from shared memory by the near-field pairs
-  __shared__ float gsh[C == CORE_GAUSS ? kGaussPolyStride * kGaussPolyN : 1];
+  __shared__ __align__(16) float gsh[C == CORE_GAUSS ? kGaussPolyStride * kGaussPolyN : 1];
   const float* gtab = nullptr;
   if constexpr (C == CORE_GAUSS) {
     stage_gauss_table(gsh);   // visible after the first tile's __syncthreads
@@ -612,7 +691,9 @@ __global__ void k_pack_src(int n, int n_pad, const I* __restrict__ x, const I* _
 }
 
 // SoA -> packed targets; r == nullptr means field points (core parameter 0)
-template <int C, class I, class T>
+// RAW_R: w = r itself (the accurate mode forms r^2 exactly in the pair), else the core
+// parameter
+template <int C, class I, class T, bool RAW_R = false>
 __global__ void k_pack_tgt(int n, int n_pad, const I* __restrict__ x, const I* __restrict__ y,
                            const I* __restrict__ z, const I* __restrict__ r, const uint32_t* __restrict__ perm,
                            V4<T>* tpos) {
@@ -622,7 +703,7 @@ __global__ void k_pack_tgt(int n, int n_pad, const I* __restrict__ x, const I* _
   if (i < n) {
     const int j = perm ? (int)perm[i] : i;
     p.x = (T)x[j]; p.y = (T)y[j]; p.z = (T)z[j];
-    p.w = r ? core_param<C, T>((T)r[j]) : T(0);
+    p.w = r ? (RAW_R ? (T)r[j] : core_param<C, T>((T)r[j])) : T(0);
   } else {
     p.x = T(0); p.y = T(0); p.z = T(0); p.w = T(0);
   }
@@ -684,7 +765,7 @@ struct PairPlan {
 template <int C, int MODE, bool GRADS, bool HAVE_TR, int TPT, class T, class O>
 struct PairKernel {
   static const void* ptr() {
-    if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value)
+    if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value && MODE != MODE_DS)
       return (const void*)&k_pair_f<C, MODE, GRADS, HAVE_TR, TPT>;
     else
       return (const void*)&k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O>;
@@ -716,8 +797,11 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
                           int nt, const I* tx, const I* ty, const I* tz, const I* tr,
                           OutPtrs<O> out, bool same, cudaStream_t st, size_t* ws_bytes_needed, char* ws_base) {
   constexpr int NC = GRADS ? 12 : 3;
-  constexpr bool ACC = (MODE == MODE_COMP);
+  constexpr bool ACC = SumComp<MODE>::value;
   constexpr bool SORT = (C == CORE_GAUSS || C == CORE_EXP);
+  // the accurate mode squares the radii itself: targets carry r (the sources' r is in the
+  // strength record); same-set calls then pack the targets separately
+  if (MODE == MODE_DS && tr) same = false;
   DeviceFacts df;
   O3G_TRY(device_facts(&df));
   int nb = 0;
@@ -759,7 +843,8 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   k_pack_src<C, I, T><<<(nsp + 255) / 256, 256, 0, st>>>(ns, nsp, sx, sy, sz, sr, ssx, ssy, ssz, sperm, spos, sstr);
   note_launch();
   if (!same) {
-    k_pack_tgt<C, I, T><<<(pl.nt_pad + 255) / 256, 256, 0, st>>>(nt, pl.nt_pad, tx, ty, tz, tr, tperm, tpos);
+    k_pack_tgt<C, I, T, MODE == MODE_DS><<<(pl.nt_pad + 255) / 256, 256, 0, st>>>(nt, pl.nt_pad, tx, ty, tz, tr,
+                                                                                tperm, tpos);
     note_launch();
   }
   if (SORT) {
@@ -774,7 +859,7 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   dim3 grid(pl.tblocks, pl.nsplit);
   KernelTimer& tm = thread_timer();
   tm.begin(st);
-  if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value)
+  if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value && MODE != MODE_DS)
     k_pair_f<C, MODE, GRADS, HAVE_TR, TPT><<<grid, kBlock, 0, st>>>(a);
   else
     k_pair<C, MODE, GRADS, HAVE_TR, TPT, T, O><<<grid, kBlock, 0, st>>>(a);
@@ -830,6 +915,19 @@ int32_t ptpt_core_d(const PtPtCall& c, const double* sx, const double* sy, const
       }                                                                                                      \
       if (htr) return run_points_points<CORE, MODE_COMP, false, true, 2, float>(O3G_PTPT_ARGS);              \
       return run_points_points<CORE, MODE_COMP, false, false, 2, float>(O3G_PTPT_ARGS);                      \
+    }                                                                                                        \
+    if (c.mode == MODE_DS) {                                                                                 \
+      if constexpr (CORE == CORE_RM || CORE == CORE_GAUSS) {                                                 \
+        if (c.grads) {                                                                                       \
+          if (htr) return run_points_points<CORE, MODE_DS, true, true, 1, float>(O3G_PTPT_ARGS);             \
+          return run_points_points<CORE, MODE_DS, true, false, 1, float>(O3G_PTPT_ARGS);                     \
+        }                                                                                                    \
+        if (htr) return run_points_points<CORE, MODE_DS, false, true, 1, float>(O3G_PTPT_ARGS);              \
+        return run_points_points<CORE, MODE_DS, false, false, 1, float>(O3G_PTPT_ARGS);                      \
+      } else {                                                                                               \
+        set_error("points_affect_points: precision ACCURATE supports the RM and Gaussian cores");            \
+        return O3G_ERR_INVALID_ARG;                                                                          \
+      }                                                                                                      \
     }                                                                                                        \
     if (c.grads) {                                                                                           \
       if (htr) return run_points_points<CORE, MODE_FP64, true, true, 1, double>(O3G_PTPT_ARGS);              \

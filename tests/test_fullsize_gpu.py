@@ -95,6 +95,10 @@ def test_precision_cloud_full_size(cuda):
     assert rel_err(uc[:, sub], u64)[0] <= 1e-5 and rel_err(gc[:, sub], g64)[0] <= 1e-5
     up, gp = _sums(x, s, r, "gauss", "plain")
     assert linf_err(up[:, sub], u64) <= 2e-5 and linf_err(gp[:, sub], g64) <= 2e-5
+    # the accurate mode: every sampled target within 1e-6
+    ua, ga = _sums(x, s, r, "gauss", "accurate")
+    assert rel_err(ua[:, sub], u64)[0] <= 1e-6 and linf_err(ua[:, sub], u64) <= 1e-7
+    assert rel_err(ga[:, sub], g64)[0] <= 1e-5 and linf_err(ga[:, sub], g64) <= 1e-6
     # the FP64 path on the device agrees with the oracle's FP64 sums
     tq = G.Points(_t(x[:, sub].astype(np.float64)), None, _t(r[sub].astype(np.float64)))
     G.points_affect_points(G.Points(_t(x.astype(np.float64)), _t(s.astype(np.float64)), _t(r.astype(np.float64))),
