@@ -483,17 +483,37 @@ __global__ void __launch_bounds__(256) k_left_gemm(const float* __restrict__ L, 
   extern __shared__ float4 lsm4[];
   float* Ls = reinterpret_cast<float*>(lsm4);   // [k][kNb], zero beyond jb
   float* Ts = Ls + (size_t)kNb * kNb;            // [k][kLeftLd]
-  for (int e = threadIdx.x; e < kNb * kNb; e += blockDim.x) {
-    const int kk = e / kNb, r = e % kNb;
-    Ls[e] = (kk < jb && r < jb) ? L[(size_t)kk * jb + r] : 0.f;
+  // staging: 8 loads in flight per thread before their stores (a load -> store loop waits
+  // out the full memory latency at every element)
+  for (int e0 = threadIdx.x; e0 < kNb * kNb; e0 += 8 * blockDim.x) {
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * blockDim.x, kk = e / kNb, r = e % kNb;
+      v[q] = (e < kNb * kNb && kk < jb && r < jb) ? __ldg(L + (size_t)kk * jb + r) : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * blockDim.x;
+      if (e < kNb * kNb) Ls[e] = v[q];
+    }
   }
   const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
   for (int c0 = blockIdx.x * kLeftCols; c0 < ncols; c0 += gridDim.x * kLeftCols) {
     const int nc = min(kLeftCols, ncols - c0);
     __syncthreads();
-    for (int e = threadIdx.x; e < kLeftCols * jb; e += blockDim.x) {
-      const int c = e / jb, kk = e % jb;
-      Ts[(size_t)kk * kLeftLd + c] = c < nc ? T[(size_t)(c0 + c) * jb + kk] : 0.f;
+    for (int e0 = threadIdx.x; e0 < kLeftCols * jb; e0 += 8 * blockDim.x) {
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * blockDim.x, c = e / jb, kk = e % jb;
+        v[q] = (e < kLeftCols * jb && c < nc) ? __ldg(T + (size_t)(c0 + c) * jb + kk) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * blockDim.x, c = e / jb, kk = e % jb;
+        if (e < kLeftCols * jb) Ts[(size_t)kk * kLeftLd + c] = v[q];
+      }
     }
     __syncthreads();
     float acc[8][4];

@@ -20,10 +20,12 @@
 //   * each slab is 4 MMAs of 128 x 256 x 8 (kind::tf32) into 256 TMEM columns; the 512
 //     columns hold two accumulators, so the epilogue of one tile overlaps the MMAs of the
 //     next;
-//   * the epilogue reads the accumulator row by row (TMEM lane = row of the tile) and
-//     subtracts it from C with coalesced streaming loads and stores, 32 columns at a time,
-//     the next chunk's loads in flight while the current one is stored; the first chunk
-//     is loaded before the accumulator is waited for.
+//   * the epilogue moves C through shared memory by TMA in chunks of 128 rows x 16 columns
+//     (two buffers for each 128-column half): a chunk is loaded two chunks ahead, each
+//     thread subtracts its row of the accumulator (TMEM lane = row of the tile) in place,
+//     and the chunk is stored back by TMA; the first chunks load while the MMAs run.
+//     C's base and leading dimension must be 16-byte aligned (the BEM's are; the public
+//     entry point copies any other C through an aligned scratch).
 // Every mbarrier wait is bounded: after kWaitLimit polls it sets the error word, every
 // other wait then gives up at once, the CTA still drains its copies, leaves the cluster
 // together with its peer and frees its tensor memory, and the host returns
@@ -49,8 +51,15 @@ constexpr int kGemmThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kTmemCols = 2 * kTN;                    // two accumulators
 constexpr unsigned long long kWaitLimit = 1ull << 26;
 constexpr unsigned long long kDrainLimit = 1ull << 22;
-constexpr int kNumBars = 2 * kStages + 5;                  // full, empty, tmem full[2], tmem empty[2], done
-constexpr size_t kGemmSmem = 1024 + (size_t)kStages * kStageBytes + 8 * kNumBars + 16;
+// C goes through shared memory in chunks of 128 rows x 16 columns (8 KB), two buffers for
+// each 128-column half of the tile
+constexpr int kCCols = 16;
+constexpr int kCBytes = kTM * kCCols * 4;
+constexpr int kChunks = kHalfN / kCCols;                   // chunks per half tile
+// full[kStages], empty[kStages], tmem full[2], tmem empty[2], done, C full[2 halves][2 buffers]
+constexpr int kNumBars = 2 * kStages + 5 + 4;
+constexpr size_t kGemmSmem = 1024 + (size_t)kStages * kStageBytes + 4 * (size_t)kCBytes + 8 * kNumBars + 16;
+static_assert(kGemmSmem <= 232448, "shared memory per CTA");
 
 // instruction descriptor of tcgen05.mma kind::tf32: D format F32 (bits 4-5 = 1), A and B
 // TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22,
@@ -172,28 +181,41 @@ __device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 32 consecutive TMEM columns of this warp's 32 lanes: thread t gets lane (base lane + t)
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
+// 16 consecutive TMEM columns of this warp's 32 lanes: thread t gets lane (base lane + t)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
-        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
-        "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
-        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
       : "r"(taddr)
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int c0, int c1, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1), "r"(src)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void named_bar(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
 
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
-    k_tc_gemm_sub(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+    k_tc_gemm_sub(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const __grid_constant__ CUtensorMap tmC, GemmArgs g) {
   extern __shared__ unsigned char smem_raw[];
   // the 128-byte swizzle repeats every 1024 bytes: stage buffers start on 1024-byte
   // boundaries; both CTAs of a pair have the same layout (multicast writes by offset)
   const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023;
   unsigned char* stages = reinterpret_cast<unsigned char*>(base);             // [kStages][A 16 KB | B 32 KB]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(stages + (size_t)kStages * kStageBytes);
+  unsigned char* cbuf = stages + (size_t)kStages * kStageBytes;                // [2 halves][2][8 KB]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(cbuf + 4 * (size_t)kCBytes);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kNumBars);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_rank();
@@ -202,6 +224,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages);
   const uint32_t tfull0 = smem_u32(bars + 2 * kStages), tempty0 = smem_u32(bars + 2 * kStages + 2);
   const uint32_t done = smem_u32(bars + 2 * kStages + 4);
+  const uint32_t cfull0 = smem_u32(bars + 2 * kStages + 5);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -213,6 +236,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
       mbar_init(tempty0 + 8 * b, kEpiWarps);
     }
     mbar_init(done, 1);
+    for (int b = 0; b < 4; ++b) mbar_init(cfull0 + 8 * b, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -293,54 +317,87 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
       (void)mbar_wait_drain(done, 0u, g.err);
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile, columns
-    // 128 h .. + 127 of the accumulator
+    // epilogue: group h (warps 2 + 4h .. 5 + 4h) owns columns 128 h .. + 127 of every tile;
+    // warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile.  C moves by TMA in
+    // chunks of 128 rows x 16 columns through two shared-memory buffers per group: the
+    // group's leader loads chunk c + 2 while chunk c is combined, and stores each chunk
+    // once the group has written it back.  Every warp runs the same sequence of named
+    // barriers whatever happens (a failed wait only turns its work off), so none waits
+    // for a warp that left.
     const int q = warp & 3, h = (warp - 2) >> 2;
-    int t = 0;
-    for (int tp = cid; tp < ntp; tp += ncl, ++t) {
-      const int buf = t & 1;
-      const int m0 = (2 * (tp % g.mpairs) + (int)rank) * kTM, n0 = (tp / g.mpairs) * kTN + kHalfN * h;
-      const int row = m0 + 32 * q + lane;
-      const bool rowok = row < g.m;
-      const float* __restrict__ cin = g.C + row;
-      float cv[2][32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int col = n0 + j;
-        cv[0][j] = (rowok && col < g.n) ? __ldcs(cin + (size_t)col * g.ldc) : 0.f;
+    const bool leader = (warp == 2 + 4 * h) && lane == 0;
+    const uint32_t cf0 = cfull0 + 16 * (uint32_t)h;
+    unsigned char* cb = cbuf + (size_t)h * 2 * kCBytes;
+    const int mine = cid < ntp ? (ntp - cid + ncl - 1) / ncl : 0;   // tiles of this CTA
+    const long long nchunks = (long long)mine * kChunks;
+    // chunk cc: its box (x = first row, y = first column), and whether it holds part of C
+    auto chunk_box = [&](long long cc, int& x, int& y) -> bool {
+      const int tp = cid + (int)(cc / kChunks) * ncl;
+      x = (2 * (tp % g.mpairs) + (int)rank) * kTM;
+      y = (tp / g.mpairs) * kTN + kHalfN * h + kCCols * (int)(cc % kChunks);
+      return x < g.m && y < g.n;
+    };
+    long long issued = 0;
+    auto issue_load = [&](long long cc) {
+      int x, y;
+      const uint32_t bar = cf0 + 8 * (uint32_t)(cc & 1);
+      if (chunk_box(cc, x, y)) {
+        mbar_expect_tx(bar, kCBytes);
+        tma_load_2d(smem_u32(cb + (size_t)(cc & 1) * kCBytes), &tmC, x, y, bar);
+      } else {
+        mbar_arrive(bar);   // nothing of C there: the phase completes at once
       }
-      int ok = 0;
-      if (lane == 0) ok = mbar_wait(tfull0 + 8 * buf, (uint32_t)((t >> 1) & 1), g.err) ? 1 : 0;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) break;
+      issued = cc + 1;
+    };
+    if (leader) {
+      if (nchunks > 0) issue_load(0);
+      if (nchunks > 1) issue_load(1);
+    }
+    bool ok = true;
+    long long cc = 0, waited = 0;   // chunks seen so far; chunks whose load this warp saw land
+    for (int t = 0; t < mine; ++t) {
+      const int buf = t & 1;
+      ok = ok && __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * buf, (uint32_t)((t >> 1) & 1), g.err));
       tc_fence_after();
-      const bool write = rowok && (*(volatile int*)g.err == 0);
       const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * kTN + kHalfN * h);
-#pragma unroll
-      for (int ch = 0; ch < kHalfN / 32; ++ch) {
-        if (ch + 1 < kHalfN / 32) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int col = n0 + 32 * (ch + 1) + j;
-            cv[(ch + 1) & 1][j] = (rowok && col < g.n) ? __ldcs(cin + (size_t)col * g.ldc) : 0.f;
-          }
-        }
-        uint32_t v[32];
-        tmem_ld32(tbase + (uint32_t)(32 * ch), v);
-        if (ch + 1 == kHalfN / 32) {
+      for (int ch = 0; ch < kChunks; ++ch, ++cc) {
+        const int b = (int)(cc & 1);
+        ok = ok && __all_sync(0xffffffffu, mbar_wait(cf0 + 8 * b, (uint32_t)((cc >> 1) & 1), g.err));
+        if (ok) waited = cc + 1;
+        uint32_t v[16];
+        tmem_ld16(tbase + (uint32_t)(kCCols * ch), v);
+        if (ch + 1 == kChunks) {
           // the accumulator is read: the MMAs of the tile after next may overwrite it
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * buf) : "memory");
+          if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
         }
-        if (write) {
+        float* cs = reinterpret_cast<float*>(cb + (size_t)b * kCBytes);   // [16 columns][128 rows]
+        if (ok) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int col = n0 + 32 * ch + j;
-            if (col < g.n) __stcs(g.C + (size_t)col * g.ldc + row, cv[ch & 1][j] - __uint_as_float(v[j]));
+          for (int j = 0; j < kCCols; ++j) {
+            float* e = cs + j * kTM + 32 * q + lane;
+            *e = *e - __uint_as_float(v[j]);
           }
         }
+        // the writes above reach the TMA store (async proxy) after the group's barrier
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        named_bar(1 + h, 128);
+        if (leader) {
+          int x, y;
+          if (ok && chunk_box(cc, x, y) && *(volatile int*)g.err == 0) tma_store_2d(&tmC, x, y, smem_u32(cs));
+          // the buffer is free once the store has read it: then chunk cc + 2 goes in
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          if (ok && cc + 2 < nchunks) issue_load(cc + 2);
+        }
       }
+    }
+    if (leader) {
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      // loads issued but not seen to land (after a failed wait): they land before the CTA
+      // leaves; bounded
+      for (long long u = waited; u < issued; ++u)
+        (void)mbar_wait_drain(cf0 + 8 * (uint32_t)(u & 1), (uint32_t)((u >> 1) & 1), g.err);
     }
   }
   tc_fence_before();
@@ -393,22 +450,28 @@ int32_t encode_fn(EncodeTiled* out) {
   return O3G_OK;
 }
 
+bool aligned16(const float* base, long long stride) {
+  return !(reinterpret_cast<uintptr_t>(base) & 15u) && !((stride * 4) & 15);
+}
+
 // a 2-D FP32 tensor map: `inner` contiguous elements per line, `outer` lines `stride`
-// elements apart, boxes of 32 x 128 with the 128-byte swizzle; reads outside are zeros
-int32_t make_map(CUtensorMap* map, const float* base, long long inner, long long outer, long long stride) {
+// elements apart; operand boxes are 32 x 128 with the 128-byte swizzle (the default), C's
+// 128 x 16 unswizzled; reads outside are zeros, writes outside are dropped
+int32_t make_map(CUtensorMap* map, const float* base, long long inner, long long outer, long long stride,
+                 int box_inner = kTK, int box_outer = kTM, bool swizzle = true) {
   EncodeTiled enc;
   O3G_TRY(encode_fn(&enc));
-  if ((reinterpret_cast<uintptr_t>(base) & 15u) || ((stride * 4) & 15) || inner <= 0 || outer <= 0) {
+  if (!aligned16(base, stride) || inner <= 0 || outer <= 0) {
     set_error("tensor-core GEMM: operand not 16-byte aligned");
     return O3G_ERR_INVALID_ARG;
   }
   const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
   const cuuint64_t strides[1] = {(cuuint64_t)(stride * 4)};
-  const cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
+  const cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     char msg[96];
     std::snprintf(msg, sizeof(msg), "tensor-core GEMM: cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -431,9 +494,14 @@ int32_t tc_gemm_sub(int m, int n, int k, const float* A, long long lda, const fl
   const int kp = (k + kTK - 1) / kTK * kTK;
   k_transpose_pad<<<dim3((m + 31) / 32, kp / 32), dim3(32, 8), 0, st>>>(A, lda, m, k, kp, at);
   note_launch();
-  CUtensorMap ta, tb;
+  if (!aligned16(C, ldc)) {
+    set_error("tensor-core GEMM: C not 16-byte aligned (base and leading dimension)");
+    return O3G_ERR_INVALID_ARG;
+  }
+  CUtensorMap ta, tb, tc;
   O3G_TRY(make_map(&ta, at, kp, m, kp));
   O3G_TRY(make_map(&tb, B, k, n, ldb));
+  O3G_TRY(make_map(&tc, C, m, n, ldc, kTM, kCCols, false));
   static std::once_flag attr;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(attr, [] {
@@ -459,7 +527,7 @@ int32_t tc_gemm_sub(int m, int n, int k, const float* A, long long lda, const fl
     return O3G_ERR_CUDA;
   }
   const int pairs = std::max(1, std::min(g.mpairs * g.ntiles, max_pairs));
-  k_tc_gemm_sub<<<2 * pairs, kGemmThreads, kGemmSmem, st>>>(ta, tb, g);
+  k_tc_gemm_sub<<<2 * pairs, kGemmThreads, kGemmSmem, st>>>(ta, tb, tc, g);
   note_launch();
   O3G_CUDA_TRY(cudaGetLastError());
   return O3G_OK;
@@ -481,11 +549,23 @@ extern "C" int32_t o3g_gemm_tf32_sub(int32_t m, int32_t n, int32_t k, const floa
   cudaStream_t st = (cudaStream_t)stream;
   Workspace* ws = nullptr;
   const size_t at_bytes = align_up(tc_gemm_scratch_floats(m, k) * sizeof(float));
-  O3G_TRY(workspace_get(st, at_bytes + 256, &ws));
+  // the epilogue moves C by TMA, which wants a 16-byte aligned base and leading dimension:
+  // any other C goes through an aligned copy
+  const bool direct = aligned16(C, ldc);
+  const long long cld = direct ? ldc : (m + 3) / 4 * 4;
+  const size_t c_bytes = direct ? 0 : align_up((size_t)cld * n * sizeof(float));
+  O3G_TRY(workspace_get(st, at_bytes + c_bytes + 256, &ws));
   float* at = reinterpret_cast<float*>(ws->base);
-  int* err = reinterpret_cast<int*>(ws->base + at_bytes);
+  float* cw = direct ? C : reinterpret_cast<float*>(ws->base + at_bytes);
+  int* err = reinterpret_cast<int*>(ws->base + at_bytes + c_bytes);
   O3G_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
-  O3G_TRY(tc_gemm_sub(m, n, k, A, lda, B, ldb, C, ldc, at, err, st));
+  if (!direct)
+    O3G_CUDA_TRY(cudaMemcpy2DAsync(cw, cld * sizeof(float), C, ldc * sizeof(float), (size_t)m * sizeof(float), n,
+                                   cudaMemcpyDeviceToDevice, st));
+  O3G_TRY(tc_gemm_sub(m, n, k, A, lda, B, ldb, cw, cld, at, err, st));
+  if (!direct)
+    O3G_CUDA_TRY(cudaMemcpy2DAsync(C, ldc * sizeof(float), cw, cld * sizeof(float), (size_t)m * sizeof(float), n,
+                                   cudaMemcpyDeviceToDevice, st));
   int herr = 0;
   O3G_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
   O3G_CUDA_TRY(cudaStreamSynchronize(st));
