@@ -136,22 +136,23 @@ struct PanelArgs {
   int n, k0, jb, R;        // matrix order, first panel column, panel width, rows per block
   int* piv;                // absolute pivot row of each column
   unsigned long long* keys;  // [2][G] tagged pivot candidates (panel_key)
-  float* crows;            // [2][G][jb] candidate rows
-  float* drow;             // [2][jb] diagonal rows
+  unsigned long long* crows; // [2][G][jb] candidate rows, tagged words (panel_word)
+  unsigned long long* drow;  // [2][jb] diagonal rows, tagged words
   int* singular;           // first singular column + 1, or 0
   unsigned tag0;           // tag of column 0 of this panel (nonzero; see panel_key)
   Barrier bar;             // error word, poll limit and the wait test's offset
 };
 
-// A block's pivot candidate for one panel column as one 64-bit word, written with release
-// semantics after the candidate row (and the diagonal row) it describes:
+// A block's pivot candidate for one panel column as one 64-bit word:
 //   bits 42-63  tag = (tag0 + column) mod 2^22: which launch and column the word is for;
 //   bits 10-41  |value| bits + 1 (0: no finite candidate);
 //   bits 0-9    the candidate's row offset inside the block's slab (R <= 1023).
-// The host zeroes the words before each factorisation and numbers the panels from 1, so a
-// word is never mistaken for a later column's.  Readers poll the words themselves: one
-// round of release stores and polls (relaxed loads, then one fence) serves as the grid
-// barrier and the exchange.
+// The rows themselves travel as 64-bit words too (panel_word): the value's bits and the
+// full 32-bit tag.  Every word names its column, so no store needs to be ordered before
+// another: readers poll the keys, then read the winner's row and re-read any word whose
+// tag is not yet the column's.  One round of relaxed stores and polls is the grid barrier
+// and the exchange.  The host zeroes keys and rows before each factorisation and numbers
+// the panels from 1, so no word is ever mistaken for a later column's.
 __device__ __forceinline__ unsigned long long panel_key(unsigned tag, float v, int rowoff) {
   const unsigned long long vk = v >= 0.f ? (unsigned long long)__float_as_uint(v) + 1ull : 0ull;
   return ((unsigned long long)(tag & 0x3FFFFFu) << 42) | (vk << 10) | (unsigned long long)rowoff;
@@ -162,8 +163,11 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   return v;
 }
 constexpr int kMaxKeysPerLane = 8;   // up to 256 panel blocks
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long panel_word(unsigned tag, float v) {
+  return ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
 }
 
 __device__ __forceinline__ void argmax_merge(float& v, int& i, float ov, int oi) {
@@ -171,43 +175,55 @@ __device__ __forceinline__ void argmax_merge(float& v, int& i, float ov, int oi)
 }
 
 // The block's candidate for panel column jc: the block argmax of (best, bi), then warp 0
-// writes the whole candidate row and warp 1 the diagonal row k0 + jc if this block holds
-// it; after a block barrier thread 0 releases the key.  Rows go out in their state after
-// column jc - 1's elimination: in the slab that update is still pending for the columns
-// beyond jc (it runs while the other blocks publish), so those entries are updated on the
-// fly here, with the same fmaf as the slab's.
-__device__ __forceinline__ void panel_publish(const PanelArgs& a, const float* slab, const float* prow, int jc,
-                                              bool pending, float best, int bi, float* rv, int* ri, int r0, int nr) {
+// writes the whole candidate row and its key, and warp 1 the diagonal row k0 + jc if this
+// block holds it; no barrier after (every word is tagged).  Rows go out in their state
+// after column jc - 1's elimination: in the slab that update is still pending for the
+// columns beyond jc, so warps 0 and 1 apply it to their row here (the same fmaf as the
+// rest of the slab) and write it back; the other rows get it in the caller's loop, which
+// skips the two returned rows (-1: none).
+__device__ __forceinline__ void panel_publish(const PanelArgs& a, float* slab, const float* prow, int jc,
+                                              bool pending, float best, int bi, float* rv, int* ri, int r0, int nr,
+                                              int& done_cand, int& done_diag) {
   const int G = gridDim.x, b = blockIdx.x, jb = a.jb, R = a.R, par = jc & 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __shared__ unsigned long long key;
+  const unsigned tag = a.tag0 + (unsigned)jc;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
   if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
   __syncthreads();
+  // the block's candidate, found by every warp alike
+  float v = lane < kPanelThreads / 32 ? rv[lane] : -1.f;
+  int i = lane < kPanelThreads / 32 ? ri[lane] : 0x7fffffff;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
   const int c = a.k0 + jc;
-  auto put_row = [&](float* dst, int rr) {
+  const bool has_cand = v >= 0.f;
+  const bool has_diag = c >= r0 && c < r0 + nr;
+  done_cand = has_cand ? i - r0 : -1;
+  done_diag = (has_diag && !(has_cand && i == c)) ? c - r0 : -1;
+  // one warp per published row: the update applied and written back, the words out to
+  // dst (and to dst2 when the candidate is the diagonal row itself)
+  auto put_row = [&](unsigned long long* dst, unsigned long long* dst2, int rr) {
     const float l = pending ? slab[(size_t)(jc - 1) * R + rr] : 0.f;
     for (int jj = lane; jj < jb; jj += 32) {
-      float v = slab[(size_t)jj * R + rr];
-      if (pending && jj > jc) v = fmaf(-l, prow[jj], v);
-      dst[jj] = v;
+      float x = slab[(size_t)jj * R + rr];
+      if (pending && jj > jc) {
+        x = fmaf(-l, prow[jj], x);
+        slab[(size_t)jj * R + rr] = x;
+      }
+      st_relaxed_u64(dst + jj, panel_word(tag, x));
+      if (dst2) st_relaxed_u64(dst2 + jj, panel_word(tag, x));
     }
   };
   if (warp == 0) {
-    float v = lane < kPanelThreads / 32 ? rv[lane] : -1.f;
-    int i = lane < kPanelThreads / 32 ? ri[lane] : 0x7fffffff;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-      argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
-    if (v >= 0.f) put_row(a.crows + ((size_t)par * G + b) * jb, i - r0);
-    if (lane == 0) key = panel_key(a.tag0 + (unsigned)jc, v, v >= 0.f ? i - r0 : 0);
-  } else if (warp == 1 && c >= r0 && c < r0 + nr) {
-    put_row(a.drow + par * jb, c - r0);
+    if (has_cand)
+      put_row(a.crows + ((size_t)par * G + b) * jb, (has_diag && i == c) ? a.drow + par * jb : nullptr, i - r0);
+    if (lane == 0) st_relaxed_u64(a.keys + (size_t)par * G + b, panel_key(tag, v, has_cand ? i - r0 : 0));
+  } else if (warp == 1 && done_diag >= 0) {
+    put_row(a.drow + par * jb, nullptr, c - r0);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) st_release_u64(a.keys + (size_t)par * G + b, key);
 }
 
 // Warp 0: waits (bounded) until every block's key for column j is out, then the pivot
@@ -220,8 +236,7 @@ __device__ int panel_collect(const PanelArgs& a, int j, float* prow, float* dsw,
   const unsigned tag = (a.tag0 + (unsigned)j + a.bar.extra) & 0x3FFFFFu;
   float v = -1.f;
   int i = 0x7fffffff, ow = -1;
-  // this lane's keys (G <= 32 kMaxKeysPerLane blocks), polled together with relaxed loads;
-  // the fence after the last poll orders the row reads below after the keys' releases
+  // this lane's keys (G <= 32 kMaxKeysPerLane blocks), polled together with relaxed loads
   unsigned long long k[kMaxKeysPerLane];
   unsigned pending = 0;
 #pragma unroll
@@ -267,14 +282,40 @@ __device__ int panel_collect(const PanelArgs& a, int j, float* prow, float* dsw,
     ow = -1;
     v = 0.f;
   }
-  // the rows were written before the keys were released, and every key has been seen by
-  // some lane of this warp: the fence orders this warp's reads after those observations
-  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  // the rows: every word read until it carries this column's tag (the stores are not
+  // ordered with the key's); bounded like the keys
+  const unsigned wtag = a.tag0 + (unsigned)j + a.bar.extra;
   const bool mine = i >= r0 && i < r0 + nr && i != c;
-  for (int jj = lane; jj < jb; jj += 32) {
-    prow[jj] = ow >= 0 ? __ldcg(a.crows + ((size_t)par * G + ow) * jb + jj) : __ldcg(a.drow + par * jb + jj);
-    if (mine) dsw[jj] = __ldcg(a.drow + par * jb + jj);
-  }
+  const unsigned long long* src = ow >= 0 ? a.crows + ((size_t)par * G + ow) * jb : a.drow + par * jb;
+  // this lane's words of a row (jb <= 128: at most 4), loaded together, stale ones again
+  auto fetch = [&](const unsigned long long* p, float* out) -> bool {
+    constexpr int kW = kNb / 32;
+    unsigned long long w[kW];
+    unsigned stale = 0;
+#pragma unroll
+    for (int q = 0; q < kW; ++q)
+      if (lane + 32 * q < jb) stale |= 1u << q;
+    for (unsigned long long it = 0; stale; ++it) {
+#pragma unroll
+      for (int q = 0; q < kW; ++q)
+        if (stale & (1u << q)) w[q] = ld_relaxed_u64(p + lane + 32 * q);
+#pragma unroll
+      for (int q = 0; q < kW; ++q)
+        if ((stale & (1u << q)) && (unsigned)(w[q] >> 32) == wtag) stale &= ~(1u << q);
+      if (!stale) break;
+      if (it > a.bar.limit || ((it & 63ull) == 63ull && *(volatile int*)a.bar.err)) {
+        atomicExch(a.bar.err, 1);
+        return false;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kW; ++q)
+      if (lane + 32 * q < jb) out[lane + 32 * q] = __uint_as_float((unsigned)w[q]);
+    return true;
+  };
+  ok = fetch(src, prow);
+  if (ok && mine) ok = fetch(a.drow + par * jb, dsw);
+  if (__any_sync(0xffffffffu, !ok)) return -1;
   if (lane == 0 && blockIdx.x == 0) {
     a.piv[c] = i;
     if (!(v > 0.f) && *a.singular == 0) *a.singular = c + 1;
@@ -306,7 +347,8 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
     float best = -1.f;
     int bi = 0x7fffffff;
     for (int r = threadIdx.x; r < nr; r += blockDim.x) argmax_merge(best, bi, fabsf(slab[r]), r0 + r);
-    panel_publish(a, slab, prow, 0, false, best, bi, rv, ri, r0, nr);
+    int dc, dd;
+    panel_publish(a, slab, prow, 0, false, best, bi, rv, ri, r0, nr, dc, dd);
   }
   for (int j = 0; j < jb; ++j) {
     const int c = a.k0 + j;
@@ -340,11 +382,13 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
       if (nxt) argmax_merge(best, bi, fabsf(row[(size_t)(j + 1) * R]), r0 + r);
     }
     if (!nxt) break;
-    panel_publish(a, slab, prow, j + 1, p != 0.f, best, bi, rv, ri, r0, nr);
-    // the rest of the rank-1 update, eight loads in flight per thread
+    int done_cand, done_diag;
+    panel_publish(a, slab, prow, j + 1, p != 0.f, best, bi, rv, ri, r0, nr, done_cand, done_diag);
+    // the rest of the rank-1 update (the published rows have theirs), eight loads in flight
+    // per thread
     if (p != 0.f) {
       for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-        if (r0 + r <= c) continue;
+        if (r0 + r <= c || r == done_cand || r == done_diag) continue;
         float* row = slab + r;
         const float l = row[(size_t)j * R];
         int jj = j + 2;
@@ -1013,15 +1057,16 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
     set_error("o3g_bem_factor: panel kernel cannot be resident");
     return O3G_ERR_INVALID_ARG;
   }
-  const size_t cand = align_up(2 * (size_t)G * sizeof(unsigned long long)) +
-                      align_up(2 * (size_t)G * kNb * sizeof(float)) + align_up(2 * (size_t)kNb * sizeof(float));
+  const size_t cand = align_up((2 * (size_t)G + 2 * (size_t)G * kNb + 2 * (size_t)kNb) * sizeof(unsigned long long));
   O3G_TRY(bem_scratch(h, cand + align_up((size_t)kNb * kNb * 4) + align_up((size_t)kNb * n * 4) + (1 << 20)));
   Carve cv(h->scratch);
-  unsigned long long* keys = cv.take<unsigned long long>(2 * (size_t)G);
-  float* crows = cv.take<float>(2 * (size_t)G * kNb);
-  float* drow = cv.take<float>(2 * (size_t)kNb);
+  // keys and tagged rows back to back, zeroed together once per factorisation
+  const size_t xwords = 2 * (size_t)G + 2 * (size_t)G * kNb + 2 * (size_t)kNb;
+  unsigned long long* keys = cv.take<unsigned long long>(xwords);
+  unsigned long long* crows = keys + 2 * (size_t)G;
+  unsigned long long* drow = crows + 2 * (size_t)G * kNb;
   O3G_CUDA_TRY(cudaMemsetAsync(h->flags, 0, 64 * sizeof(int), st));
-  O3G_CUDA_TRY(cudaMemsetAsync(keys, 0, 2 * (size_t)G * sizeof(unsigned long long), st));
+  O3G_CUDA_TRY(cudaMemsetAsync(keys, 0, xwords * sizeof(unsigned long long), st));
   O3G_CUDA_TRY(cudaMemcpy2DAsync(h->LU, ld * sizeof(float), h->A, ld * sizeof(float), n * sizeof(float), n,
                                  cudaMemcpyDeviceToDevice, st));
   KernelTimer& tm = thread_timer();
