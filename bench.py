@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--skip-ring", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-splitmerge", action="store_true")
-    ap.add_argument("--only", choices=["bem", "ring", "batch", "coupled", "splitmerge"], default=None,
+    ap.add_argument("--only", choices=["bem", "ring", "batch", "coupled", "splitmerge", "gemm"], default=None,
                     help="run one workload section alone and print its results (profiling)")
     ap.add_argument("--coupled-steps", type=int, default=2,
                     help="coupled sphere + 1M-particle Ralston steps to time (0 skips; 20 = the full run)")
@@ -312,9 +312,10 @@ def measured_peaks():
         return {}
 
 
-def bench_tc_gemm(G, torch, m=8192, n=8192, k=512, reps=5):
+def bench_tc_gemm(G, torch, m=40448, n=40448, k=512, reps=5):
     """The LU's trailing update on its own: C -= A B (o3g_gemm_tf32_sub, tcgen05 kind::tf32)
-    at the size of a mid-factorisation update, k = 512 (the outer panel).  Achieved TFLOP/s
+    at the size of the first big update of the n = 40,960 factorisation (m = n = 40,448,
+    k = 512, the outer panel).  Achieved TFLOP/s
     (2 m n k per call) against the TF32 tensor roof, taken as half the measured dense bf16
     rate (MEASURED_PEAKS.json bf16_tflops; TF32 runs at half the bf16 rate), and the HBM
     traffic the update cannot avoid (C read and written once, A and B read) against the
@@ -819,7 +820,10 @@ def run_ours(args):
               "ring": lambda: bench_ring(args, G, torch, W),
               "batch": lambda: bench_batch(args, G, torch, W, flush),
               "coupled": lambda: bench_coupled(args, G, torch, W),
-              "splitmerge": lambda: bench_splitmerge(args, G, torch, W)}[args.only]
+              "splitmerge": lambda: bench_splitmerge(args, G, torch, W),
+              "gemm": lambda: {"%dx%dx%d" % mnk: bench_tc_gemm(G, torch, *mnk)
+                               for mnk in ((8192, 8192, 512), (16384, 16384, 512), (40448, 40448, 512),
+                                           (40448, 384, 128))}}[args.only]
         res = fn()
         torch.cuda.synchronize()
         if rank == 0:
@@ -998,7 +1002,7 @@ def run_ours(args):
                          "kernel_ms": statistics.median(acc_kms),
                          "over_plain": plain_step / statistics.median(acc_ms),
                          "path": "double-single pair terms (exact separation, d^2, core, cross product), "
-                                 "velocity terms rounded once, compensated sums",
+                                 "velocity in double-single running sums, two-sum folds",
                          "error_vs_fp64": fp64["errors_vs_fp64"]["accurate"] if fp64 else None},
             "rm_core_same_cloud": rm,
             "fp64_same_gpu": fp64 and {"value": fp64["value"], "unit": UNIT, "targets": fp64["targets"],

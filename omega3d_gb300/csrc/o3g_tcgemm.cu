@@ -55,10 +55,12 @@ constexpr unsigned long long kDrainLimit = 1ull << 22;
 // each 128-column half of the tile
 constexpr int kCCols = 16;
 constexpr int kCBytes = kTM * kCCols * 4;
+constexpr int kCBufs = 2;                                  // buffers per half: loads kCBufs chunks ahead
 constexpr int kChunks = kHalfN / kCCols;                   // chunks per half tile
 // full[kStages], empty[kStages], tmem full[2], tmem empty[2], done, C full[2 halves][2 buffers]
-constexpr int kNumBars = 2 * kStages + 5 + 4;
-constexpr size_t kGemmSmem = 1024 + (size_t)kStages * kStageBytes + 4 * (size_t)kCBytes + 8 * kNumBars + 16;
+constexpr int kNumBars = 2 * kStages + 5 + 2 * kCBufs;
+constexpr size_t kGemmSmem =
+    1024 + (size_t)kStages * kStageBytes + 2 * (size_t)kCBufs * kCBytes + 8 * kNumBars + 16;
 static_assert(kGemmSmem <= 232448, "shared memory per CTA");
 
 // instruction descriptor of tcgen05.mma kind::tf32: D format F32 (bits 4-5 = 1), A and B
@@ -215,7 +217,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
   const uintptr_t base = (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023;
   unsigned char* stages = reinterpret_cast<unsigned char*>(base);             // [kStages][A 16 KB | B 32 KB]
   unsigned char* cbuf = stages + (size_t)kStages * kStageBytes;                // [2 halves][2][8 KB]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(cbuf + 4 * (size_t)kCBytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(cbuf + 2 * (size_t)kCBufs * kCBytes);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kNumBars);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_rank();
@@ -236,7 +238,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
       mbar_init(tempty0 + 8 * b, kEpiWarps);
     }
     mbar_init(done, 1);
-    for (int b = 0; b < 4; ++b) mbar_init(cfull0 + 8 * b, 1);
+    for (int b = 0; b < 2 * kCBufs; ++b) mbar_init(cfull0 + 8 * b, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -319,15 +321,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
   } else {
     // epilogue: group h (warps 2 + 4h .. 5 + 4h) owns columns 128 h .. + 127 of every tile;
     // warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile.  C moves by TMA in
-    // chunks of 128 rows x 16 columns through two shared-memory buffers per group: the
-    // group's leader loads chunk c + 2 while chunk c is combined, and stores each chunk
-    // once the group has written it back.  Every warp runs the same sequence of named
+    // chunks of 128 rows x 16 columns through kCBufs shared-memory buffers per group: the
+    // group's leader loads chunk c + kCBufs while chunk c is combined, and stores each
+    // chunk once the group has written it back.  Every warp runs the same sequence of named
     // barriers whatever happens (a failed wait only turns its work off), so none waits
     // for a warp that left.
     const int q = warp & 3, h = (warp - 2) >> 2;
     const bool leader = (warp == 2 + 4 * h) && lane == 0;
-    const uint32_t cf0 = cfull0 + 16 * (uint32_t)h;
-    unsigned char* cb = cbuf + (size_t)h * 2 * kCBytes;
+    const uint32_t cf0 = cfull0 + 8 * kCBufs * (uint32_t)h;
+    unsigned char* cb = cbuf + (size_t)h * kCBufs * kCBytes;
     const int mine = cid < ntp ? (ntp - cid + ncl - 1) / ncl : 0;   // tiles of this CTA
     const long long nchunks = (long long)mine * kChunks;
     // chunk cc: its box (x = first row, y = first column), and whether it holds part of C
@@ -340,19 +342,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
     long long issued = 0;
     auto issue_load = [&](long long cc) {
       int x, y;
-      const uint32_t bar = cf0 + 8 * (uint32_t)(cc & 1);
+      const uint32_t bar = cf0 + 8 * (uint32_t)(cc % kCBufs);
       if (chunk_box(cc, x, y)) {
         mbar_expect_tx(bar, kCBytes);
-        tma_load_2d(smem_u32(cb + (size_t)(cc & 1) * kCBytes), &tmC, x, y, bar);
+        tma_load_2d(smem_u32(cb + (size_t)(cc % kCBufs) * kCBytes), &tmC, x, y, bar);
       } else {
         mbar_arrive(bar);   // nothing of C there: the phase completes at once
       }
       issued = cc + 1;
     };
-    if (leader) {
-      if (nchunks > 0) issue_load(0);
-      if (nchunks > 1) issue_load(1);
-    }
+    if (leader)
+      for (long long u = 0; u < kCBufs && u < nchunks; ++u) issue_load(u);
     bool ok = true;
     long long cc = 0, waited = 0;   // chunks seen so far; chunks whose load this warp saw land
     for (int t = 0; t < mine; ++t) {
@@ -361,8 +361,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
       tc_fence_after();
       const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * kTN + kHalfN * h);
       for (int ch = 0; ch < kChunks; ++ch, ++cc) {
-        const int b = (int)(cc & 1);
-        ok = ok && __all_sync(0xffffffffu, mbar_wait(cf0 + 8 * b, (uint32_t)((cc >> 1) & 1), g.err));
+        const int b = (int)(cc % kCBufs);
+        ok = ok && __all_sync(0xffffffffu, mbar_wait(cf0 + 8 * b, (uint32_t)((cc / kCBufs) & 1), g.err));
         if (ok) waited = cc + 1;
         uint32_t v[16];
         tmem_ld16(tbase + (uint32_t)(kCCols * ch), v);
@@ -386,9 +386,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
         if (leader) {
           int x, y;
           if (ok && chunk_box(cc, x, y) && *(volatile int*)g.err == 0) tma_store_2d(&tmC, x, y, smem_u32(cs));
-          // the buffer is free once the store has read it: then chunk cc + 2 goes in
+          // the buffer is free once the store has read it: then chunk cc + kCBufs goes in
           asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          if (ok && cc + 2 < nchunks) issue_load(cc + 2);
+          if (ok && cc + kCBufs < nchunks) issue_load(cc + kCBufs);
         }
       }
     }
@@ -397,7 +397,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
       // loads issued but not seen to land (after a failed wait): they land before the CTA
       // leaves; bounded
       for (long long u = waited; u < issued; ++u)
-        (void)mbar_wait_drain(cf0 + 8 * (uint32_t)(u & 1), (uint32_t)((u >> 1) & 1), g.err);
+        (void)mbar_wait_drain(cf0 + 8 * (uint32_t)(u % kCBufs), (uint32_t)((u / kCBufs) & 1), g.err);
     }
   }
   tc_fence_before();
