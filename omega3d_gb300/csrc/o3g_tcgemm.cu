@@ -20,12 +20,12 @@
 //   * each slab is 4 MMAs of 128 x 256 x 8 (kind::tf32) into 256 TMEM columns; the 512
 //     columns hold two accumulators, so the epilogue of one tile overlaps the MMAs of the
 //     next;
-//   * the epilogue moves C through shared memory by TMA in chunks of 128 rows x 16 columns
-//     (two buffers for each 128-column half): a chunk is loaded two chunks ahead, each
-//     thread subtracts its row of the accumulator (TMEM lane = row of the tile) in place,
-//     and the chunk is stored back by TMA; the first chunks load while the MMAs run.
-//     C's base and leading dimension must be 16-byte aligned (the BEM's are; the public
-//     entry point copies any other C through an aligned scratch).
+//   * the epilogue never loads C: each thread writes its row of -acc (TMEM lane = row of
+//     the tile) into a shared-memory chunk of 128 rows x 16 columns (two buffers for each
+//     128-column half), and a TMA reduce-add (cp.reduce.async.bulk.tensor .add) adds the
+//     chunk into C in L2, rounded once: the same value as C - acc.  C's base and leading
+//     dimension must be 16-byte aligned (the BEM's are; the public entry point copies any
+//     other C through an aligned scratch).
 // Every mbarrier wait is bounded: after kWaitLimit polls it sets the error word, every
 // other wait then gives up at once, the CTA still drains its copies, leaves the cluster
 // together with its peer and frees its tensor memory, and the host returns
@@ -51,14 +51,15 @@ constexpr int kGemmThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kTmemCols = 2 * kTN;                    // two accumulators
 constexpr unsigned long long kWaitLimit = 1ull << 26;
 constexpr unsigned long long kDrainLimit = 1ull << 22;
-// C goes through shared memory in chunks of 128 rows x 16 columns (8 KB), two buffers for
-// each 128-column half of the tile
+// -acc goes through shared memory in chunks of 128 rows x 16 columns (8 KB), kCBufs buffers
+// for each 128-column half of the tile, into C by TMA reduce-add
 constexpr int kCCols = 16;
 constexpr int kCBytes = kTM * kCCols * 4;
-constexpr int kCBufs = 2;                                  // buffers per half: loads kCBufs chunks ahead
+constexpr int kCBufs = 2;                                  // buffers per half (>= 2)
+static_assert(kCBufs >= 2, "a reduce reads one buffer while the next is written");
 constexpr int kChunks = kHalfN / kCCols;                   // chunks per half tile
-// full[kStages], empty[kStages], tmem full[2], tmem empty[2], done, C full[2 halves][2 buffers]
-constexpr int kNumBars = 2 * kStages + 5 + 2 * kCBufs;
+// full[kStages], empty[kStages], tmem full[2], tmem empty[2], done
+constexpr int kNumBars = 2 * kStages + 5;
 constexpr size_t kGemmSmem =
     1024 + (size_t)kStages * kStageBytes + 2 * (size_t)kCBufs * kCBytes + 8 * kNumBars + 16;
 static_assert(kGemmSmem <= 232448, "shared memory per CTA");
@@ -194,13 +195,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int c0, int c1, uint32_t src) {
-  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
-                   reinterpret_cast<uint64_t>(map)),
-               "r"(c0), "r"(c1), "r"(src)
-               : "memory");
-  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -226,7 +220,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages);
   const uint32_t tfull0 = smem_u32(bars + 2 * kStages), tempty0 = smem_u32(bars + 2 * kStages + 2);
   const uint32_t done = smem_u32(bars + 2 * kStages + 4);
-  const uint32_t cfull0 = smem_u32(bars + 2 * kStages + 5);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -238,7 +231,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
       mbar_init(tempty0 + 8 * b, kEpiWarps);
     }
     mbar_init(done, 1);
-    for (int b = 0; b < 2 * kCBufs; ++b) mbar_init(cfull0 + 8 * b, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -320,50 +312,27 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
     }
   } else {
     // epilogue: group h (warps 2 + 4h .. 5 + 4h) owns columns 128 h .. + 127 of every tile;
-    // warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile.  C moves by TMA in
-    // chunks of 128 rows x 16 columns through kCBufs shared-memory buffers per group: the
-    // group's leader loads chunk c + kCBufs while chunk c is combined, and stores each
-    // chunk once the group has written it back.  Every warp runs the same sequence of named
-    // barriers whatever happens (a failed wait only turns its work off), so none waits
-    // for a warp that left.
+    // warp w reads TMEM lanes 32 (w % 4) .. + 31 = rows of the tile.  C is never loaded
+    // here: each chunk of 128 rows x 16 columns of -acc goes to a shared-memory buffer and
+    // is added into C by a TMA reduce (cp.reduce.async.bulk.tensor .add: L2 performs
+    // C + (-acc), rounded once, the value C - acc).  Every warp runs the same sequence of
+    // named barriers whatever happens (a failed wait only turns its work off), so none
+    // waits for a warp that left.
     const int q = warp & 3, h = (warp - 2) >> 2;
     const bool leader = (warp == 2 + 4 * h) && lane == 0;
-    const uint32_t cf0 = cfull0 + 8 * kCBufs * (uint32_t)h;
     unsigned char* cb = cbuf + (size_t)h * kCBufs * kCBytes;
     const int mine = cid < ntp ? (ntp - cid + ncl - 1) / ncl : 0;   // tiles of this CTA
-    const long long nchunks = (long long)mine * kChunks;
-    // chunk cc: its box (x = first row, y = first column), and whether it holds part of C
-    auto chunk_box = [&](long long cc, int& x, int& y) -> bool {
-      const int tp = cid + (int)(cc / kChunks) * ncl;
-      x = (2 * (tp % g.mpairs) + (int)rank) * kTM;
-      y = (tp / g.mpairs) * kTN + kHalfN * h + kCCols * (int)(cc % kChunks);
-      return x < g.m && y < g.n;
-    };
-    long long issued = 0;
-    auto issue_load = [&](long long cc) {
-      int x, y;
-      const uint32_t bar = cf0 + 8 * (uint32_t)(cc % kCBufs);
-      if (chunk_box(cc, x, y)) {
-        mbar_expect_tx(bar, kCBytes);
-        tma_load_2d(smem_u32(cb + (size_t)(cc % kCBufs) * kCBytes), &tmC, x, y, bar);
-      } else {
-        mbar_arrive(bar);   // nothing of C there: the phase completes at once
-      }
-      issued = cc + 1;
-    };
-    if (leader)
-      for (long long u = 0; u < kCBufs && u < nchunks; ++u) issue_load(u);
     bool ok = true;
-    long long cc = 0, waited = 0;   // chunks seen so far; chunks whose load this warp saw land
+    long long cc = 0;
     for (int t = 0; t < mine; ++t) {
       const int buf = t & 1;
+      const int tp = cid + t * ncl;
+      const int x = (2 * (tp % g.mpairs) + (int)rank) * kTM;
+      const int y0 = (tp / g.mpairs) * kTN + kHalfN * h;
       ok = ok && __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * buf, (uint32_t)((t >> 1) & 1), g.err));
       tc_fence_after();
       const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * kTN + kHalfN * h);
       for (int ch = 0; ch < kChunks; ++ch, ++cc) {
-        const int b = (int)(cc % kCBufs);
-        ok = ok && __all_sync(0xffffffffu, mbar_wait(cf0 + 8 * b, (uint32_t)((cc / kCBufs) & 1), g.err));
-        if (ok) waited = cc + 1;
         uint32_t v[16];
         tmem_ld16(tbase + (uint32_t)(kCCols * ch), v);
         if (ch + 1 == kChunks) {
@@ -372,33 +341,27 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads)
           __syncwarp();
           if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
         }
-        float* cs = reinterpret_cast<float*>(cb + (size_t)b * kCBytes);   // [16 columns][128 rows]
-        if (ok) {
+        // the buffer's previous reduce finished reading it before the last group barrier
+        float* cs = reinterpret_cast<float*>(cb + (size_t)(cc % kCBufs) * kCBytes);   // [16 columns][128 rows]
 #pragma unroll
-          for (int j = 0; j < kCCols; ++j) {
-            float* e = cs + j * kTM + 32 * q + lane;
-            *e = *e - __uint_as_float(v[j]);
-          }
-        }
-        // the writes above reach the TMA store (async proxy) after the group's barrier
+        for (int j = 0; j < kCCols; ++j) cs[j * kTM + 32 * q + lane] = -__uint_as_float(v[j]);
+        // the writes above reach the TMA reduce (async proxy) after the group's barrier;
+        // before it, the leader lets the reduces issued so far finish reading their buffers
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (leader) asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(kCBufs - 2) : "memory");
         named_bar(1 + h, 128);
-        if (leader) {
-          int x, y;
-          if (ok && chunk_box(cc, x, y) && *(volatile int*)g.err == 0) tma_store_2d(&tmC, x, y, smem_u32(cs));
-          // the buffer is free once the store has read it: then chunk cc + kCBufs goes in
-          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          if (ok && cc + kCBufs < nchunks) issue_load(cc + kCBufs);
+        const int y = y0 + kCCols * ch;
+        if (leader && ok && x < g.m && y < g.n && *(volatile int*)g.err == 0) {
+          asm volatile(
+              "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                  reinterpret_cast<uint64_t>(&tmC)),
+              "r"(x), "r"(y), "r"(smem_u32(cs))
+              : "memory");
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
         }
       }
     }
-    if (leader) {
-      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-      // loads issued but not seen to land (after a failed wait): they land before the CTA
-      // leaves; bounded
-      for (long long u = waited; u < issued; ++u)
-        (void)mbar_wait_drain(cf0 + 8 * (uint32_t)(u % kCBufs), (uint32_t)((u / kCBufs) & 1), g.err);
-    }
+    if (leader) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
