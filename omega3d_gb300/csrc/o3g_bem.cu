@@ -38,6 +38,7 @@
 namespace o3g {
 
 constexpr int kNb = 128;              // panel width
+constexpr int kNbOuter = 512;         // outer panel width: k of the big trailing updates
 constexpr int kPanelThreads = 512;
 constexpr int kSolveThreads = 1024;
 constexpr unsigned long long kSpinLimit = 1ull << 25;
@@ -417,16 +418,19 @@ __global__ void __launch_bounds__(kPanelThreads) k_panel_lu(PanelArgs a) {
 // after all interchanges the value of slot perm[s] ends up in slot s.  Then one warp per
 // column gathers the touched values and scatters them permuted: two parallel passes per
 // column instead of a chain of dependent loads.
-constexpr int kSwapMax = 512;
+// dynamic shared memory for np interchanges: 8 warps' segments of 2 np floats, then pv,
+// slot_of (np ints each), rowof, perm (2 np ints each)
+inline size_t laswp_smem(int np_) { return (size_t)(8 * 2 * np_ + 6 * np_) * 4; }
 __global__ void __launch_bounds__(256) k_laswp(float* A, long long ld, int n, int p0, int p1, const int* piv, int c0,
                                                int c1, int s0, int s1) {
-  __shared__ float seg[8][2 * kSwapMax];
-  __shared__ int pv[kSwapMax];
-  __shared__ int slot_of[kSwapMax];     // slot of pivot row pv[e]
-  __shared__ int rowof[2 * kSwapMax];
-  __shared__ int perm[2 * kSwapMax];
-  __shared__ int nslots;
+  extern __shared__ float lsw[];
   const int np_ = p1 - p0;
+  float* segs = lsw;                                         // [8][2 np]
+  int* pv = reinterpret_cast<int*>(segs + 8 * 2 * np_);      // [np]
+  int* slot_of = pv + np_;                                   // [np]: slot of pivot row pv[e]
+  int* rowof = slot_of + np_;                                // [2 np]
+  int* perm = rowof + 2 * np_;                               // [2 np]
+  __shared__ int nslots;
   for (int e = threadIdx.x; e < np_; e += blockDim.x) pv[e] = piv[p0 + e];
   __syncthreads();
   // the first interchange naming each pivot row below p1 (the same row can be named twice)
@@ -473,9 +477,10 @@ __global__ void __launch_bounds__(256) k_laswp(float* A, long long ld, int n, in
     int col = c0 + t;
     if (skip && col >= s0) col += skip;
     float* a = A + (size_t)col * ld;
-    for (int q = lane; q < ns; q += 32) seg[warp][q] = a[rowof[perm[q]]];
+    float* seg = segs + (size_t)warp * 2 * np_;
+    for (int q = lane; q < ns; q += 32) seg[q] = a[rowof[perm[q]]];
     __syncwarp();
-    for (int q = lane; q < ns; q += 32) a[rowof[q]] = seg[warp][q];
+    for (int q = lane; q < ns; q += 32) a[rowof[q]] = seg[q];
     __syncwarp();
   }
 }
@@ -1073,10 +1078,11 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
   tm.begin(st);
   const size_t tsm = (size_t)kNb * kNb * sizeof(float);
   O3G_CUDA_TRY(cudaFuncSetAttribute(k_trsm_unit_lower, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  O3G_CUDA_TRY(cudaFuncSetAttribute(k_laswp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)laswp_smem(kNbOuter)));
   // C = C - A B on the tensor cores (o3g_tcgemm.cu: tcgen05, TF32 products, FP32 sums; all
   // operands column-major in LU); the error word of its pipeline waits is flags[4]
   if (!h->tcw) {
-    const cudaError_t e = o3g::dev_alloc((void**)&h->tcw, tc_gemm_scratch_floats(n, 512) * sizeof(float));
+    const cudaError_t e = o3g::dev_alloc((void**)&h->tcw, tc_gemm_scratch_floats(n, kNbOuter) * sizeof(float));
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
       h->tcw = nullptr;
@@ -1119,13 +1125,12 @@ extern "C" int32_t o3g_bem_factor(o3g_bem_t* h, void* stream) {
     const int cnt = (c1 - c0) - (s1 > s0 ? s1 - s0 : 0);
     if (cnt <= 0) return;
     const int lb = std::min((cnt + 7) / 8, 8 * df.num_sms);
-    k_laswp<<<lb, 256, 0, st>>>(h->LU, ld, n, p0, p1, h->piv, c0, c1, s0, s1);
+    k_laswp<<<lb, 256, laswp_smem(p1 - p0), st>>>(h->LU, ld, n, p0, p1, h->piv, c0, c1, s0, s1);
     note_launch();
   };
   auto at = [&](int r, int c) { return h->LU + (size_t)c * ld + r; };
   // two-level right-looking LU: kNb-column panels inside kNbOuter-column outer panels; the
   // big trailing update of each outer panel has k = kNbOuter
-  constexpr int kNbOuter = 512;
   for (int K0 = 0; K0 < n; K0 += kNbOuter) {
     const int KB = std::min(kNbOuter, n - K0), K1 = K0 + KB;
     for (int k0 = K0; k0 < K1; k0 += kNb) {
