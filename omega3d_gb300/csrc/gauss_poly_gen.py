@@ -24,10 +24,10 @@ import numpy as np
 from numpy.polynomial import chebyshev as C
 from scipy.special import erf
 
-# interval j = [(j/2)^2, ((j+1)/2)^2) for j < 13 and [42.25, 48] for j = 13, so that the
-# kernels find j as floor(2 sqrt q) capped at 13
-EDGES = [(j / 2.0) ** 2 for j in range(14)] + [48.0]
-DEG = 6
+# interval j = [j, j + 1) for j = 0..47, so that the kernels find j as the integer part of
+# q (one conversion, no square root); degree 5 reaches the float rounding of q already
+EDGES = [float(j) for j in range(49)]
+DEG = 5
 # one interval's row: s, o, then (G_k, D_k) from k = DEG down to 0 (the order Horner's rule
 # consumes them)
 STRIDE = 2 + 2 * (DEG + 1)
@@ -125,7 +125,7 @@ namespace o3g {{
 
 constexpr int kGaussPolyDeg = {DEG};
 constexpr int kGaussPolyStride = {STRIDE};   // floats per interval: (s, o), (G[k], D[k]) for k = {DEG}..0
-constexpr int kGaussPolyN = {len(table)};        // intervals; interval j covers [(j/2)^2, ((j+1)/2)^2)
+constexpr int kGaussPolyN = {len(table)};        // intervals; interval j covers [j, j + 1)
 constexpr int kGaussPolyLast = {len(table) - 1};
 // float pair e2 of interval j at kGaussPoly[2 (e2 * kGaussPolyN + j)], [.. + 1]
 __device__ const __align__(16) float kGaussPoly[{STRIDE} * {len(table)}] = {{
@@ -141,8 +141,8 @@ __device__ const __align__(16) float kGaussPoly[{STRIDE} * {len(table)}] = {{
 # ---- the accurate (double-single) evaluation: o3g_gauss_poly_ds.h ----------------------
 # Degree DEG_DS in t = q s + o, with s and o the float32 values the kernel uses (the fit is
 # made in that t, so the map itself adds no error).  The kernel runs Horner's rule in float
-# for the coefficients of degree >= 3 (together at most 2.1 % of |G| or |D| on every
-# interval, so their float rounding stays near 1e-9 relative) and in double-single
+# for the coefficients of degree >= 3 (together at most 0.14 % of |G| or |D| on every
+# interval, so their float rounding stays near 1e-10 relative) and in double-single
 # arithmetic for degrees 2, 1, 0, whose coefficients are stored as (hi, lo) float pairs.
 DEG_DS = 8
 NDS = 3          # low-order coefficients kept as (hi, lo) pairs

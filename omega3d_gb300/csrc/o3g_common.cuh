@@ -232,19 +232,14 @@ __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 // piecewise polynomials of o3g_gauss_poly.h (Horner's rule in t = q s_j + o_j): branch-free,
 // no erf/exp/division.
 //
-// Interval of q: j covers [(j/2)^2, ((j+1)/2)^2) up to [42.25, 48], so j = floor(2 sqrt q)
-// capped at the last.  With the hardware reciprocal square root, q within about 1e-7
-// (relative) of an edge may land in the neighbouring interval, whose polynomial is still
-// fitted there (the fits are checked 1e-4 of their width beyond both ends).
-__device__ __forceinline__ int gauss_interval(float q) {
-  const float qq = fmaxf(q, 1.0e-30f);
-  return min((int)(2.0f * qq * rsqrtf(qq)), kGaussPolyLast);
-}
+// Interval of q: j covers [j, j + 1) up to [47, 48], so j is the integer part of q (q >= 0)
+// capped at the last; the fits are checked 1e-4 of their width beyond both ends.
+__device__ __forceinline__ int gauss_interval(float q) { return min((int)q, kGaussPolyLast); }
 
 // G(q) and D(q) by Horner's rule in t.  The table holds float pairs (s, o), (G_k, D_k),
 // coefficient-major (pair e2 of interval j at e2 * N + j), so the lanes of a warp, whatever
-// their intervals, read each pair from one 112-byte span (or, from a shared-memory copy,
-// from distinct banks), and the two chains advance together in packed FMAs (FFMA2: each
+// their intervals (neighbouring targets and sources give neighbouring q), read each pair
+// from a few cache lines or banks, and the two chains advance together in packed FMAs (FFMA2: each
 // lane rounds like FFMA, so G and D are bit-identical to two scalar chains).  `tab`: a
 // block's shared-memory copy of kGaussPoly (stage_gauss_table, 8-byte aligned), or nullptr
 // for the global table through the read-only cache.

@@ -6,7 +6,7 @@ velocity terms added unrounded into double-single running sums that the compensa
 Tolerances against the FP64 oracle (per-target relative error, metrics.rel_err):
   * velocity per target <= 1e-6 everywhere, the accuracy form the mode exists for;
   * velocity L-infinity <= 1e-7: the terms carry about 44 bits (the Gaussian core's
-    double-single polynomials are within 1.3e-9 of the function) and their sums are
+    double-single polynomials are within 1.2e-10 of the function) and their sums are
     exact to that level, so the float outputs' own rounding (6e-8) is what remains;
   * gradients per target <= 1e-5 and L-infinity <= 1e-6 (their terms are formed in float
     from the double-single core, as in COMPENSATED);
