@@ -31,9 +31,9 @@ struct SrcRec {
 struct TriG { float x0, y0, z0, x1, y1, z1, x2, y2, z2; };
 
 __device__ __forceinline__ void cen(const TriG& t, float& cx, float& cy, float& cz) {
-  cx = __fdiv_rn(__fadd_rn(__fadd_rn(t.x0, t.x1), t.x2), 3.0f);
-  cy = __fdiv_rn(__fadd_rn(__fadd_rn(t.y0, t.y1), t.y2), 3.0f);
-  cz = __fdiv_rn(__fadd_rn(__fadd_rn(t.z0, t.z1), t.z2), 3.0f);
+  cx = div3_rn(__fadd_rn(__fadd_rn(t.x0, t.x1), t.x2));
+  cy = div3_rn(__fadd_rn(__fadd_rn(t.y0, t.y1), t.y2));
+  cz = div3_rn(__fadd_rn(__fadd_rn(t.z0, t.z1), t.z2));
 }
 __device__ __forceinline__ float dist_rn3(float ax, float ay, float az, float bx, float by, float bz) {
   const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
@@ -88,6 +88,7 @@ template <int NUNK>
 __device__ __noinline__ void pair_subdivide(const TriG& s0, const TriG& t0, float sa, float ta, float s1x, float s1y,
                                             float s1z, float s2x, float s2y, float s2z, float q, int maxlev,
                                             float (*u)[3]) {
+  const float thr0 = __fmul_rn(__fadd_rn(__fsqrt_rn(sa), __fsqrt_rn(ta)), 4.0f);
   unsigned st[kCStack];
   int sp = 0;
   auto push = [&](unsigned code) {
@@ -103,11 +104,12 @@ __device__ __noinline__ void pair_subdivide(const TriG& s0, const TriG& t0, floa
     const TriG s = descend(s0, (code >> 3) & 0xffu, lev);
     const TriG t = descend(t0, (code >> 11) & 0xffu, lev);
     const float f4 = __int_as_float((127 - 2 * lev) << 23);   // 0.25^lev: the children's area factor
-    const float csa = sa * f4, cta = ta * f4;
     float scx, scy, scz, tcx, tcy, tcz;
     cen(s, scx, scy, scz);
     cen(t, tcx, tcy, tcz);
-    const float thr = __fmul_rn(__fadd_rn(__fsqrt_rn(csa), __fsqrt_rn(cta)), 4.0f);
+    // 4 (sqrt(sa 0.25^lev) + sqrt(ta 0.25^lev)) = thr0 0.5^lev exactly (scaling by powers of
+    // two commutes with the correctly rounded sqrt and add)
+    const float thr = __fmul_rn(thr0, __int_as_float((127 - lev) << 23));
     if (lev >= maxlev || dist_rn3(tcx, tcy, tcz, scx, scy, scz) > thr) {
       const float f = f4 * f4;   // 0.0625^lev (Kernels.h:1275-1278)
       leaf3<NUNK>(tcx, tcy, tcz, scx, scy, scz, s1x * f, s1y * f, s1z * f, s2x * f, s2y * f, s2z * f, q * f, u);
@@ -250,6 +252,8 @@ __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __
     const SrcRec s = srec[j];
     const TriG S0 = stri[j], T0 = ttri[i];
     const float sa = s.s1.w, ta = tarea[i];
+    // the level-lev threshold is thr0 0.5^lev exactly (as in pair_subdivide)
+    const float thr0 = __fmul_rn(__fadd_rn(__fsqrt_rn(sa), __fsqrt_rn(ta)), 4.0f);
     float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     // level L items: (parent index in the level L-1 list, child 0..15); codes keep the
     // source path in bits 0..7 and the target path in bits 8..15 (2 bits per level)
@@ -273,7 +277,7 @@ __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __
           float scx, scy, scz, tcx, tcy, tcz;
           cen(S, scx, scy, scz);
           cen(T, tcx, tcy, tcz);
-          const float thr = __fmul_rn(__fadd_rn(__fsqrt_rn(sa * f4), __fsqrt_rn(ta * f4)), 4.0f);
+          const float thr = __fmul_rn(thr0, __int_as_float((127 - lev) << 23));
           if (lev >= maxlev || dist_rn3(tcx, tcy, tcz, scx, scy, scz) > thr) {
             const float f = f4 * f4;
             leaf3<NUNK>(tcx, tcy, tcz, scx, scy, scz, s.s1.x * f, s.s1.y * f, s.s1.z * f, s.s2.x * f, s.s2.y * f,

@@ -210,6 +210,17 @@ __device__ __forceinline__ float exp_tang(float x) {
   return res * __int_as_float((127 + (n >> 5)) << 23);  // times 2^k, exact for normal results
 }
 
+// x / 3 correctly rounded, without a division: q = x RN(1/3), the residual x - 3 q exactly
+// (one fma), then q + residual RN(1/3) rounded once (Markstein's correction step for a
+// constant divisor, with the correctly rounded reciprocal 0x3EAAAAAB).  Checked against IEEE
+// x / 3.0f for all 2^32 float inputs; zero is passed through to keep its sign.
+__device__ __forceinline__ float div3_rn(float x) {
+  const float y = 0.333333343f;
+  const float q = __fmul_rn(x, y);
+  const float r = __fmaf_rn(-q, 3.0f, x);
+  return x == 0.0f ? x : __fmaf_rn(r, y, q);
+}
+
 // dx dx + dy dy + dz dz with every product and sum rounded, left to right: the reference's
 // expression (Kernels.h:167-170) as an uncontracted build evaluates it
 __device__ __forceinline__ float dist2_ref(float dx, float dy, float dz) {

@@ -40,9 +40,9 @@ struct Tri {
 
 // centroid and well-separation test in the reference's order (Kernels.h:1141-1158)
 __device__ __forceinline__ void centroid(const Tri& t, float& cx, float& cy, float& cz) {
-  cx = __fdiv_rn(__fadd_rn(__fadd_rn(t.x0, t.x1), t.x2), 3.0f);
-  cy = __fdiv_rn(__fadd_rn(__fadd_rn(t.y0, t.y1), t.y2), 3.0f);
-  cz = __fdiv_rn(__fadd_rn(__fadd_rn(t.z0, t.z1), t.z2), 3.0f);
+  cx = div3_rn(__fadd_rn(__fadd_rn(t.x0, t.x1), t.x2));
+  cy = div3_rn(__fadd_rn(__fadd_rn(t.y0, t.y1), t.y2));
+  cz = div3_rn(__fadd_rn(__fadd_rn(t.z0, t.z1), t.z2));
 }
 __device__ __forceinline__ float dist_rn(float tx, float ty, float tz, float cx, float cy, float cz) {
   const float dx = __fsub_rn(tx, cx), dy = __fsub_rn(ty, cy), dz = __fsub_rn(tz, cz);
