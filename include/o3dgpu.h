@@ -112,6 +112,10 @@ int32_t o3g_fp32_peak_probe(int32_t iters, void* stream, double* tflops, float* 
  * of a rounding boundary, and 1 ulp from it there.  For tests and
  * measurement; no counterpart in the reference, which calls its host library's expf. */
 int32_t o3g_exp_probe(int32_t n, const float* x, float* y, void* stream);
+/* Check of the division-free x / 3 of the panel centroids against IEEE division on the
+ * device, for the float bit patterns first .. first + count - 1 (count <= 2^32 - first):
+ * *mismatches = how many results differ in any bit (synchronises on `stream`). */
+int32_t o3g_div3_check(uint64_t first, uint64_t count, uint64_t* mismatches, void* stream);
 
 /* C -= A B on the tensor cores (tcgen05, TF32 products, FP32 sums): the update of the BEM
  * factorisation (o3g_bem_factor), callable on its own.  Device arrays, column-major:

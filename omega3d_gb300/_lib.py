@@ -86,6 +86,8 @@ def _declare(l):
     l.o3g_fp32_peak_probe.argtypes = [c_i32, P, P, P]
     l.o3g_exp_probe.restype = c_i32
     l.o3g_exp_probe.argtypes = [c_i32, P, P, P]
+    l.o3g_div3_check.restype = c_i32
+    l.o3g_div3_check.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
     l.o3g_gemm_tf32_sub.restype = c_i32
     l.o3g_gemm_tf32_sub.argtypes = [c_i32, c_i32, c_i32, P, ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64, P]
     l.o3g_points_affect_points.restype = c_i32

@@ -77,3 +77,42 @@ extern "C" int32_t o3g_exp_probe(int32_t n, const float* x, float* y, void* stre
   O3G_CUDA_TRY(cudaGetLastError());
   return O3G_OK;
 }
+
+namespace o3g {
+// div3_rn against IEEE division by 3 for the float bit patterns first .. first + count - 1
+// (a grid-stride sweep; every mismatch counted)
+__global__ void k_div3_check(unsigned long long first, unsigned long long count, unsigned long long* mismatches) {
+  unsigned long long bad = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+    const float x = __uint_as_float((unsigned)(first + k));
+    if (!isfinite(x)) continue;
+    if (__float_as_uint(div3_rn(x)) != __float_as_uint(__fdiv_rn(x, 3.0f))) ++bad;
+  }
+  if (bad) atomicAdd(mismatches, bad);
+}
+}  // namespace o3g
+
+extern "C" int32_t o3g_div3_check(uint64_t first, uint64_t count, uint64_t* mismatches, void* stream) {
+  using namespace o3g;
+  if (!mismatches || first > (1ull << 32) || count > (1ull << 32) - first) {
+    set_error("o3g_div3_check: the range must lie within the 2^32 float bit patterns; mismatches non-null");
+    return O3G_ERR_INVALID_ARG;
+  }
+  DeviceFacts df;
+  O3G_TRY(device_facts(&df));
+  cudaStream_t st = (cudaStream_t)stream;
+  Workspace* ws = nullptr;
+  O3G_TRY(workspace_get(st, 256, &ws));
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(ws->base);
+  O3G_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), st));
+  if (count > 0) {
+    k_div3_check<<<8 * df.num_sms, 256, 0, st>>>(first, count, d);
+    note_launch();
+  }
+  unsigned long long h = 0;
+  O3G_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st));
+  O3G_CUDA_TRY(cudaStreamSynchronize(st));
+  *mismatches = h;
+  return O3G_OK;
+}

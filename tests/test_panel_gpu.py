@@ -187,3 +187,14 @@ def test_panels_affect_panels_vs_oracle(cuda, on_device, self_influence):
         u = t.pu.copy()
     assert rel_err(u, uo)[0] <= 1e-5
     assert np.abs(u).max() > 0
+
+
+def test_centroid_division_by_three_is_ieee_for_every_float(cuda):
+    """The panel kernels form centroids as (a + b + c) / 3 in the reference's float order;
+    the division is a multiply by RN(1/3) and one fma correction (Markstein).  It must give
+    the IEEE quotient, bit for bit, for every one of the 2^32 float inputs."""
+    import ctypes
+    from omega3d_gb300 import _lib as L
+    bad = ctypes.c_uint64(1)
+    assert L.lib().o3g_div3_check(0, 1 << 32, ctypes.byref(bad), None) == 0
+    assert bad.value == 0
