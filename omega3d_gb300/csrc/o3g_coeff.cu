@@ -35,9 +35,20 @@ __device__ __forceinline__ void cen(const TriG& t, float& cx, float& cy, float& 
   cy = div3_rn(__fadd_rn(__fadd_rn(t.y0, t.y1), t.y2));
   cz = div3_rn(__fadd_rn(__fadd_rn(t.z0, t.z1), t.z2));
 }
-__device__ __forceinline__ float dist_rn3(float ax, float ay, float az, float bx, float by, float bz) {
+// |a - b| > thr as the reference decides it (the distance rounded to float: the correctly
+// rounded square root of the rounded sum of rounded squares), with thr2 = thr * thr rounded.
+// The correctly rounded square root is monotone and thr is a float, so the squared
+// distance d2 decides whenever it is more than 2^-20 away from thr2 (relative): above,
+// sqrt(d2) > thr (1 + 2^-22), more than half of thr's spacing (at most 2^-23 thr) beyond
+// thr, so it rounds above thr; below, sqrt(d2) < thr and it rounds to thr at most.  Only
+// the few pairs near the threshold take the square root.
+__device__ __forceinline__ bool farther_rn(float ax, float ay, float az, float bx, float by, float bz, float thr,
+                                           float thr2) {
   const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
-  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  if (d2 > __fmul_rn(thr2, 1.00000095367431640625f)) return true;    // 1 + 2^-20
+  if (d2 < __fmul_rn(thr2, 0.99999904632568359375f)) return false;   // 1 - 2^-20
+  return __fsqrt_rn(d2) > thr;
 }
 
 // singular leaf at target point t from a source point c with vortex strengths s1, s2 and
@@ -110,7 +121,7 @@ __device__ __noinline__ void pair_subdivide(const TriG& s0, const TriG& t0, floa
     // 4 (sqrt(sa 0.25^lev) + sqrt(ta 0.25^lev)) = thr0 0.5^lev exactly (scaling by powers of
     // two commutes with the correctly rounded sqrt and add)
     const float thr = __fmul_rn(thr0, __int_as_float((127 - lev) << 23));
-    if (lev >= maxlev || dist_rn3(tcx, tcy, tcz, scx, scy, scz) > thr) {
+    if (lev >= maxlev || farther_rn(tcx, tcy, tcz, scx, scy, scz, thr, __fmul_rn(thr, thr))) {
       const float f = f4 * f4;   // 0.0625^lev (Kernels.h:1275-1278)
       leaf3<NUNK>(tcx, tcy, tcz, scx, scy, scz, s1x * f, s1y * f, s1z * f, s2x * f, s2y * f, s2z * f, q * f, u);
     } else if (sp + 16 <= kCStack) {
@@ -168,20 +179,45 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
   const int j0 = blockIdx.y * kCB;
   sr[threadIdx.x] = srec[j0 + threadIdx.x];
   __syncthreads();
-  if (i >= tnp) return;
-  const TriG tt = ttri[i];
+  // every lane of a warp stays in the loop (the near-pair list is claimed per warp); lanes
+  // past the last target compute on a copy of it and write nothing
+  const bool valid = i < tnp;
+  const int ic = valid ? i : tnp - 1;
+  const TriG tt = ttri[ic];
   float tcx, tcy, tcz;
   cen(tt, tcx, tcy, tcz);
-  const float ta = tarea[i];
+  const float ta = tarea[ic];
   const float sqta = __fsqrt_rn(ta);
-  const float b[3][3] = {{t1x[i], t1y[i], t1z[i]}, {t2x[i], t2y[i], t2z[i]},
-                         {NUNK == 3 ? tnx[i] : 0.f, NUNK == 3 ? tny[i] : 0.f, NUNK == 3 ? tnz[i] : 0.f}};
+  const float b[3][3] = {{t1x[ic], t1y[ic], t1z[ic]}, {t2x[ic], t2y[ic], t2z[ic]},
+                         {NUNK == 3 ? tnx[ic] : 0.f, NUNK == 3 ? tny[ic] : 0.f, NUNK == 3 ? tnz[ic] : 0.f}};
   const float fac = (float)(1.0 / (4.0 * 3.14159265358979323846));
+  const int lane = threadIdx.x & 31;
   const int jend = min(kCB, snp - j0);
   for (int jj = 0; jj < jend; ++jj) {
     const int j = j0 + jj;
+    const bool self = is_self && j == i;
+    const SrcRec s = sr[jj];
+    const float thr = __fmul_rn(__fadd_rn(s.c.w, sqta), 4.0f);
+    const bool far = maxlev == 0 || farther_rn(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, thr, __fmul_rn(thr, thr));
+    const bool near = valid && !self && !far;
+    bool listed = false;
+    if (nl.cap > 0) {
+      // one atomic per warp for its near pairs of this source
+      const unsigned m = __ballot_sync(0xffffffffu, near);
+      if (m) {
+        unsigned base = 0;
+        if (lane == __ffs(m) - 1) base = atomicAdd(nl.count, (unsigned)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+        const unsigned slot = base + (unsigned)__popc(m & ((1u << lane) - 1u));
+        if (near && slot < nl.cap) {
+          nl.pairs[slot] = make_uint2((unsigned)i, (unsigned)j);
+          listed = true;   // written by k_coeff_near
+        }
+      }
+    }
+    if (!valid || listed) continue;
     float* col = coeff + (size_t)j * NUNK * (size_t)ld + (size_t)i * NUNK;
-    if (is_self && j == i) {
+    if (self) {
       // Coefficients.h:414-436, then the 1/(4 pi) scale of :443-447, both in float
       const float tp = (float)(2.0 * 3.14159265358979323846);
       col[0] = 0.f * fac;
@@ -197,22 +233,12 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
       }
       continue;
     }
-    const SrcRec s = sr[jj];
     float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    const float thr = __fmul_rn(__fadd_rn(s.c.w, sqta), 4.0f);
-    if (maxlev == 0 || dist_rn3(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z) > thr) {
+    if (far)
       leaf3<NUNK>(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, u);
-    } else {
-      if (nl.cap > 0) {
-        const unsigned slot = atomicAdd(nl.count, 1u);
-        if (slot < nl.cap) {
-          nl.pairs[slot] = make_uint2((unsigned)i, (unsigned)j);
-          continue;   // written by k_coeff_near
-        }
-      }
+    else
       pair_subdivide<NUNK>(stri[j], tt, s.s1.w, ta, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, maxlev,
                            u);
-    }
 #pragma unroll
     for (int k = 0; k < NUNK; ++k)
 #pragma unroll
@@ -226,7 +252,56 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
 // every child pair that is neither well separated nor at maxlev contributes 16 pairs to the
 // next level, kept in a per-warp list in shared memory in enumeration order.  Leaves are
 // summed per lane and reduced across the warp in a fixed order.
+//
+// A pair at level L needs only the centroids of one level-L sub-triangle of each panel,
+// and every pair of a level shares them: the warp builds the 4^L sub-triangles of both
+// panels once per level (each from its stored parent by child(), the same operations as a
+// descent from the root) and keeps their centroids in shared memory, indexed by the
+// path (2 bits per level, level 1 in the low bits).  A pair then costs six shared loads,
+// the distance test and the leaf.
 constexpr int kNearWarps = 4;
+struct NearShared {
+  float tri[2][20][9];   // [source, target][level 1: 0..3, level 2: 4..19] sub-triangles
+  float cen[2][84][3];   // [source, target][level 1: 0..3, level 2: 4..19, level 3: 20..83]
+};
+
+__device__ __forceinline__ void store_tri(float* d, const TriG& t) {
+  d[0] = t.x0; d[1] = t.y0; d[2] = t.z0; d[3] = t.x1; d[4] = t.y1; d[5] = t.z1; d[6] = t.x2; d[7] = t.y2; d[8] = t.z2;
+}
+__device__ __forceinline__ TriG load_tri(const float* d) {
+  return TriG{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]};
+}
+__device__ __forceinline__ void store_cen(float* d, const TriG& t) {
+  float cx, cy, cz;
+  cen(t, cx, cy, cz);
+  d[0] = cx; d[1] = cy; d[2] = cz;
+}
+
+// the level-lev sub-triangles of both panels (and their centroids) into sh; lev 1..3
+__device__ __forceinline__ void build_level(NearShared& sh, const TriG& S0, const TriG& T0, int lev, int lane) {
+  if (lev == 1) {
+    if (lane < 8) {
+      const int side = lane >> 2, c = lane & 3;
+      const TriG t = child(side ? T0 : S0, c);
+      store_tri(sh.tri[side][c], t);
+      store_cen(sh.cen[side][c], t);
+    }
+  } else if (lev == 2) {
+    // path p = (level-2 child << 2) | level-1 child
+    const int side = lane >> 4, p = lane & 15;
+    const TriG t = child(load_tri(sh.tri[side][p & 3]), p >> 2);
+    store_tri(sh.tri[side][4 + p], t);
+    store_cen(sh.cen[side][4 + p], t);
+  } else {
+#pragma unroll 1
+    for (int e = lane; e < 128; e += 32) {
+      const int side = e >> 6, p = e & 63;
+      store_cen(sh.cen[side][20 + p], child(load_tri(sh.tri[side][4 + (p & 15)]), p >> 4));
+    }
+  }
+  __syncwarp();
+}
+
 template <int NUNK>
 __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __restrict__ srec,
                                                                const TriG* __restrict__ stri,
@@ -243,7 +318,9 @@ __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __
                                                                const float* __restrict__ tnz, int maxlev,
                                                                float* __restrict__ coeff, long long ld, NearList nl) {
   __shared__ unsigned lst[kNearWarps][2][256];
+  __shared__ NearShared shw[kNearWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  NearShared& sh = shw[warp];
   const unsigned total = min(*nl.count, nl.cap);
   const float fac = (float)(1.0 / (4.0 * 3.14159265358979323846));
   for (unsigned p = blockIdx.x * kNearWarps + warp; p < total; p += gridDim.x * kNearWarps) {
@@ -259,10 +336,15 @@ __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __
     // source path in bits 0..7 and the target path in bits 8..15 (2 bits per level)
     int nparent = 1;
     for (int lev = 1; lev <= maxlev; ++lev) {
+      build_level(sh, S0, T0, lev, lane);
       const int nitems = nparent * 16;
       const int cur = lev & 1, prev = cur ^ 1;
       int nnext = 0;
       const float f4 = __int_as_float((127 - 2 * lev) << 23);
+      const float f = f4 * f4;   // 0.0625^lev (Kernels.h:1275-1278)
+      const float thr = __fmul_rn(thr0, __int_as_float((127 - lev) << 23));
+      const float thr2 = __fmul_rn(thr, thr);
+      const int off = lev == 1 ? 0 : (lev == 2 ? 4 : 20);   // first centroid of the level
       for (int base = 0; base < nitems; base += 32) {
         const int k = base + lane;
         bool expand = false;
@@ -273,13 +355,11 @@ __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __
           const unsigned sp = (pc & 0xffu) | (a << (2 * (lev - 1)));
           const unsigned tp = ((pc >> 8) & 0xffu) | (b << (2 * (lev - 1)));
           code = sp | (tp << 8);
-          const TriG S = descend(S0, sp, lev), T = descend(T0, tp, lev);
-          float scx, scy, scz, tcx, tcy, tcz;
-          cen(S, scx, scy, scz);
-          cen(T, tcx, tcy, tcz);
-          const float thr = __fmul_rn(thr0, __int_as_float((127 - lev) << 23));
-          if (lev >= maxlev || dist_rn3(tcx, tcy, tcz, scx, scy, scz) > thr) {
-            const float f = f4 * f4;
+          const float* sc = sh.cen[0][off + sp];
+          const float* tc = sh.cen[1][off + tp];
+          const float scx = sc[0], scy = sc[1], scz = sc[2];
+          const float tcx = tc[0], tcy = tc[1], tcz = tc[2];
+          if (lev >= maxlev || farther_rn(tcx, tcy, tcz, scx, scy, scz, thr, thr2)) {
             leaf3<NUNK>(tcx, tcy, tcz, scx, scy, scz, s.s1.x * f, s.s1.y * f, s.s1.z * f, s.s2.x * f, s.s2.y * f,
                         s.s2.z * f, s.s1.w * f, u);
           } else {
@@ -306,8 +386,11 @@ __global__ void __launch_bounds__(32 * kNearWarps) k_coeff_near(const SrcRec* __
       if (l == 0) { bx = t1x[i]; by = t1y[i]; bz = t1z[i]; }
       else if (l == 1) { bx = t2x[i]; by = t2y[i]; bz = t2z[i]; }
       else { bx = tnx[i]; by = tny[i]; bz = tnz[i]; }
+      const float ux = k == 0 ? u[0][0] : (k == 1 ? u[1][0] : u[2][0]);
+      const float uy = k == 0 ? u[0][1] : (k == 1 ? u[1][1] : u[2][1]);
+      const float uz = k == 0 ? u[0][2] : (k == 1 ? u[1][2] : u[2][2]);
       float* col = coeff + (size_t)j * NUNK * (size_t)ld + (size_t)i * NUNK;
-      col[(size_t)k * ld + l] = (u[k][0] * bx + u[k][1] * by + u[k][2] * bz) * fac;
+      col[(size_t)k * ld + l] = (ux * bx + uy * by + uz * bz) * fac;
     }
     __syncwarp();
   }
