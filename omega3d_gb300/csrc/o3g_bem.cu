@@ -1580,50 +1580,80 @@ __global__ void k_split_f64_multi(DIn src, float* xh, float* xl, int n) {
 }
 
 // part[cb][c][i] = sum over the columns of chunk cb of A[i, j] x_c[j], double-single as in
-// k_matvec_ds: every matrix element is loaded once for the K vectors
+// k_matvec_ds: every matrix element is loaded once for the K vectors.  With K vectors the
+// sums cost K times the FP32 instructions of one, so they run in packed FP32 (FFMA2,
+// FADD2, FMUL2; each lane rounds like the scalar instruction): columns j and j + 1 of the
+// chunk ride in the two lanes, each lane carrying its own double-single sum, added in
+// double at the end.  Differences are formed as fused multiply-adds with -1 (exact
+// negation), so the two-sum needs no negated operands: shared memory holds x_h, -x_h and
+// x_l of each column pair.
+__device__ __forceinline__ void ds_add_product2(float2 a, float2 h, float2 hn, float2 l, float2& hi, float2& lo) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 pn = __fmul2_rn(a, hn);                      // -p, p = a h rounded
+  const float2 e = __ffma2_rn(a, h, pn);                    // a h - p, exact
+  const float2 sum = __ffma2_rn(pn, m1, hi);                // hi + p
+  const float2 bb = __ffma2_rn(hi, m1, sum);                // sum - hi
+  const float2 t2 = __ffma2_rn(__ffma2_rn(bb, m1, sum), m1, hi);   // hi - (sum - bb)
+  const float2 t = __ffma2_rn(__fadd2_rn(pn, bb), m1, t2);  // t2 + (p - bb)
+  hi = sum;
+  lo = __ffma2_rn(a, l, __fadd2_rn(lo, __fadd2_rn(t, e)));
+}
+
 template <int K>
 __global__ void __launch_bounds__(256) k_matvec_ds_multi(const float* __restrict__ A, long long ld, int n,
                                                          const float* __restrict__ xh, const float* __restrict__ xl,
                                                          double* __restrict__ part) {
-  __shared__ float sh[K][kMvChunkM], sl[K][kMvChunkM];
+  constexpr int M2 = kMvChunkM / 2;
+  __shared__ float2 sh[K][M2], shn[K][M2], sl[K][M2];   // column pairs (x_h, -x_h, x_l)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int cb = blockIdx.y;
   const int j0 = cb * kMvChunkM, m = min(n - j0, kMvChunkM);
 #pragma unroll
   for (int c = 0; c < K; ++c)
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
-      sh[c][k] = xh[(size_t)c * n + j0 + k];
-      sl[c][k] = xl[(size_t)c * n + j0 + k];
+    for (int k = threadIdx.x; k < M2; k += blockDim.x) {
+      // a column beyond the chunk gets x = 0 (and its matrix element 0 below)
+      const float h0 = 2 * k < m ? xh[(size_t)c * n + j0 + 2 * k] : 0.f;
+      const float h1 = 2 * k + 1 < m ? xh[(size_t)c * n + j0 + 2 * k + 1] : 0.f;
+      const float l0 = 2 * k < m ? xl[(size_t)c * n + j0 + 2 * k] : 0.f;
+      const float l1 = 2 * k + 1 < m ? xl[(size_t)c * n + j0 + 2 * k + 1] : 0.f;
+      sh[c][k] = make_float2(h0, h1);
+      shn[c][k] = make_float2(-h0, -h1);
+      sl[c][k] = make_float2(l0, l1);
     }
   __syncthreads();
   if (i >= n) return;
   const float* a = A + (size_t)j0 * ld + i;
-  float hi[K], lo[K];
+  float2 hi[K], lo[K];
 #pragma unroll
-  for (int c = 0; c < K; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
+  for (int c = 0; c < K; ++c) { hi[c] = make_float2(0.f, 0.f); lo[c] = make_float2(0.f, 0.f); }
+  const float2 m1 = make_float2(-1.f, -1.f);
   int k = 0;
   for (; k + 8 <= m; k += 8) {
-    float av[8];
+    float2 av[4];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) av[q] = __ldg(a + (size_t)(k + q) * ld);
+    for (int q = 0; q < 4; ++q)
+      av[q] = make_float2(__ldg(a + (size_t)(k + 2 * q) * ld), __ldg(a + (size_t)(k + 2 * q + 1) * ld));
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
+    for (int q = 0; q < 4; ++q)
 #pragma unroll
-      for (int c = 0; c < K; ++c) ds_add_product(av[q], sh[c][k + q], sl[c][k + q], hi[c], lo[c]);
+      for (int c = 0; c < K; ++c)
+        ds_add_product2(av[q], sh[c][k / 2 + q], shn[c][k / 2 + q], sl[c][k / 2 + q], hi[c], lo[c]);
+    // renormalise: move the bulk of lo into hi (Dekker's fast two-sum, |hi| >= |lo|)
 #pragma unroll
     for (int c = 0; c < K; ++c) {
-      const float s2 = __fadd_rn(hi[c], lo[c]);
-      lo[c] = __fsub_rn(lo[c], __fsub_rn(s2, hi[c]));
+      const float2 s2 = __fadd2_rn(hi[c], lo[c]);
+      lo[c] = __ffma2_rn(__ffma2_rn(hi[c], m1, s2), m1, lo[c]);
       hi[c] = s2;
     }
   }
-  for (; k < m; ++k) {
-    const float av = __ldg(a + (size_t)k * ld);
+  for (; k < m; k += 2) {   // the chunk's last columns (m is even except at the matrix edge)
+    const float2 av = make_float2(__ldg(a + (size_t)k * ld), k + 1 < m ? __ldg(a + (size_t)(k + 1) * ld) : 0.f);
 #pragma unroll
-    for (int c = 0; c < K; ++c) ds_add_product(av, sh[c][k], sl[c][k], hi[c], lo[c]);
+    for (int c = 0; c < K; ++c) ds_add_product2(av, sh[c][k / 2], shn[c][k / 2], sl[c][k / 2], hi[c], lo[c]);
   }
 #pragma unroll
-  for (int c = 0; c < K; ++c) part[((size_t)cb * K + c) * n + i] = (double)hi[c] + (double)lo[c];
+  for (int c = 0; c < K; ++c)
+    part[((size_t)cb * K + c) * n + i] = ((double)hi[c].x + (double)lo[c].x) + ((double)hi[c].y + (double)lo[c].y);
 }
 
 // y_c = b_c - sum_cb part (b given) or y_c = sum_cb part, c = blockIdx.y < K; per-block sums
@@ -1782,11 +1812,17 @@ static int32_t matvec_multi(o3g_bem_t* h, int K, const DIn& x, const DIn& b, con
   const int nrb = (n + 255) / 256;
   const int ncb = (n + kMvChunkM - 1) / kMvChunkM;
   int nc = 0;
-  if (x.p[0]) {
+  if (x.p[0] && K == 1) {
+    // one vector: the single-vector product (HBM-bound already, 1024-column chunks)
+    k_split_f64_multi<<<dim3(nrb, 1), 256, 0, st>>>(x, xh, xl, n);
+    const int ncb1 = (n + kMvChunk - 1) / kMvChunk;
+    k_matvec_ds<<<dim3(nrb, ncb1), 256, 0, st>>>(h->A, h->ld, n, xh, xl, part);
+    note_launch(2);
+    nc = ncb1;
+  } else if (x.p[0]) {
     k_split_f64_multi<<<dim3(nrb, K), 256, 0, st>>>(x, xh, xl, n);
     const dim3 g(nrb, ncb);
     switch (K) {
-      case 1: k_matvec_ds_multi<1><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
       case 2: k_matvec_ds_multi<2><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
       case 3: k_matvec_ds_multi<3><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;
       case 4: k_matvec_ds_multi<4><<<g, 256, 0, st>>>(h->A, h->ld, n, xh, xl, part); break;

@@ -173,8 +173,10 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
                                                const float* __restrict__ t2y, const float* __restrict__ t2z,
                                                const float* __restrict__ tnx, const float* __restrict__ tny,
                                                const float* __restrict__ tnz, int tnp, int is_self, int maxlev,
-                                               float* __restrict__ coeff, long long ld, NearList nl) {
+                                               float* __restrict__ coeff, long long ld, int vec2, NearList nl) {
   __shared__ SrcRec sr[kCB];
+  // per warp, one column's entries of its 32 targets, for coalesced stores (NUNK == 3)
+  __shared__ float ob[NUNK == 3 ? kCB / 32 : 1][NUNK == 3 ? 3 * 3 * 32 : 1];
   const int i = blockIdx.x * kCB + threadIdx.x;
   const int j0 = blockIdx.y * kCB;
   sr[threadIdx.x] = srec[j0 + threadIdx.x];
@@ -215,35 +217,64 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
         }
       }
     }
-    if (!valid || listed) continue;
-    float* col = coeff + (size_t)j * NUNK * (size_t)ld + (size_t)i * NUNK;
-    if (self) {
-      // Coefficients.h:414-436, then the 1/(4 pi) scale of :443-447, both in float
-      const float tp = (float)(2.0 * 3.14159265358979323846);
-      col[0] = 0.f * fac;
-      col[1] = tp * fac;
-      if (NUNK == 3) col[2] = 0.f;
-      col[(size_t)ld] = -tp * fac;
-      col[(size_t)ld + 1] = 0.f;
-      if (NUNK == 3) {
-        col[(size_t)ld + 2] = 0.f;
-        col[2 * (size_t)ld] = 0.f;
-        col[2 * (size_t)ld + 1] = 0.f;
-        col[2 * (size_t)ld + 2] = tp * fac;
-      }
-      continue;
-    }
-    float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    if (far)
-      leaf3<NUNK>(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, u);
-    else
-      pair_subdivide<NUNK>(stri[j], tt, s.s1.w, ta, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, maxlev,
-                           u);
+    // the block entries v[k][l] (source unknown k, target unknown l); the listed pairs get
+    // 0 here and their values from k_coeff_near, which runs after this kernel
+    float v[NUNK][NUNK];
 #pragma unroll
     for (int k = 0; k < NUNK; ++k)
 #pragma unroll
-      for (int l = 0; l < NUNK; ++l)
-        col[(size_t)k * ld + l] = (u[k][0] * b[l][0] + u[k][1] * b[l][1] + u[k][2] * b[l][2]) * fac;
+      for (int l = 0; l < NUNK; ++l) v[k][l] = 0.f;
+    if (self) {
+      // Coefficients.h:414-436, then the 1/(4 pi) scale of :443-447, both in float
+      const float tp = (float)(2.0 * 3.14159265358979323846);
+      v[0][0] = 0.f * fac;
+      v[0][1] = tp * fac;
+      v[1][0] = -tp * fac;
+      if (NUNK == 3) v[2][2] = tp * fac;
+    } else if (valid && !listed) {
+      float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      if (far)
+        leaf3<NUNK>(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, u);
+      else
+        pair_subdivide<NUNK>(stri[j], tt, s.s1.w, ta, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w,
+                             maxlev, u);
+#pragma unroll
+      for (int k = 0; k < NUNK; ++k)
+#pragma unroll
+        for (int l = 0; l < NUNK; ++l) v[k][l] = (u[k][0] * b[l][0] + u[k][1] * b[l][1] + u[k][2] * b[l][2]) * fac;
+    }
+    // column j NUNK + k holds rows i NUNK + l: a warp's 32 targets are 32 NUNK consecutive
+    // floats of each column
+    float* col = coeff + (size_t)j * NUNK * (size_t)ld;
+    if (NUNK == 2 && vec2) {
+      // 8-byte aligned rows: one float2 per column, each warp store 256 contiguous bytes
+      if (valid) {
+#pragma unroll
+        for (int k = 0; k < NUNK; ++k)
+          *reinterpret_cast<float2*>(col + (size_t)k * ld + (size_t)i * 2) = make_float2(v[k][0], v[k][1]);
+      }
+    } else if (NUNK == 3) {
+      // through shared memory, so that each warp store covers 128 contiguous bytes
+      float* w = ob[threadIdx.x >> 5];
+      const int i0 = i - lane;
+#pragma unroll
+      for (int k = 0; k < NUNK; ++k)
+#pragma unroll
+        for (int l = 0; l < NUNK; ++l) w[k * 96 + lane * 3 + l] = v[k][l];
+      __syncwarp();
+      const int rows = min(32, tnp - i0) * 3;
+#pragma unroll
+      for (int k = 0; k < NUNK; ++k)
+#pragma unroll
+        for (int e = lane; e < 96; e += 32)
+          if (e < rows) col[(size_t)k * ld + (size_t)i0 * 3 + e] = w[k * 96 + e];
+      __syncwarp();
+    } else if (valid) {
+#pragma unroll
+      for (int k = 0; k < NUNK; ++k)
+#pragma unroll
+        for (int l = 0; l < NUNK; ++l) col[(size_t)k * ld + (size_t)i * NUNK + l] = v[k][l];
+    }
   }
 }
 
@@ -463,10 +494,12 @@ extern "C" int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int3
   KernelTimer& tm = thread_timer();
   tm.begin(st);
   const int nearblocks = 8 * df.num_sms;
+  // float2 stores when every row pair (2 i, 2 i + 1) of every column is 8-byte aligned
+  const int vec2 = nunk == 2 && ((uintptr_t)coeffs & 7u) == 0 && (ld & 1) == 0;
   if (nunk == 2) {
     k_coeff<2><<<grid, kCB, 0, st>>>(srec, stri, snp, ttri, targ->area, targ->x1x, targ->x1y, targ->x1z, targ->x2x,
                                      targ->x2y, targ->x2z, nullptr, nullptr, nullptr, tnp, is_self, maxlev, coeffs, ld,
-                                     nl);
+                                     vec2, nl);
     if (cap > 0)
       k_coeff_near<2><<<nearblocks, 32 * kNearWarps, 0, st>>>(srec, stri, ttri, targ->area, targ->x1x, targ->x1y,
                                                               targ->x1z, targ->x2x, targ->x2y, targ->x2z, nullptr,
@@ -474,7 +507,7 @@ extern "C" int32_t o3g_panels_on_panels_coeff(int32_t maxlev, int32_t nunk, int3
   } else {
     k_coeff<3><<<grid, kCB, 0, st>>>(srec, stri, snp, ttri, targ->area, targ->x1x, targ->x1y, targ->x1z, targ->x2x,
                                      targ->x2y, targ->x2z, targ->nx, targ->ny, targ->nz, tnp, is_self, maxlev, coeffs,
-                                     ld, nl);
+                                     ld, 0, nl);
     if (cap > 0)
       k_coeff_near<3><<<nearblocks, 32 * kNearWarps, 0, st>>>(srec, stri, ttri, targ->area, targ->x1x, targ->x1y,
                                                               targ->x1z, targ->x2x, targ->x2y, targ->x2z, targ->nx,
