@@ -232,16 +232,25 @@ __global__ void __launch_bounds__(kCB) k_coeff(const SrcRec* __restrict__ srec, 
       v[1][0] = -tp * fac;
       if (NUNK == 3) v[2][2] = tp * fac;
     } else if (valid && !listed) {
-      float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      if (far)
+      // two accumulators: the one handed to the out-of-line subdivision lives in local
+      // memory, the far pairs' one stays in registers
+      auto project = [&](const float (*u)[3]) {
+#pragma unroll
+        for (int k = 0; k < NUNK; ++k)
+#pragma unroll
+          for (int l = 0; l < NUNK; ++l)
+            v[k][l] = (u[k][0] * b[l][0] + u[k][1] * b[l][1] + u[k][2] * b[l][2]) * fac;
+      };
+      if (far) {
+        float u[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
         leaf3<NUNK>(tcx, tcy, tcz, s.c.x, s.c.y, s.c.z, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w, u);
-      else
+        project(u);
+      } else {
+        float us[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
         pair_subdivide<NUNK>(stri[j], tt, s.s1.w, ta, s.s1.x, s.s1.y, s.s1.z, s.s2.x, s.s2.y, s.s2.z, s.s1.w,
-                             maxlev, u);
-#pragma unroll
-      for (int k = 0; k < NUNK; ++k)
-#pragma unroll
-        for (int l = 0; l < NUNK; ++l) v[k][l] = (u[k][0] * b[l][0] + u[k][1] * b[l][1] + u[k][2] * b[l][2]) * fac;
+                             maxlev, us);
+        project(us);
+      }
     }
     // column j NUNK + k holds rows i NUNK + l: a warp's 32 targets are 32 NUNK consecutive
     // floats of each column
