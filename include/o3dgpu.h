@@ -305,6 +305,13 @@ int32_t o3g_bem_solve(o3g_bem_t* h, const float* b, float* x, double* x64, int32
  * assembled matrix (o3g_bem_matrix / o3g_bem_set_block). */
 int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
                             int32_t max_iter, int32_t restart, int32_t* iters, double* relres, void* stream);
+/* unknowns per panel (1..3, dividing n; default 1) of the assembled system: the GMRES solves
+ * (o3g_bem_solve_gmres, o3g_bem_solve_gmres_many) then precondition with the inverses of the
+ * bs x bs diagonal blocks, a panel's self-influence (Coefficients.h:414-436), applied on the
+ * right so that the residual stays ||b - A x||.  The reference's Eigen GMRES uses a diagonal
+ * preconditioner (BEM.h:182-202); with 1 nothing changes (the vortex rows' diagonal is 0,
+ * where a diagonal preconditioner is the identity). */
+int32_t o3g_bem_set_unknowns_per_panel(o3g_bem_t* h, int32_t bs);
 /* Several right-hand sides at once: B holds nrhs vectors of n floats back to back (column c
  * at B + c n, an n x nrhs column-major block), X (float) and X64 (double, nullable) the
  * solutions in the same layout, iters and relres (nullable) nrhs entries.  Each refinement

@@ -130,6 +130,8 @@ def _declare(l):
     l.o3g_bem_solve.argtypes = [P, P, P, P, c_i32, c_d, c_i32, P, P, P]
     l.o3g_bem_solve_gmres.restype = c_i32
     l.o3g_bem_solve_gmres.argtypes = [P, P, P, P, c_i32, c_d, c_i32, c_i32, P, P, P]
+    l.o3g_bem_set_unknowns_per_panel.restype = c_i32
+    l.o3g_bem_set_unknowns_per_panel.argtypes = [P, c_i32]
     l.o3g_bem_solve_many.restype = c_i32
     l.o3g_bem_solve_many.argtypes = [P, c_i32, P, P, P, c_i32, c_d, c_i32, P, P, P]
     l.o3g_bem_solve_gmres_many.restype = c_i32

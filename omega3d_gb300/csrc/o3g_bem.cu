@@ -927,6 +927,7 @@ struct o3g_bem {
   float* tcw = nullptr;   // K-major copies of the update's left operand (n x 512)
   bool factored = false;
   int panel_blocks = 0, solve_blocks = 0;
+  int bs = 1;             // unknowns per panel: GMRES preconditions with the bs x bs diagonal blocks
 };
 
 using namespace o3g;
@@ -999,6 +1000,16 @@ extern "C" int32_t o3g_bem_matrix(o3g_bem_t* h, float** A, int64_t* ld) {
   *A = h->A;
   *ld = h->ld;
   h->factored = false;
+  return O3G_OK;
+}
+
+extern "C" int32_t o3g_bem_set_unknowns_per_panel(o3g_bem_t* h, int32_t bs) {
+  O3G_TRY(bem_check(h));
+  if (bs < 1 || bs > 3 || h->n % bs != 0) {
+    set_error("o3g_bem_set_unknowns_per_panel: bs must be 1..3 and divide n");
+    return O3G_ERR_INVALID_ARG;
+  }
+  h->bs = bs;
   return O3G_OK;
 }
 
@@ -1374,6 +1385,56 @@ __global__ void k_kry_scale(double* w, int n, double s) {
   if (i < n) w[i] *= s;
 }
 
+// Block-Jacobi preconditioner of GMRES: the inverses (FP64) of the bs x bs diagonal blocks
+// of A, one per panel (the panel's self-influence, Coefficients.h:414-436, when the blocks
+// are surfaces on themselves).  A block that is singular or not finite gets the identity.
+// Minv[p] is row-major.
+__global__ void k_block_inv(const float* __restrict__ A, long long ld, int nb, int bs, double* __restrict__ Minv) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nb) return;
+  double a[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+  const size_t o = (size_t)p * bs;
+  for (int r = 0; r < bs; ++r)
+    for (int c = 0; c < bs; ++c) a[r][c] = (double)A[(o + c) * ld + o + r];
+  double inv[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+  // cofactors of the 3 x 3 (a 1 x 1 or 2 x 2 block sits in the leading corner of an
+  // identity, so the same formula serves)
+  const double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  const double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+  const double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  const double det = a[0][0] * c00 + a[0][1] * c01 + a[0][2] * c02;
+  if (det != 0.0 && isfinite(det)) {
+    const double id = 1.0 / det;
+    inv[0][0] = c00 * id;
+    inv[1][0] = c01 * id;
+    inv[2][0] = c02 * id;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) * id;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) * id;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * id;
+  }
+  for (int r = 0; r < bs; ++r)
+    for (int c = 0; c < bs; ++c) Minv[(size_t)p * bs * bs + r * bs + c] = inv[r][c];
+}
+// out = M^-1 in (acc = 0) or out += M^-1 in (acc = 1), K vectors of n (blockIdx.y)
+__global__ void k_block_apply(const double* __restrict__ Minv, int nb, int bs, const double* __restrict__ in,
+                              double* __restrict__ out, int n, int acc) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nb) return;
+  const double* x = in + (size_t)blockIdx.y * n + (size_t)p * bs;
+  double* y = out + (size_t)blockIdx.y * n + (size_t)p * bs;
+  const double* M = Minv + (size_t)p * bs * bs;
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int c = 0; c < bs; ++c) v[c] = x[c];
+  for (int r = 0; r < bs; ++r) {
+    double t = 0.0;
+    for (int c = 0; c < bs; ++c) t += M[r * bs + c] * v[c];
+    y[r] = acc ? y[r] + t : t;
+  }
+}
+
 namespace {
 // one classical Gram-Schmidt pass: hp = V^T w (kc columns), w -= V hp
 void gs_pass(const double* V, int n, int kc, double* w, double* hp, double* part, cudaStream_t st) {
@@ -1402,9 +1463,11 @@ double host_sum(const std::vector<double>& v) {
 // basis, sums in a fixed order), Givens
 // rotations of the small Hessenberg matrix on the host, FP64-accurate matrix products
 // (k_matvec_ds).  The true residual ||b - A x|| / ||b|| (BEM.h:227-230) is recomputed at
-// every restart and decides convergence.  No preconditioner: the vortex-sheet rows of the
-// matrix have a zero diagonal (Coefficients.h:414-436), where a Jacobi preconditioner is
-// the identity.
+// every restart and decides convergence.  The vortex-sheet rows of the matrix have a zero
+// diagonal (Coefficients.h:414-436), where a Jacobi preconditioner is the identity; with the
+// unknowns per panel set (o3g_bem_set_unknowns_per_panel) GMRES is right-preconditioned by
+// the inverses of the panels' diagonal blocks (A M^-1 u = b, x = M^-1 u), which keeps the
+// residual the system's own.
 extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, double* x64, int32_t mem, double tol,
                                        int32_t max_iter, int32_t restart, int32_t* iters, double* relres,
                                        void* stream) {
@@ -1421,14 +1484,23 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
   const int ncb = (n + kMvChunk - 1) / kMvChunk;
   const int nrb = (n + 255) / 256;
   const int nkb = (n + kKrylovRows - 1) / kKrylovRows;
+  const int bs = h->bs, npb = n / bs;
+  const bool pre = bs > 1;
   const size_t need = align_up((size_t)(m + 1) * n * 8) + 2 * align_up((size_t)n * 8) + 4 * align_up((size_t)n * 4) +
                       align_up((size_t)ncb * n * 8) + align_up((size_t)nrb * 8) + align_up((size_t)2 * (m + 1) * 8) +
-                      2 * align_up((size_t)nkb * (m + 1) * 8);
+                      2 * align_up((size_t)nkb * (m + 1) * 8) + align_up((size_t)n * bs * 8) + align_up((size_t)n * 8);
   O3G_TRY(bem_scratch(h, need));
   Carve cv(h->scratch);
   double* V = cv.take<double>((size_t)(m + 1) * n);
   double* bd = cv.take<double>(n);
   double* xd = cv.take<double>(n);
+  double* Minv = cv.take<double>((size_t)n * bs);   // the diagonal blocks' inverses (pre)
+  double* zd = cv.take<double>(n);                  // M^-1 v, and V y before M^-1 (pre)
+  const int pgrid = (npb + 255) / 256;
+  if (pre) {
+    k_block_inv<<<pgrid, 256, 0, st>>>(h->A, ld, npb, bs, Minv);
+    note_launch();
+  }
   float* bf = cv.take<float>(n);
   float* xf = cv.take<float>(n);
   float* xh = cv.take<float>(n);
@@ -1490,7 +1562,14 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
       for (; k < m && total < max_iter;) {
         double* vk = V + (size_t)k * n;
         double* w = V + (size_t)(k + 1) * n;
-        O3G_TRY(matvec(vk, nullptr, w, nullptr));
+        if (pre) {
+          // right preconditioning: w = A M^-1 v_k, so the residual stays the system's own
+          k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, vk, zd, n, 0);
+          note_launch();
+          O3G_TRY(matvec(zd, nullptr, w, nullptr));
+        } else {
+          O3G_TRY(matvec(vk, nullptr, w, nullptr));
+        }
         // classical Gram-Schmidt, twice
         for (int pass = 0; pass < 2; ++pass) gs_pass(V, n, k + 1, w, hd + (size_t)pass * (m + 1), kpart, st);
         norm_partials(w, n, npart, st);
@@ -1528,8 +1607,16 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
         y[i] = Hat(i, i) != 0.0 ? sacc / Hat(i, i) : 0.0;
       }
       O3G_CUDA_TRY(cudaMemcpyAsync(hd, y.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
-      k_kry_update<<<nrb, 256, 0, st>>>(V, n, k, hd, 1.0, xd);
-      note_launch();
+      if (pre) {
+        // x += M^-1 (V y)
+        O3G_CUDA_TRY(cudaMemsetAsync(zd, 0, (size_t)n * 8, st));
+        k_kry_update<<<nrb, 256, 0, st>>>(V, n, k, hd, 1.0, zd);
+        k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, zd, xd, n, 1);
+        note_launch(2);
+      } else {
+        k_kry_update<<<nrb, 256, 0, st>>>(V, n, k, hd, 1.0, xd);
+        note_launch();
+      }
     }
   }
   tm.end(st);
@@ -2045,9 +2132,12 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
   const int nrb = (n + 255) / 256;
   const size_t kn = (size_t)KM * n;
   const int nkb = (n + kKrylovRows - 1) / kKrylovRows;
+  const int bs = h->bs, npb = n / bs, pgrid = (npb + 255) / 256;
+  const bool pre = bs > 1;   // right-preconditioned by the diagonal blocks, as o3g_bem_solve_gmres
   const size_t need = align_up(kn * (m + 1) * 8) + 2 * align_up(kn * 8) + 3 * align_up(kn * 4) +
                       align_up((size_t)ncb * kn * 8) + align_up((size_t)KM * nrb * 8) +
-                      align_up((size_t)KM * 2 * (m + 1) * 8) + 2 * align_up((size_t)nkb * (m + 1) * 8);
+                      align_up((size_t)KM * 2 * (m + 1) * 8) + 2 * align_up((size_t)nkb * (m + 1) * 8) +
+                      align_up((size_t)n * bs * 8) + align_up(kn * 8);
   O3G_TRY(bem_scratch(h, need));
   Carve cv(h->scratch);
   double* V = cv.take<double>(kn * (m + 1));     // basis of column c at V + c (m+1) n
@@ -2061,7 +2151,13 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
   double* hd = cv.take<double>((size_t)KM * 2 * (m + 1));
   double* kpart = cv.take<double>((size_t)nkb * (m + 1));
   double* npart = cv.take<double>((size_t)nkb * (m + 1));
+  double* Minv = cv.take<double>((size_t)n * bs);
+  double* zb = cv.take<double>(kn);   // per column: M^-1 v, and V y before M^-1
   std::vector<double> hnp((size_t)nkb);
+  if (pre) {
+    k_block_inv<<<pgrid, 256, 0, st>>>(h->A, h->ld, npb, bs, Minv);
+    note_launch();
+  }
   const cudaMemcpyKind h2d = mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const cudaMemcpyKind d2h = mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   bool all_converged = true;
@@ -2151,6 +2247,11 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
         for (int q = 0; q < (int)act.size(); ++q) {
           xin.p[q] = Vc(act[q], R[act[q]].k);
           wout.p[q] = Vc(act[q], R[act[q]].k + 1);
+          if (pre) {
+            k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, xin.p[q], zb + (size_t)q * n, n, 0);
+            note_launch();
+            xin.p[q] = zb + (size_t)q * n;
+          }
         }
         O3G_TRY(matvec_multi(h, (int)act.size(), xin, none, wout, xh, xl, part, nrm, nullptr, st));
       }
@@ -2197,8 +2298,16 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
             s.y[i] = Hat(i, i) != 0.0 ? sacc / Hat(i, i) : 0.0;
           }
           O3G_CUDA_TRY(cudaMemcpyAsync(hc_d, s.y.data(), (size_t)kk * 8, cudaMemcpyHostToDevice, st));
-          k_kry_update<<<nrb, 256, 0, st>>>(Vb, n, kk, hc_d, 1.0, xd + (size_t)c * n);
-          note_launch();
+          if (pre) {
+            double* z = zb + (size_t)c * n;
+            O3G_CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)n * 8, st));
+            k_kry_update<<<nrb, 256, 0, st>>>(Vb, n, kk, hc_d, 1.0, z);
+            k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, z, xd + (size_t)c * n, n, 1);
+            note_launch(2);
+          } else {
+            k_kry_update<<<nrb, 256, 0, st>>>(Vb, n, kk, hc_d, 1.0, xd + (size_t)c * n);
+            note_launch();
+          }
           s.fresh = true;
         }
       }

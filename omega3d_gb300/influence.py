@@ -492,7 +492,9 @@ class BEM:
         self.factored = False
 
     def assemble(self, src_arrays, targ_arrays, nunk, is_self, rstart=0, cstart=0, maxlev=3, stream=None):
-        """Coefficients.h:169 written straight into the system matrix at (rstart, cstart)."""
+        """Coefficients.h:169 written straight into the system matrix at (rstart, cstart).
+        A surface's block on itself on the diagonal also sets the unknowns per panel, so
+        that GMRES preconditions with the panels' diagonal blocks (set_unknowns_per_panel)."""
         base, ld = self.matrix()
         s = surface_struct(src_arrays)
         t = surface_struct(targ_arrays)
@@ -500,6 +502,12 @@ class BEM:
         L.check(L.lib().o3g_panels_on_panels_coeff(maxlev, nunk, int(is_self), ctypes.byref(s), ctypes.byref(t),
                                                    base + 4 * (cstart * ld + rstart), ld, h),
                 "o3g_panels_on_panels_coeff")
+        if is_self and rstart == cstart and rstart % nunk == 0 and self.n % nunk == 0:
+            self.set_unknowns_per_panel(nunk)
+
+    def set_unknowns_per_panel(self, bs):
+        """Block size of the GMRES preconditioner (1 = none; o3g_bem_set_unknowns_per_panel)."""
+        L.check(L.lib().o3g_bem_set_unknowns_per_panel(self.h, int(bs)), "o3g_bem_set_unknowns_per_panel")
 
     def set_rhs(self, cstart, b):
         self.b[cstart:cstart + len(b)] = _np_host(b)
