@@ -772,15 +772,21 @@ struct PairKernel {
   }
 };
 
-// Chooses the source split so that the grid covers >= ~6 waves of resident blocks.
-inline void plan_pair(int ns, int nt, int tpt, int slots, PairPlan* p) {
+// Chooses the source split so that the grid covers >= `waves` waves of resident blocks.
+// The blocks' work differs (near- and far-field tiles), so the last wave leaves SMs idle;
+// more, shorter blocks shrink that tail.  Measured on the 262,144-particle Gaussian cloud
+// (compensated kernel, one GB300): 6 waves 116.7 ms, 12 113.2, 24 111.8, 48 110.8, 96
+// 110.2 ms, while the per-split partial sums the reduction reads grow with the split
+// count (29 splits, 730 MB, at 96 waves).  The allocating entry points use kPairWaves.
+constexpr int kPairWaves = 48;
+inline void plan_pair(int ns, int nt, int tpt, int slots, PairPlan* p, int waves = 6) {
   p->tpt = tpt;
   p->ntiles = (ns + kBlock - 1) / kBlock;
   p->ns_pad = p->ntiles * kBlock;
   const int tchunk = kBlock * tpt;
   p->tblocks = (nt + tchunk - 1) / tchunk;
   p->nt_pad = p->tblocks * tchunk;
-  const long want = 6L * (slots > 0 ? slots : 1);
+  const long want = (long)waves * (slots > 0 ? slots : 1);
   long nsplit = (want + p->tblocks - 1) / p->tblocks;
   const long max_split = p->ntiles >= 2 ? p->ntiles / 2 : 1;
   if (nsplit > max_split) nsplit = max_split;
@@ -807,7 +813,7 @@ int32_t run_points_points(int ns, const I* sx, const I* sy, const I* sz, const I
   int nb = 0;
   O3G_TRY(occupancy_blocks(PairKernel<C, MODE, GRADS, HAVE_TR, TPT, T, O>::ptr(), kBlock, &nb));
   PairPlan pl;
-  plan_pair(ns, nt, TPT, nb * df.num_sms, &pl);
+  plan_pair(ns, nt, TPT, nb * df.num_sms, &pl, kPairWaves);
   const int nsp = same ? (pl.ns_pad > pl.nt_pad ? pl.ns_pad : pl.nt_pad) : pl.ns_pad;
   size_t bytes = 2 * align_up((size_t)nsp * sizeof(V4<T>));
   if (!same) bytes += align_up((size_t)pl.nt_pad * sizeof(V4<T>));
