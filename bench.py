@@ -193,6 +193,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def bem_rates(n, assemble_ms, factor_ms):
+    """The assembly's rate against the HBM roof (it writes the n x n FP32 matrix once: 4 n^2
+    algorithmic bytes) and the factorisation's effective rate (2/3 n^3 flops)."""
+    out = {"assemble_gbs": 4.0 * n * n / (assemble_ms * 1e-3) / 1e9,
+           "factor_tflops_effective": (2.0 / 3.0) * float(n) ** 3 / (factor_ms * 1e-3) / 1e12}
+    pk = measured_peaks()
+    if pk.get("hbm_gbs"):
+        out["assemble_frac_of_hbm"] = out["assemble_gbs"] / pk["hbm_gbs"]
+    return out
+
+
 def bench_bem(args, G, torch, W, fp64=True):
     """BEM on a sphere: unit sphere from 5 icosahedral refinements (20,480 panels), freestream
     (1,0,0), 100,000 particles in the shell 1.02 < r < 1.5 (seed 3); RHS from the particles
@@ -232,6 +243,7 @@ def bench_bem(args, G, torch, W, fp64=True):
                    "assemble_ms": e[1].elapsed_time(e[2]), "factor_ms": e[2].elapsed_time(e[3]),
                    "solve_ms": e[3].elapsed_time(e[4]), "refinements": bem.iters, "relres": bem.relres,
                    "total_ms": e[0].elapsed_time(e[4])}
+            res.update(bem_rates(n, res["assemble_ms"], res["factor_ms"]))
             # the reference's own method on the same assembled matrix: GMRES, no factorisation
             e[5].record()
             xg = bem.solve(rhs, tol=1e-10, max_iter=300, method="gmres")

@@ -99,3 +99,15 @@ def test_guarded_section_reports_errors_in_the_line():
     out = bench.guarded(broken)
     assert out == {"error": "RuntimeError: o3g_batch_run failed: timeout"}
     json.dumps(out)
+
+
+def test_bem_rates_are_the_algorithmic_figures():
+    """The BEM section's assembly rate counts the matrix written once (4 n^2 bytes) and the
+    factorisation's effective rate 2/3 n^3 flops."""
+    import bench
+    r = bench.bem_rates(40960, 8.0, 280.0)
+    assert abs(r["assemble_gbs"] - 4.0 * 40960 ** 2 / 8.0e-3 / 1e9) < 1e-9
+    assert abs(r["factor_tflops_effective"] - (2.0 / 3.0) * 40960.0 ** 3 / 0.28 / 1e12) < 1e-9
+    pk = bench.measured_peaks()
+    if pk.get("hbm_gbs"):
+        assert abs(r["assemble_frac_of_hbm"] - r["assemble_gbs"] / pk["hbm_gbs"]) < 1e-12
