@@ -220,7 +220,14 @@ __global__ void __launch_bounds__(kPB) k_panpt(const PanelFar* __restrict__ far,
       } else {
         const PanelNear nr = nearr[(size_t)tile * kPB + jj];
         const Tri root{nr.a.x, nr.a.y, nr.a.z, nr.a.w, nr.b.x, nr.b.y, nr.b.z, nr.b.w, nr.d.x, nr.d.y, 0};
-        subdivide<GRADS, SRC, ACC>(px, py, pz, root, f.s.x, f.s.y, f.s.z, f.s.w, maxlev, a);
+        // the out-of-line subdivision works on a copy of the sums (in local memory); handing
+        // it `a` itself would put every far pair's sums in local memory too
+        float as[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) as[c] = a[c];
+        subdivide<GRADS, SRC, ACC>(px, py, pz, root, f.s.x, f.s.y, f.s.z, f.s.w, maxlev, as);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) a[c] = as[c];
       }
     }
     if (ACC) fold_tile<NC>(a, hi, lo);
@@ -279,7 +286,12 @@ __global__ void __launch_bounds__(kPB) k_ptpan(const PanelFar* __restrict__ far,
         leaf<false, false, ACC>(p.x, p.y, p.z, f.c.x, f.c.y, f.c.z, w.x, w.y, w.z, 0.f, a);
       } else {
         const Tri root{nr.a.x, nr.a.y, nr.a.z, nr.a.w, nr.b.x, nr.b.y, nr.b.z, nr.b.w, nr.d.x, nr.d.y, 0};
-        subdivide<false, false, ACC>(p.x, p.y, p.z, root, w.x, w.y, w.z, 0.f, maxlev, a);
+        float as[3];   // a copy for the out-of-line subdivision, as in k_panpt
+#pragma unroll
+        for (int c = 0; c < 3; ++c) as[c] = a[c];
+        subdivide<false, false, ACC>(p.x, p.y, p.z, root, w.x, w.y, w.z, 0.f, maxlev, as);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a[c] = as[c];
       }
     }
     if (ACC) fold_tile<3>(a, hi, lo);
