@@ -1385,20 +1385,23 @@ __global__ void k_kry_scale(double* w, int n, double s) {
   if (i < n) w[i] *= s;
 }
 
-// Block-Jacobi preconditioner of GMRES: the inverses (FP64) of the bs x bs diagonal blocks
+// Block-Jacobi preconditioner of GMRES: the inverses (FP64) of the BS x BS diagonal blocks
 // of A, one per panel (the panel's self-influence, Coefficients.h:414-436, when the blocks
 // are surfaces on themselves).  A block that is singular or not finite gets the identity.
-// Minv[p] is row-major.
-__global__ void k_block_inv(const float* __restrict__ A, long long ld, int nb, int bs, double* __restrict__ Minv) {
+// Minv[p] is row-major.  BS is a template argument so the blocks stay in registers.
+template <int BS>
+__global__ void k_block_inv(const float* __restrict__ A, long long ld, int nb, double* __restrict__ Minv) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nb) return;
   double a[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
-  const size_t o = (size_t)p * bs;
-  for (int r = 0; r < bs; ++r)
-    for (int c = 0; c < bs; ++c) a[r][c] = (double)A[(o + c) * ld + o + r];
+  const size_t o = (size_t)p * BS;
+#pragma unroll
+  for (int r = 0; r < BS; ++r)
+#pragma unroll
+    for (int c = 0; c < BS; ++c) a[r][c] = (double)A[(o + c) * ld + o + r];
   double inv[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
-  // cofactors of the 3 x 3 (a 1 x 1 or 2 x 2 block sits in the leading corner of an
-  // identity, so the same formula serves)
+  // cofactors of the 3 x 3 (a 2 x 2 block sits in the leading corner of an identity, so
+  // the same formula serves)
   const double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
   const double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
   const double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
@@ -1415,24 +1418,44 @@ __global__ void k_block_inv(const float* __restrict__ A, long long ld, int nb, i
     inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
     inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * id;
   }
-  for (int r = 0; r < bs; ++r)
-    for (int c = 0; c < bs; ++c) Minv[(size_t)p * bs * bs + r * bs + c] = inv[r][c];
+#pragma unroll
+  for (int r = 0; r < BS; ++r)
+#pragma unroll
+    for (int c = 0; c < BS; ++c) Minv[(size_t)p * BS * BS + r * BS + c] = inv[r][c];
 }
-// out = M^-1 in (acc = 0) or out += M^-1 in (acc = 1), K vectors of n (blockIdx.y)
-__global__ void k_block_apply(const double* __restrict__ Minv, int nb, int bs, const double* __restrict__ in,
-                              double* __restrict__ out, int n, int acc) {
+// out = M^-1 in (acc = 0) or out += M^-1 in (acc = 1)
+template <int BS>
+__global__ void k_block_apply(const double* __restrict__ Minv, int nb, const double* __restrict__ in,
+                              double* __restrict__ out, int acc) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nb) return;
-  const double* x = in + (size_t)blockIdx.y * n + (size_t)p * bs;
-  double* y = out + (size_t)blockIdx.y * n + (size_t)p * bs;
-  const double* M = Minv + (size_t)p * bs * bs;
-  double v[3] = {0.0, 0.0, 0.0};
-  for (int c = 0; c < bs; ++c) v[c] = x[c];
-  for (int r = 0; r < bs; ++r) {
+  const double* x = in + (size_t)p * BS;
+  double* y = out + (size_t)p * BS;
+  const double* M = Minv + (size_t)p * BS * BS;
+  double v[BS];
+#pragma unroll
+  for (int c = 0; c < BS; ++c) v[c] = x[c];
+#pragma unroll
+  for (int r = 0; r < BS; ++r) {
     double t = 0.0;
-    for (int c = 0; c < bs; ++c) t += M[r * bs + c] * v[c];
+#pragma unroll
+    for (int c = 0; c < BS; ++c) t += M[r * BS + c] * v[c];
     y[r] = acc ? y[r] + t : t;
   }
+}
+// launches for the unknowns per panel (2 or 3)
+static void block_inv(const float* A, long long ld, int nb, int bs, double* Minv, cudaStream_t st) {
+  const int g = (nb + 255) / 256;
+  if (bs == 2) k_block_inv<2><<<g, 256, 0, st>>>(A, ld, nb, Minv);
+  else         k_block_inv<3><<<g, 256, 0, st>>>(A, ld, nb, Minv);
+  note_launch();
+}
+static void block_apply(const double* Minv, int nb, int bs, const double* in, double* out, int acc,
+                        cudaStream_t st) {
+  const int g = (nb + 255) / 256;
+  if (bs == 2) k_block_apply<2><<<g, 256, 0, st>>>(Minv, nb, in, out, acc);
+  else         k_block_apply<3><<<g, 256, 0, st>>>(Minv, nb, in, out, acc);
+  note_launch();
 }
 
 namespace {
@@ -1496,11 +1519,7 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
   double* xd = cv.take<double>(n);
   double* Minv = cv.take<double>((size_t)n * bs);   // the diagonal blocks' inverses (pre)
   double* zd = cv.take<double>(n);                  // M^-1 v, and V y before M^-1 (pre)
-  const int pgrid = (npb + 255) / 256;
-  if (pre) {
-    k_block_inv<<<pgrid, 256, 0, st>>>(h->A, ld, npb, bs, Minv);
-    note_launch();
-  }
+  if (pre) block_inv(h->A, ld, npb, bs, Minv, st);
   float* bf = cv.take<float>(n);
   float* xf = cv.take<float>(n);
   float* xh = cv.take<float>(n);
@@ -1564,8 +1583,7 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
         double* w = V + (size_t)(k + 1) * n;
         if (pre) {
           // right preconditioning: w = A M^-1 v_k, so the residual stays the system's own
-          k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, vk, zd, n, 0);
-          note_launch();
+          block_apply(Minv, npb, bs, vk, zd, 0, st);
           O3G_TRY(matvec(zd, nullptr, w, nullptr));
         } else {
           O3G_TRY(matvec(vk, nullptr, w, nullptr));
@@ -1611,8 +1629,8 @@ extern "C" int32_t o3g_bem_solve_gmres(o3g_bem_t* h, const float* b, float* x, d
         // x += M^-1 (V y)
         O3G_CUDA_TRY(cudaMemsetAsync(zd, 0, (size_t)n * 8, st));
         k_kry_update<<<nrb, 256, 0, st>>>(V, n, k, hd, 1.0, zd);
-        k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, zd, xd, n, 1);
-        note_launch(2);
+        note_launch();
+        block_apply(Minv, npb, bs, zd, xd, 1, st);
       } else {
         k_kry_update<<<nrb, 256, 0, st>>>(V, n, k, hd, 1.0, xd);
         note_launch();
@@ -2132,7 +2150,7 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
   const int nrb = (n + 255) / 256;
   const size_t kn = (size_t)KM * n;
   const int nkb = (n + kKrylovRows - 1) / kKrylovRows;
-  const int bs = h->bs, npb = n / bs, pgrid = (npb + 255) / 256;
+  const int bs = h->bs, npb = n / bs;
   const bool pre = bs > 1;   // right-preconditioned by the diagonal blocks, as o3g_bem_solve_gmres
   const size_t need = align_up(kn * (m + 1) * 8) + 2 * align_up(kn * 8) + 3 * align_up(kn * 4) +
                       align_up((size_t)ncb * kn * 8) + align_up((size_t)KM * nrb * 8) +
@@ -2154,10 +2172,7 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
   double* Minv = cv.take<double>((size_t)n * bs);
   double* zb = cv.take<double>(kn);   // per column: M^-1 v, and V y before M^-1
   std::vector<double> hnp((size_t)nkb);
-  if (pre) {
-    k_block_inv<<<pgrid, 256, 0, st>>>(h->A, h->ld, npb, bs, Minv);
-    note_launch();
-  }
+  if (pre) block_inv(h->A, h->ld, npb, bs, Minv, st);
   const cudaMemcpyKind h2d = mem == O3G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const cudaMemcpyKind d2h = mem == O3G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   bool all_converged = true;
@@ -2248,8 +2263,7 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
           xin.p[q] = Vc(act[q], R[act[q]].k);
           wout.p[q] = Vc(act[q], R[act[q]].k + 1);
           if (pre) {
-            k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, xin.p[q], zb + (size_t)q * n, n, 0);
-            note_launch();
+            block_apply(Minv, npb, bs, xin.p[q], zb + (size_t)q * n, 0, st);
             xin.p[q] = zb + (size_t)q * n;
           }
         }
@@ -2302,8 +2316,8 @@ extern "C" int32_t o3g_bem_solve_gmres_many(o3g_bem_t* h, int32_t nrhs, const fl
             double* z = zb + (size_t)c * n;
             O3G_CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)n * 8, st));
             k_kry_update<<<nrb, 256, 0, st>>>(Vb, n, kk, hc_d, 1.0, z);
-            k_block_apply<<<pgrid, 256, 0, st>>>(Minv, npb, bs, z, xd + (size_t)c * n, n, 1);
-            note_launch(2);
+            note_launch();
+            block_apply(Minv, npb, bs, z, xd + (size_t)c * n, 1, st);
           } else {
             k_kry_update<<<nrb, 256, 0, st>>>(Vb, n, kk, hc_d, 1.0, xd + (size_t)c * n);
             note_launch();
